@@ -1,0 +1,136 @@
+/*
+ * refdrv.cpp -- driver for the reference build (test infrastructure).
+ *
+ * Runs the reference's own one-component loop (fJmodels.cpp:86-144) with the
+ * radial grid taken from the command line instead of SetGrid(200.), and dumps
+ * every intermediate at full precision so the oracle can be checked against
+ * the reference code itself.
+ *
+ *   refdrv <param file> <rmin> <rmax> <points file or -> <dump file>
+ *
+ * Points file lines: "P R z" (potential and gradient), "A R z vR vphi vz"
+ * (actions with Delta from the table, as df() does), "M R z" (rhofDF).
+ */
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+#include "Utils.h"
+#include "UtilsLeg.h"
+#include "readParam.h"
+#include "Potential.h"
+#include "models.h"
+#include "Delta.h"
+#include "Tabulate.h"
+#include "uvOrb.h"
+#include "DF.h"
+#include "Integ.h"
+#include "potLeg.h"
+#include "Stats.h"
+#include "writeOut.h"
+
+double ar[NR], Dgrid[NGRID], Egrid[NGRID];
+double ** __restrict phil, ** __restrict Pr, ** __restrict Pr2,
+       ** __restrict rhl, ** __restrict vrotl, ** __restrict sigRl,
+       ** __restrict sigpl, ** __restrict sigzl, ** __restrict sigRzl;
+FILE * __restrict f_lz;
+
+static FILE *out;
+static void dumpv(const char *name, const double *v, int n)
+{
+    fprintf(out, "%s %d\n", name, n);
+    for (int i = 0; i < n; i++) fprintf(out, "%.17g\n", v[i]);
+}
+static void dumpm(const char *name, double **m, int nx, int ny)
+{
+    fprintf(out, "%s %d\n", name, nx * ny);
+    for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++) fprintf(out, "%.17g\n", m[i][j]);
+}
+
+int main(int argc, char **argv)
+{
+    if (argc < 6) { fprintf(stderr, "usage: refdrv param rmin rmax points dump\n"); return 2; }
+    phil = mat<double>(NR, NPOLY); Pr = mat<double>(NR, NPOLY); Pr2 = mat<double>(NR, NPOLY);
+    rhl = mat<double>(NR, NPOLY); vrotl = mat<double>(NR, NPOLY);
+    sigRl = mat<double>(NR, NPOLY); sigpl = mat<double>(NR, NPOLY);
+    sigzl = mat<double>(NR, NPOLY); sigRzl = mat<double>(NR, NPOLY);
+    struct fJParams fJP = readParam(argv[1]);
+    double rmin = atof(argv[2]), rmax = atof(argv[3]);
+    for (int i = 0; i < NR; i++) ar[i] = pow(10., log10(rmin) + (log10(rmax) - log10(rmin)) * i / (NR - 1));
+    out = fopen(argv[5], "w");
+    f_lz = fopen("/dev/null", "w");
+    std::vector<std::vector<double>> pts;
+    if (strcmp(argv[4], "-")) {
+        std::ifstream pf(argv[4]);
+        std::string line;
+        while (std::getline(pf, line)) {
+            std::stringstream ss(line);
+            char t;
+            ss >> t;
+            std::vector<double> v{(double)t};
+            double x;
+            while (ss >> x) v.push_back(x);
+            if (v.size() > 1) pts.push_back(v);
+        }
+    }
+    dumpv("ar", ar, NR);
+
+    SetModel(fJP);
+    Potential p;
+    p.selectGuessRho(fJP.modName != "null" ? fJP.modName : "Hernquist");
+    p.computeGuessRhl();
+    p.computePhil();
+    dumpm("guess_rhl", rhl, NR, NPOLY);
+    dumpm("guess_phil", phil, NR, NPOLY);
+    dumpm("guess_Pr", Pr, NR, NPOLY);
+    dumpm("guess_Pr2", Pr2, NR, NPOLY);
+
+    std::vector<double> pv;
+    for (auto &v : pts)
+        if ((char)v[0] == 'P') { pv.push_back(p(v[1], v[2])); pv.push_back(p.dR(v[1], v[2])); pv.push_back(p.dz(v[1], v[2])); }
+    dumpv("pot_points", pv.data(), (int)pv.size());
+
+    tabulateDelta(&p);
+    dumpv("Egrid", Egrid, NGRID);
+    dumpv("Dgrid", Dgrid, NGRID);
+
+    setDF(&fJP, &p, 1);
+    std::vector<double> av, mv;
+    for (auto &v : pts) {
+        if ((char)v[0] == 'A') {
+            double x[3] = {v[1], v[2], p(v[1], v[2])}, vel[2] = {v[3], v[5]};
+            double H = .5 * (v[3] * v[3] + v[4] * v[4] + v[5] * v[5]) + x[2];
+            if (H >= 0) { av.push_back(-1); av.push_back(-1); continue; }
+            uvOrb o(Deltafn(H), v[1] * v[4], x[2], x, vel, &p);
+            av.push_back(o.Ju());
+            av.push_back(o.Jv());
+        } else if ((char)v[0] == 'M') {
+            double vr, sR, sp, sz, sRz;
+            double d = rhofDF(v[1], v[2], &p, &vr, &sR, &sp, &sz, &sRz);
+            double m6[6] = {d, vr, sR, sp, sz, sRz};
+            for (double q : m6) mv.push_back(q);
+        }
+    }
+    dumpv("actions", av.data(), (int)av.size());
+    dumpv("moments", mv.data(), (int)mv.size());
+    fflush(out);
+
+    for (int k = 0; k < fJP.itermax; k++) {
+        printf("\n Iter:%d\n", k);
+        computeNewPhi(&p, rhl, sigRl, sigpl, sigzl, sigRzl, vrotl);
+        char nm[64];
+        double **mats[9] = {rhl, vrotl, sigRl, sigpl, sigzl, sigRzl, phil, Pr, Pr2};
+        const char *names[9] = {"rhl", "vrotl", "sigRl", "sigpl", "sigzl", "sigRzl", "phil", "Pr", "Pr2"};
+        for (int q = 0; q < 9; q++) { snprintf(nm, sizeof nm, "it%d_%s", k, names[q]); dumpm(nm, mats[q], NR, NPOLY); }
+        fflush(out);
+        writeOut(fJP, k, &p);
+        vir2(&p);
+        fflush(stdout);
+    }
+    fclose(out);
+    return 0;
+}
