@@ -1,0 +1,101 @@
+"""ctypes declarations of include/fjgpu.h (the C ABI of libfjgpu.so)."""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfjgpu.so")
+
+DP = C.POINTER(C.c_double)
+
+FJ_OK = 0
+FJ_DF_DPL, FJ_DF_QUASIISO = 0, 1
+FJ_PREC_FP64, FJ_PREC_MIXED = 0, 1
+FJ_JQUAD_QAGS = 0
+FJ_GUESS = {"Hernquist": 0, "Isochrone": 1, "NFW": 2}
+
+
+class fj_potential(C.Structure):
+    _fields_ = [("nr", C.c_int), ("npoly", C.c_int), ("ar", C.c_void_p), ("phil", C.c_void_p),
+                ("Pr", C.c_void_p), ("Pr2", C.c_void_p)]
+
+
+class fj_delta_table(C.Structure):
+    _fields_ = [("ngrid", C.c_int), ("Egrid", C.c_void_p), ("Dgrid", C.c_void_p)]
+
+
+class fj_df_params(C.Structure):
+    _fields_ = [("kind", C.c_int)] + [(n, C.c_double) for n in
+                                      ("alpha", "beta", "J0", "mass", "dphi_h", "dz_h", "dphi_g", "dz_g", "chi", "k")]
+
+
+class fj_quad_rule(C.Structure):
+    _fields_ = [("nq", C.c_int), ("xq", DP), ("wq", DP), ("jquad", C.c_int), ("precision", C.c_int)]
+
+
+class fj_moment_stats(C.Structure):
+    _fields_ = [("nodes", C.c_longlong), ("bound", C.c_longlong), ("failures", C.c_longlong),
+                ("kernel_ms", C.c_double)]
+
+
+class fj_model_config(C.Structure):
+    _fields_ = [("nr", C.c_int), ("ngauss", C.c_int), ("npoly", C.c_int), ("ngrid", C.c_int),
+                ("rmin", C.c_double), ("rmax", C.c_double), ("guess", C.c_int),
+                ("mass", C.c_double), ("r0", C.c_double), ("q", C.c_double),
+                ("df", fj_df_params), ("rule", fj_quad_rule), ("itermax", C.c_int), ("tol", C.c_double)]
+
+
+class fj_model_result(C.Structure):
+    _fields_ = [(n, DP) for n in ("ar", "coef6", "phil", "Pr", "Pr2", "Egrid", "Dgrid", "grids6")] + [
+        ("vir7", C.c_double * 7), ("iterations", C.c_int), ("last_change", C.c_double),
+        ("bound", C.c_longlong), ("failures", C.c_longlong), ("wall_ms", C.c_double), ("kernel_ms", C.c_double)]
+
+
+P = C.POINTER
+CTX = C.c_void_p
+SIGNATURES = {
+    "fj_version": ([], C.c_char_p),
+    "fj_ctx_create": ([C.c_int, P(C.c_void_p)], C.c_int),
+    "fj_ctx_destroy": ([CTX], C.c_int),
+    "fj_ctx_set_stream": ([CTX, C.c_void_p], C.c_int),
+    "fj_ctx_synchronize": ([CTX], C.c_int),
+    "fj_last_error": ([CTX], C.c_char_p),
+    "fj_moments": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule), C.c_int,
+                    C.c_void_p, P(fj_moment_stats)], C.c_int),
+    "fj_moments_points": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule),
+                           C.c_void_p, C.c_int, C.c_void_p, P(fj_moment_stats)], C.c_int),
+    "fj_legendre_project": ([CTX, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "fj_poisson": ([CTX, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "fj_sum_potentials": ([CTX, C.c_int] + [C.c_void_p] * 9, C.c_int),
+    "fj_compute_new_phi": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule), C.c_int,
+                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, P(fj_moment_stats)], C.c_int),
+    "fj_actions": ([CTX, P(fj_potential), P(fj_delta_table), C.c_void_p, C.c_size_t, C.c_int, C.c_void_p], C.c_int),
+    "fj_potential_eval": ([CTX, P(fj_potential), C.c_void_p, C.c_size_t, C.c_void_p], C.c_int),
+    "fj_vir2": ([CTX, P(fj_potential), C.c_int, C.c_void_p, DP], C.c_int),
+    "fj_log_grid": ([C.c_double, C.c_double, C.c_int, DP], C.c_int),
+    "fj_gauleg": ([C.c_double, C.c_double, C.c_int, DP, DP], C.c_int),
+    "fj_guess_rhl": ([C.c_int, C.c_int, C.c_int, DP, C.c_int, C.c_double, C.c_double, C.c_double, DP], C.c_int),
+    "fj_tabulate_delta": ([P(fj_potential), C.c_int, DP, DP], C.c_int),
+    "fj_write_out": ([C.c_char_p, C.c_int, C.c_int, C.c_int, DP, DP, DP], C.c_int),
+    "fj_run_model": ([CTX, P(fj_model_config), P(fj_model_result)], C.c_int),
+}
+
+_lib = None
+
+
+def load(build_if_missing=True):
+    """Load libfjgpu.so (building it first when a source is newer).  Raises if it cannot."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        from . import build as _b
+        _b.build()
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"libfjgpu.so is missing at {LIB_PATH}; run python -m fjmodels_gb300.build")
+    lib = C.CDLL(LIB_PATH)
+    for name, (args, res) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib

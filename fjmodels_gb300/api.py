@@ -1,0 +1,305 @@
+"""Host-side mirror of the reference's interfaces over the C ABI.
+
+Names follow the reference: ``rhofDF`` grids (integ/Integ.cpp), ``computeNewPhi``
+(pot/potLeg.cpp), ``computePhil`` (pot/Potential.cpp), ``uvOrb`` actions
+(uvOrb/uvOrb.cpp), ``vir2`` (libs/Stats.cpp), ``writeOut`` (io/writeOut.cpp),
+``readParam`` (io/readParam.cpp).  Device arrays are torch CUDA tensors
+(float64, contiguous); torch only provides the memory and the stream.  There is
+no CPU fallback: every compute call goes to libfjgpu.so and raises if the
+library or the GPU is unavailable.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi as A
+
+# the reference's live velocity rule, include/GaussPts.h:79-88 (QUAD22 "rectangle method")
+XPT11 = np.array([-1., -0.50118723, -0.25118864, -0.12589254, -0.06309573,
+                  -0.03162278, -0.01584893, -0.00794328, -0.00398107, -0.00199526,
+                  -0.001, 0.001, 0.00199526, 0.00398107, 0.00794328,
+                  0.01584893, 0.03162278, 0.06309573, 0.12589254, 0.25118864,
+                  0.50118723, 1.])
+XW11 = np.array([0.49881277, 0.37440568, 0.18764735, 0.09404645, 0.04713488,
+                 0.0236234, 0.01183975, 0.00593393, 0.00297401, 0.00149054,
+                 0.00149763, 0.00149763, 0.00149054, 0.00297401, 0.00593393,
+                 0.01183975, 0.0236234, 0.04713488, 0.09404645, 0.18764735,
+                 0.37440568, 0.49881277])
+
+# DF slopes selected by model name (df/DF.cpp:40-43)
+MODEL_SLOPES = {"Hernquist": (1.667, 5.0), "Isochrone": (0.0, 5.0), "NFW": (1.667, 3.0)}
+
+
+class FJError(RuntimeError):
+    pass
+
+
+def _dp(a):
+    return a.ctypes.data_as(A.DP)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _ptr(t):
+    """Device pointer of a torch CUDA float64 tensor (or an int address)."""
+    if isinstance(t, int):
+        return t
+    if not t.is_cuda or not t.is_contiguous():
+        raise FJError("device arrays must be contiguous CUDA tensors")
+    return t.data_ptr()
+
+
+def tanh_sinh_rule(n=22, h=None):
+    """Symmetric n-point tanh-sinh rule on [-1,1] (Takahasi & Mori 1974):
+    x_k = tanh(pi/2 sinh(k h)), w_k = h pi/2 cosh(k h) / cosh^2(pi/2 sinh(k h)),
+    with k = -(n-1)/2 .. (n-1)/2 in steps of 1 and h chosen so the outermost
+    node sits at 1 - 1e-5.  Weights are renormalised to sum to 2."""
+    ks = np.arange(n) - (n - 1) / 2.0
+    if h is None:
+        kmax = ks[-1]
+        t = np.arctanh(1 - 1e-5) * 2 / np.pi
+        h = np.arcsinh(t) / kmax
+    u = np.pi / 2 * np.sinh(ks * h)
+    x = np.tanh(u)
+    w = h * np.pi / 2 * np.cosh(ks * h) / np.cosh(u) ** 2
+    return x, w * (2.0 / w.sum())
+
+
+class DFParams:
+    """DF of one component (df/DF.cpp:36-63): slopes from the model name, J0 = sqrt(M r0)."""
+
+    def __init__(self, model="Hernquist", dphi_h=0.55, dz_h=0.55, dphi_g=1.0, dz_g=1.0, chi=0.0, mass=1.0,
+                 r0=1.0, k=0.5, kind=A.FJ_DF_DPL, alpha=None, beta=None):
+        a, b = MODEL_SLOPES.get(model, (alpha, beta))
+        if alpha is not None and model not in MODEL_SLOPES:
+            a, b = alpha, beta
+        if a is None or b is None:
+            raise FJError("either set a known model or alpha and beta")
+        self.c = A.fj_df_params(kind, a, b, float(np.sqrt(mass * r0)), mass, dphi_h, dz_h, dphi_g, dz_g, chi, k)
+        self.model, self.mass, self.r0 = model, mass, r0
+
+
+class Rule:
+    """Velocity rule (same on the three axes) + momentum-integral rule + arithmetic."""
+
+    def __init__(self, xq=XPT11, wq=XW11, jquad=A.FJ_JQUAD_QAGS, precision=A.FJ_PREC_FP64):
+        self.xq, self.wq = _f64(xq), _f64(wq)
+        self.c = A.fj_quad_rule(len(self.xq), _dp(self.xq), _dp(self.wq), jquad, precision)
+
+
+class Context:
+    """One CUDA context/stream of libfjgpu (fj_ctx)."""
+
+    def __init__(self, device=0):
+        self.lib = A.load()
+        h = C.c_void_p()
+        rc = self.lib.fj_ctx_create(device, C.byref(h))
+        if rc != A.FJ_OK:
+            raise FJError(f"fj_ctx_create failed ({rc}): no usable CUDA device {device}")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.fj_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != A.FJ_OK:
+            raise FJError(f"{what} failed ({rc}): {self.lib.fj_last_error(self.h).decode()}")
+
+    def sync(self):
+        self._check(self.lib.fj_ctx_synchronize(self.h), "synchronize")
+
+    # ---------------------------------------------------------------- structs
+    @staticmethod
+    def potential(ar, phil, Pr, Pr2):
+        npoly = phil.numel() // ar.numel()
+        return A.fj_potential(ar.numel(), npoly, _ptr(ar), _ptr(phil), _ptr(Pr), _ptr(Pr2))
+
+    @staticmethod
+    def delta(Egrid, Dgrid):
+        return A.fj_delta_table(Egrid.numel(), _ptr(Egrid), _ptr(Dgrid))
+
+    # ---------------------------------------------------------------- hot path
+    def moments(self, pot, delta, df, rule, ngauss, grids6):
+        """rhofDF over the meridional grid (pot/potLeg.cpp:54-58)."""
+        st = A.fj_moment_stats()
+        self._check(self.lib.fj_moments(self.h, C.byref(pot), C.byref(delta), C.byref(df.c), C.byref(rule.c),
+                                        ngauss, _ptr(grids6), C.byref(st)), "fj_moments")
+        return st
+
+    def moments_points(self, pot, delta, df, rule, Rz, out6):
+        st = A.fj_moment_stats()
+        self._check(self.lib.fj_moments_points(self.h, C.byref(pot), C.byref(delta), C.byref(df.c),
+                                               C.byref(rule.c), _ptr(Rz), Rz.shape[0], _ptr(out6), C.byref(st)),
+                    "fj_moments_points")
+        return st
+
+    def legendre_project(self, nr, ngauss, npoly, ar, grids6, coef6):
+        self._check(self.lib.fj_legendre_project(self.h, nr, ngauss, npoly, _ptr(ar), _ptr(grids6), _ptr(coef6)),
+                    "fj_legendre_project")
+
+    def computePhil(self, ar, rhl, phil, Pr, Pr2):
+        nr = ar.numel()
+        self._check(self.lib.fj_poisson(self.h, nr, rhl.numel() // nr, _ptr(ar), _ptr(rhl), _ptr(phil), _ptr(Pr),
+                                        _ptr(Pr2)), "fj_poisson")
+
+    def updatePhil(self, a3, b3, out3):
+        n = a3[0].numel()
+        self._check(self.lib.fj_sum_potentials(self.h, n, *[_ptr(t) for t in (*a3, *b3, *out3)]),
+                    "fj_sum_potentials")
+
+    def computeNewPhi(self, pot, delta, df, rule, ngauss, grids6, coef6, phil, Pr, Pr2):
+        st = A.fj_moment_stats()
+        self._check(self.lib.fj_compute_new_phi(self.h, C.byref(pot), C.byref(delta), C.byref(df.c),
+                                                C.byref(rule.c), ngauss, _ptr(grids6), _ptr(coef6), _ptr(phil),
+                                                _ptr(Pr), _ptr(Pr2), C.byref(st)), "fj_compute_new_phi")
+        return st
+
+    def uvOrb_actions(self, pot, delta, pts, out, jquad=A.FJ_JQUAD_QAGS):
+        self._check(self.lib.fj_actions(self.h, C.byref(pot), C.byref(delta), _ptr(pts), pts.shape[0], jquad,
+                                        _ptr(out)), "fj_actions")
+
+    def potential_eval(self, pot, Rz, out):
+        self._check(self.lib.fj_potential_eval(self.h, C.byref(pot), _ptr(Rz), Rz.shape[0], _ptr(out)),
+                    "fj_potential_eval")
+
+    def vir2(self, pot, ngauss, coef6):
+        out = np.zeros(7)
+        self._check(self.lib.fj_vir2(self.h, C.byref(pot), ngauss, _ptr(coef6), _dp(out)), "fj_vir2")
+        return dict(zip(("KRR", "Kzz", "WRR", "Wzz", "pot", "mass_pr", "mass_sum"), out))
+
+    # ---------------------------------------------------------------- whole model
+    def run_model(self, nr, ngauss, npoly, rmin, rmax, df, rule, itermax, tol=0.0, ngrid=30, q=1.0,
+                  keep_grids=False):
+        """One-component self-consistent model (fJmodels.cpp:86-144) with host buffers."""
+        cfg = A.fj_model_config(nr, ngauss, npoly, ngrid, rmin, rmax, A.FJ_GUESS.get(df.model, 0), df.mass, df.r0,
+                                q, df.c, rule.c, itermax, tol)
+        out = {"ar": np.zeros(nr), "coef6": np.zeros((6, nr, npoly)), "phil": np.zeros((nr, npoly)),
+               "Pr": np.zeros((nr, npoly)), "Pr2": np.zeros((nr, npoly)), "Egrid": np.zeros(ngrid),
+               "Dgrid": np.zeros(ngrid)}
+        grids = np.zeros((6, nr, ngauss)) if keep_grids else None
+        res = A.fj_model_result(*[_dp(out[k]) for k in ("ar", "coef6", "phil", "Pr", "Pr2", "Egrid", "Dgrid")],
+                                _dp(grids) if keep_grids else None)
+        self._check(self.lib.fj_run_model(self.h, C.byref(cfg), C.byref(res)), "fj_run_model")
+        out.update(vir7=np.array(res.vir7[:]), iterations=res.iterations, last_change=res.last_change,
+                   bound=res.bound, failures=res.failures, wall_ms=res.wall_ms, kernel_ms=res.kernel_ms)
+        if keep_grids:
+            out["grids6"] = grids
+        return out
+
+
+# -------------------------------------------------------------- host setup
+def log_grid(rmin, rmax, n):
+    ar = np.zeros(n)
+    if A.load().fj_log_grid(rmin, rmax, n, _dp(ar)) != A.FJ_OK:
+        raise FJError("log_grid: bad arguments")
+    return ar
+
+
+def gauleg(x1, x2, n):
+    x, w = np.zeros(n), np.zeros(n)
+    A.load().fj_gauleg(x1, x2, n, _dp(x), _dp(w))
+    return x, w
+
+
+def guess_rhl(ar, ngauss, npoly, model="Hernquist", mass=1.0, r0=1.0, q=1.0):
+    ar = _f64(ar)
+    rhl = np.zeros((len(ar), npoly))
+    if A.load().fj_guess_rhl(len(ar), ngauss, npoly, _dp(ar), A.FJ_GUESS[model], mass, r0, q, _dp(rhl)) != A.FJ_OK:
+        raise FJError("guess_rhl: bad arguments")
+    return rhl
+
+
+def tabulate_delta(ar, phil, Pr, Pr2, ngrid=30):
+    """tabulateDelta on host tables (delta/tabulate.cpp:13-38)."""
+    ar, phil, Pr, Pr2 = (_f64(x) for x in (ar, phil, Pr, Pr2))
+    pot = A.fj_potential(len(ar), phil.size // len(ar), ar.ctypes.data, phil.ctypes.data, Pr.ctypes.data,
+                         Pr2.ctypes.data)
+    E, D = np.zeros(ngrid), np.zeros(ngrid)
+    rc = A.load().fj_tabulate_delta(C.byref(pot), ngrid, _dp(E), _dp(D))
+    return E, D, rc
+
+
+def writeOut(path, ar, mats9, ngauss, header):
+    """_writeOut (io/writeOut.cpp:74-138).  header = (dphi_h, dz_h, dphi_g, dz_g, chi, mass, r0, A, B)."""
+    ar = _f64(ar)
+    m = _f64(mats9)
+    nr = len(ar)
+    npoly = m.size // (9 * nr)
+    hdr = np.zeros(10)
+    hdr[:9] = header
+    rc = A.load().fj_write_out(path.encode(), nr, npoly, ngauss, _dp(hdr), _dp(ar), _dp(m))
+    if rc != A.FJ_OK:
+        raise FJError(f"writeOut failed ({rc}) for {path}")
+
+
+def _to_string(x, eps=2):
+    return f"{x:.{eps}f}"
+
+
+def composeName(model, dphi_h, dz_h, dphi_g, dz_g, it, comp=1, outName="null"):
+    """Output file name of io/writeOut.cpp:22-56 and 87-88."""
+    if outName != "null":
+        name = f"{outName}_{it}.out"
+    else:
+        name = model[:5] + "_" + "_".join(_to_string(v) for v in (dphi_h, dz_h, dphi_g, dz_g)) + f"_{it}.out"
+    if comp == 2 and outName == "null":
+        name += "2c"
+    return os.path.join("models", name)
+
+
+UNSET = -999.0
+
+
+def readParam(path="param.txt"):
+    """Key/value parameter file of io/readParam.cpp:31-111 (unknown keys ignored,
+    comment/blank/indented lines skipped); returns (params dict, component count)."""
+    keys = {"itermax": "itermax", "model": "modName", "A": "alpha", "B": "beta", "outfile": "outName",
+            "chi": "chi", "h(J):dphi": "dphi_h_in", "h(J):dz": "dz_h_in", "g(J):dphi": "dphi_g_in",
+            "g(J):dz": "dz_g_in", "mass": "mass", "r0": "r0", "q": "q"}
+    p = {"itermax": 5, "modName": "null", "outName": "null"}
+    for v in ("alpha", "beta", "dphi_h_in", "dz_h_in", "dphi_g_in", "dz_g_in", "chi", "mass", "r0", "q"):
+        p[v] = UNSET
+        p[v + "_2" if not v.endswith("_in") else v + "2"] = UNSET
+    p["modName2"] = p["outName2"] = "null"
+    if not os.path.exists(path):
+        raise FJError(f"ERROR in opening parameter file {path}! Are you sure the file exists?")
+    for line in open(path):
+        line = line.rstrip("\n")
+        if not line or line[0] in "# \t":
+            continue
+        parts = line.split()
+        key, val = parts[0], (parts[1] if len(parts) > 1 else None)
+        two = key.startswith("2:")
+        base = key[2:] if two else key
+        if base not in keys or val is None:
+            continue
+        field = keys[base]
+        if two:
+            field = {"modName": "modName2", "outName": "outName2"}.get(field, field + ("2" if field.endswith("_in") else "_2"))
+        if field.startswith(("modName", "outName")):
+            p[field] = val
+        else:
+            p[field] = int(float(val)) if field == "itermax" else float(val)
+    one = ((p["modName"] != "null" or (p["alpha"] != UNSET and p["beta"] != UNSET)) and
+           all(p[k] != UNSET for k in ("chi", "mass", "r0", "q", "dphi_h_in", "dz_h_in", "dphi_g_in", "dz_g_in")))
+    if not one:
+        raise FJError("ERROR: parameterfile must contain at least one component!")
+    comps = 1
+    if p["modName2"] != "null" or (p["alpha_2"] != UNSET and p["beta_2"] != UNSET):
+        if all(p[k] != UNSET for k in ("chi_2", "mass_2", "r0_2", "q_2", "dphi_h_in2", "dz_h_in2", "dphi_g_in2",
+                                        "dz_g_in2")):
+            comps = 2
+        else:
+            raise FJError("ERROR in parameterfile: second components is missing some parameter to initialize!")
+    return p, comps

@@ -1,0 +1,810 @@
+// fj_api.cu -- the C ABI of include/fjgpu.h: context, cached rule tables,
+// launches of the hot path, and the host-side setup the reference also runs
+// once on the host (grid, guess density, focal-distance table, coefficient
+// file writer) plus the one-component self-consistent loop.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/fjgpu.h"
+#include "fj_internal.h"
+
+// the host-only functors below instantiate the __host__ __device__ Brent template on the host only
+#pragma nv_diag_suppress 20011, 20014
+
+using namespace fj;
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+struct fj_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own = nullptr;
+    std::string err;
+    DevBuf partial, counters, poisson_ws, rule, misc;
+    std::map<int, DevBuf> gauss_nodes;                 // ngauss -> [2][ngauss] (ci, wi)
+    std::map<std::pair<int, int>, DevBuf> poly;        // (ngauss, npoly) -> [npoly][ngauss]
+    std::map<int, DevBuf> gl_rules;                    // jquad -> [2][n]
+    std::vector<double> rule_host;                     // last uploaded velocity rule
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+int fail(fj_ctx *c, int code, const std::string &msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(fj_ctx *c, cudaError_t e, const char *what)
+{
+    return fail(c, FJ_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define FJ_CUDA(call)                                      \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+int ensure(fj_ctx *ctx, DevBuf &b, size_t bytes)
+{
+    if (b.bytes >= bytes) return FJ_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) return fail(ctx, FJ_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    b.bytes = bytes;
+    return FJ_OK;
+}
+
+// Gauss-Legendre on [x1,x2] with the iteration of include/UtilsLeg.h:18-39
+void gauleg_host(double x1, double x2, int n, double *x, double *w)
+{
+    const double eps = 3.0e-11;
+    const int m = (n + 1) / 2;
+    const double xm = 0.5 * (x2 + x1), xl = 0.5 * (x2 - x1);
+    double pp = 0, z1;
+    for (int i = 0; i < m; i++) {
+        double z = cos(3.141592654 * (i + 0.75) / (n + 0.5));
+        do {
+            double p1 = 1, p2 = 0, p3;
+            for (int j = 0; j < n; j++) {
+                p3 = p2;
+                p2 = p1;
+                p1 = ((2 * (j + 1) - 1) * z * p2 - j * p3) / (double)(j + 1);
+            }
+            pp = n * (z * p1 - p2) / (z * z - 1.0);
+            z1 = z;
+            z = z1 - p1 / pp;
+        } while (fabs(z - z1) > eps);
+        x[i] = xm - xl * z;
+        x[n - i - 1] = xm + xl * z;
+        w[i] = 2 * xl / ((1 - z * z) * pp * pp);
+        w[n - i - 1] = w[i];
+    }
+}
+
+void evenlegend_host(int npoly, double c, double *pol)
+{
+    const double c2 = c * c;
+    pol[0] = 1;
+    if (npoly < 2) return;
+    pol[1] = 1.5 * c2 - .5;
+    for (int np = 2; np < npoly; np++) pol[np] = evenleg_next(np, c2, pol[np - 2], pol[np - 1]);
+}
+
+int gauss_nodes(fj_ctx *ctx, int ngauss, const double **dptr)
+{
+    auto it = ctx->gauss_nodes.find(ngauss);
+    if (it == ctx->gauss_nodes.end()) {
+        std::vector<double> h(2 * ngauss);
+        gauleg_host(0, 1, ngauss, h.data(), h.data() + ngauss);
+        DevBuf b;
+        int rc = ensure(ctx, b, h.size() * sizeof(double));
+        if (rc) return rc;
+        FJ_CUDA(cudaMemcpy(b.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+        it = ctx->gauss_nodes.emplace(ngauss, b).first;
+    }
+    *dptr = (const double *)it->second.p;
+    return FJ_OK;
+}
+
+int poly_table(fj_ctx *ctx, int ngauss, int npoly, const double **dptr)
+{
+    auto key = std::make_pair(ngauss, npoly);
+    auto it = ctx->poly.find(key);
+    if (it == ctx->poly.end()) {
+        std::vector<double> ci(ngauss), wi(ngauss), pol(npoly), h((size_t)npoly * ngauss);
+        gauleg_host(0, 1, ngauss, ci.data(), wi.data());
+        for (int g = 0; g < ngauss; g++) {
+            evenlegend_host(npoly, ci[g], pol.data());
+            for (int np = 0; np < npoly; np++) h[(size_t)np * ngauss + g] = 2 * pol[np] * wi[g];
+        }
+        DevBuf b;
+        int rc = ensure(ctx, b, h.size() * sizeof(double));
+        if (rc) return rc;
+        FJ_CUDA(cudaMemcpy(b.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+        it = ctx->poly.emplace(key, b).first;
+    }
+    *dptr = (const double *)it->second.p;
+    return FJ_OK;
+}
+
+int gl_rule(fj_ctx *ctx, int n, GLRule *out)
+{
+    if (n <= 0) { *out = GLRule{0, nullptr, nullptr}; return FJ_OK; }
+    auto it = ctx->gl_rules.find(n);
+    if (it == ctx->gl_rules.end()) {
+        std::vector<double> h(2 * n);
+        gauleg_host(0, 1, n, h.data(), h.data() + n);
+        DevBuf b;
+        int rc = ensure(ctx, b, h.size() * sizeof(double));
+        if (rc) return rc;
+        FJ_CUDA(cudaMemcpy(b.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+        it = ctx->gl_rules.emplace(n, b).first;
+    }
+    const double *p = (const double *)it->second.p;
+    *out = GLRule{n, p, p + n};
+    return FJ_OK;
+}
+
+int upload_rule(fj_ctx *ctx, const fj_quad_rule *r, const double **xq, const double **wq)
+{
+    std::vector<double> h(r->xq, r->xq + r->nq);
+    h.insert(h.end(), r->wq, r->wq + r->nq);
+    if (h != ctx->rule_host) {
+        int rc = ensure(ctx, ctx->rule, h.size() * sizeof(double));
+        if (rc) return rc;
+        FJ_CUDA(cudaMemcpyAsync(ctx->rule.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+        FJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->rule_host = h;
+    }
+    *xq = (const double *)ctx->rule.p;
+    *wq = *xq + r->nq;
+    return FJ_OK;
+}
+
+DFDev df_dev(const fj_df_params *d)
+{
+    DFDev o;
+    o.kind = d->kind;
+    o.alpha = d->alpha; o.beta = d->beta; o.J0 = d->J0;
+    o.norm = d->mass / pow(d->J0, 3);
+    o.tpi3 = pow(kTPI, 3.);
+    o.dphi_h = d->dphi_h; o.dz_h = d->dz_h; o.dphi_g = d->dphi_g; o.dz_g = d->dz_g;
+    o.chi = d->chi; o.k = d->k;
+    return o;
+}
+
+int check_pot(fj_ctx *ctx, const fj_potential *p)
+{
+    if (!p || p->nr < 11 || p->npoly < 1 || p->npoly > kMaxPoly || !p->ar || !p->phil || !p->Pr || !p->Pr2)
+        return fail(ctx, FJ_ERR_ARG, "potential: need 11 <= nr, 1 <= npoly <= 24 and all tables");
+    return FJ_OK;
+}
+
+PotView view(const fj_potential *p) { return PotView{p->nr, p->npoly, p->ar, p->phil, p->Pr, p->Pr2}; }
+
+int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
+                const fj_quad_rule *rule, int ngauss, const double *Rz, int npts, double *out6,
+                fj_moment_stats *stats)
+{
+    int rc = check_pot(ctx, pot);
+    if (rc) return rc;
+    if (!delta || delta->ngrid < 2 || !delta->Egrid || !delta->Dgrid) return fail(ctx, FJ_ERR_ARG, "delta table");
+    if (!df || !rule || rule->nq < 1 || rule->nq > 64 || rule->jquad < 0 || rule->jquad > 64 || !out6 || npts < 1)
+        return fail(ctx, FJ_ERR_ARG, "moments: bad rule, df or sizes");
+    if (rule->precision != FJ_PREC_FP64) return fail(ctx, FJ_ERR_ARG, "moments: precision mode not available");
+    MomentArgs a;
+    a.P = view(pot);
+    a.Eg = delta->Egrid; a.Dg = delta->Dgrid; a.ngrid = delta->ngrid;
+    if ((rc = upload_rule(ctx, rule, &a.xq, &a.wq))) return rc;
+    a.nq = rule->nq;
+    if ((rc = gl_rule(ctx, rule->jquad, &a.gl))) return rc;
+    a.df = df_dev(df);
+    a.ci = nullptr; a.ngauss = ngauss; a.Rz = Rz; a.npts = npts;
+    if (!Rz) {
+        const double *gn;
+        if ((rc = gauss_nodes(ctx, ngauss, &gn))) return rc;
+        a.ci = gn;
+    }
+    const long long nq3 = (long long)rule->nq * rule->nq * rule->nq;
+    a.blocks_per_point = (int)((nq3 + kMomentBlock - 1) / kMomentBlock);
+    if ((rc = ensure(ctx, ctx->partial, (size_t)npts * a.blocks_per_point * 6 * sizeof(double)))) return rc;
+    if ((rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long)))) return rc;
+    a.partial = (double *)ctx->partial.p;
+    a.counters = (unsigned long long *)ctx->counters.p;
+    a.out6 = out6;
+    FJ_CUDA(cudaMemsetAsync(a.counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    FJ_CUDA(launch_moments(a, ctx->stream));
+    FJ_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (stats) {
+        unsigned long long h[4];
+        FJ_CUDA(cudaMemcpyAsync(h, a.counters, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+        FJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+        stats->nodes = nq3 * npts;
+        stats->bound = (long long)h[0];
+        stats->failures = (long long)h[1];
+        stats->kernel_ms = ms;
+    }
+    return FJ_OK;
+}
+
+}  // namespace
+
+// =================================================================== ABI
+extern "C" {
+
+const char *fj_version(void) { return "fjmodels-gb300 0.1 (sm_103a)"; }
+
+int fj_ctx_create(int device, fj_ctx **out)
+{
+    if (!out) return FJ_ERR_ARG;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) return FJ_ERR_NODEVICE;
+    fj_ctx *c = new fj_ctx;
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+        delete c;
+        return FJ_ERR_CUDA;
+    }
+    c->stream = c->own;
+    *out = c;
+    return FJ_OK;
+}
+
+int fj_ctx_destroy(fj_ctx *ctx)
+{
+    if (!ctx) return FJ_OK;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (DevBuf *b : {&ctx->partial, &ctx->counters, &ctx->poisson_ws, &ctx->rule, &ctx->misc})
+        if (b->p) cudaFree(b->p);
+    for (auto &kv : ctx->gauss_nodes) cudaFree(kv.second.p);
+    for (auto &kv : ctx->poly) cudaFree(kv.second.p);
+    for (auto &kv : ctx->gl_rules) cudaFree(kv.second.p);
+    cudaEventDestroy(ctx->ev0);
+    cudaEventDestroy(ctx->ev1);
+    if (ctx->own) cudaStreamDestroy(ctx->own);
+    delete ctx;
+    return FJ_OK;
+}
+
+int fj_ctx_set_stream(fj_ctx *ctx, void *stream)
+{
+    if (!ctx) return FJ_ERR_ARG;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own;
+    return FJ_OK;
+}
+
+int fj_ctx_synchronize(fj_ctx *ctx)
+{
+    if (!ctx) return FJ_ERR_ARG;
+    FJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    return FJ_OK;
+}
+
+const char *fj_last_error(fj_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int fj_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
+               const fj_quad_rule *rule, int ngauss, double *grids6, fj_moment_stats *stats)
+{
+    if (!ctx || !pot || ngauss < 1) return fail(ctx, FJ_ERR_ARG, "moments: bad arguments");
+    return run_moments(ctx, pot, delta, df, rule, ngauss, nullptr, pot->nr * ngauss, grids6, stats);
+}
+
+int fj_moments_points(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
+                      const fj_quad_rule *rule, const double *Rz, int npts, double *out6, fj_moment_stats *stats)
+{
+    if (!ctx || !Rz) return fail(ctx, FJ_ERR_ARG, "moments_points: bad arguments");
+    return run_moments(ctx, pot, delta, df, rule, 0, Rz, npts, out6, stats);
+}
+
+int fj_legendre_project(fj_ctx *ctx, int nr, int ngauss, int npoly, const double *ar, const double *grids6,
+                        double *coef6)
+{
+    if (!ctx || nr < 3 || ngauss < 1 || npoly < 1 || npoly > kMaxPoly || !ar || !grids6 || !coef6)
+        return fail(ctx, FJ_ERR_ARG, "legendre_project: bad arguments");
+    const double *poly;
+    int rc = poly_table(ctx, ngauss, npoly, &poly);
+    if (rc) return rc;
+    FJ_CUDA(launch_project(nr, ngauss, npoly, ar, poly, grids6, coef6, ctx->stream));
+    return FJ_OK;
+}
+
+int fj_poisson(fj_ctx *ctx, int nr, int npoly, const double *ar, const double *rhl, double *phil, double *Pr,
+               double *Pr2)
+{
+    if (!ctx || nr < 2 || npoly < 1 || npoly > kMaxPoly || !ar || !rhl || !phil || !Pr || !Pr2)
+        return fail(ctx, FJ_ERR_ARG, "poisson: bad arguments");
+    int rc = ensure(ctx, ctx->poisson_ws, poisson_ws_bytes(nr, npoly));
+    if (rc) return rc;
+    if ((rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long)))) return rc;
+    FJ_CUDA(launch_poisson(nr, npoly, ar, rhl, phil, Pr, Pr2, ctx->poisson_ws.p,
+                           (unsigned long long *)ctx->counters.p, ctx->stream));
+    return FJ_OK;
+}
+
+int fj_sum_potentials(fj_ctx *ctx, int n, const double *phil_a, const double *Pr_a, const double *Pr2_a,
+                      const double *phil_b, const double *Pr_b, const double *Pr2_b, double *phil, double *Pr,
+                      double *Pr2)
+{
+    if (!ctx || n < 1) return fail(ctx, FJ_ERR_ARG, "sum_potentials: bad arguments");
+    FJ_CUDA(launch_sum3(n, phil_a, Pr_a, Pr2_a, phil_b, Pr_b, Pr2_b, phil, Pr, Pr2, ctx->stream));
+    return FJ_OK;
+}
+
+int fj_compute_new_phi(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
+                       const fj_quad_rule *rule, int ngauss, double *grids6, double *coef6, double *phil_out,
+                       double *Pr_out, double *Pr2_out, fj_moment_stats *stats)
+{
+    int rc = fj_moments(ctx, pot, delta, df, rule, ngauss, grids6, stats);
+    if (rc) return rc;
+    if ((rc = fj_legendre_project(ctx, pot->nr, ngauss, pot->npoly, pot->ar, grids6, coef6))) return rc;
+    return fj_poisson(ctx, pot->nr, pot->npoly, pot->ar, coef6, phil_out, Pr_out, Pr2_out);
+}
+
+int fj_actions(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const double *pts, size_t n,
+               int jquad, double *out)
+{
+    if (!ctx) return FJ_ERR_ARG;
+    int rc = check_pot(ctx, pot);
+    if (rc) return rc;
+    if (!delta || delta->ngrid < 2 || !pts || !out || jquad < 0 || jquad > 64)
+        return fail(ctx, FJ_ERR_ARG, "actions: bad arguments");
+    GLRule gl;
+    if ((rc = gl_rule(ctx, jquad, &gl))) return rc;
+    FJ_CUDA(launch_actions(view(pot), delta->Egrid, delta->Dgrid, delta->ngrid, gl, pts, n, out, ctx->stream));
+    return FJ_OK;
+}
+
+int fj_potential_eval(fj_ctx *ctx, const fj_potential *pot, const double *Rz, size_t n, double *out)
+{
+    if (!ctx) return FJ_ERR_ARG;
+    int rc = check_pot(ctx, pot);
+    if (rc) return rc;
+    if (!Rz || !out) return fail(ctx, FJ_ERR_ARG, "potential_eval: bad arguments");
+    FJ_CUDA(launch_potential_eval(view(pot), Rz, n, out, ctx->stream));
+    return FJ_OK;
+}
+
+int fj_vir2(fj_ctx *ctx, const fj_potential *pot, int ngauss, const double *coef6, double *out7)
+{
+    if (!ctx) return FJ_ERR_ARG;
+    int rc = check_pot(ctx, pot);
+    if (rc) return rc;
+    if (ngauss < 1 || !coef6 || !out7) return fail(ctx, FJ_ERR_ARG, "vir2: bad arguments");
+    const double *gn;
+    if ((rc = gauss_nodes(ctx, ngauss, &gn))) return rc;
+    if ((rc = ensure(ctx, ctx->misc, 8 * sizeof(double)))) return rc;
+    FJ_CUDA(launch_vir2(view(pot), ngauss, gn, gn + ngauss, coef6, (double *)ctx->misc.p, ctx->stream));
+    FJ_CUDA(cudaMemcpyAsync(out7, ctx->misc.p, 7 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    FJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    return FJ_OK;
+}
+
+// ------------------------------------------------------------ host setup
+int fj_log_grid(double rmin, double rmax, int n, double *ar)
+{
+    if (n < 2 || !(rmin > 0) || !(rmax > rmin) || !ar) return FJ_ERR_ARG;
+    for (int i = 0; i < n; i++) ar[i] = pow(10., log10(rmin) + (log10(rmax) - log10(rmin)) * i / (n - 1));
+    return FJ_OK;
+}
+
+int fj_gauleg(double x1, double x2, int n, double *x, double *w)
+{
+    if (n < 1 || !x || !w) return FJ_ERR_ARG;
+    gauleg_host(x1, x2, n, x, w);
+    return FJ_OK;
+}
+
+int fj_guess_rhl(int nr, int ngauss, int npoly, const double *ar, int kind, double mass, double r0, double q,
+                 double *rhl)
+{
+    if (nr < 1 || ngauss < 1 || npoly < 1 || npoly > kMaxPoly || !ar || !rhl || kind < 0 || kind > 2)
+        return FJ_ERR_ARG;
+    const double q2 = q * q;
+    auto rho = [&](double R, double z) {  // pot/models.cpp:40-56
+        const double m = sqrt(R * R + z * z / q2);
+        if (kind == FJ_GUESS_ISOCHRONE) {
+            const double a = sqrt(r0 * r0 + m * m);
+            return mass / kFPI / (q * pow((a + r0) * a, 2) * a) * r0 * (r0 + 2 * a);
+        }
+        if (kind == FJ_GUESS_NFW) return mass / (m / r0 * pow(r0 + m, 2)) / kFPI;
+        return mass / (m / r0 * pow(r0 + m, 3)) / kTPI;
+    };
+    std::vector<double> ci(ngauss), wi(ngauss), si(ngauss), pol(npoly);
+    gauleg_host(0, 1, ngauss, ci.data(), wi.data());
+    for (int g = 0; g < ngauss; g++) si[g] = sqrt(1 - ci[g] * ci[g]);
+    std::vector<double> poly((size_t)npoly * ngauss);
+    for (int g = 0; g < ngauss; g++) {
+        evenlegend_host(npoly, ci[g], pol.data());
+        for (int np = 0; np < npoly; np++) poly[(size_t)np * ngauss + g] = 2 * pol[np] * wi[g];
+    }
+    for (int n = 0; n < nr; n++)
+        for (int np = 0; np < npoly; np++) {
+            double s = 0.;
+            for (int g = 0; g < ngauss; g++) s += poly[(size_t)np * ngauss + g] * rho(ar[n] * si[g], ar[n] * ci[g]);
+            rhl[n * npoly + np] = s;
+        }
+    rhl[0] = 2 * rho(ar[0] * si[0], ar[0] * ci[0]);
+    return FJ_OK;
+}
+
+}  // extern "C"
+
+// --------------------------------------------------- focal-distance table
+// tabulateDelta (delta/tabulate.cpp:13-38) and the Delta class
+// (delta/Delta.cpp) on the host.  Orbits use an extrapolated modified-
+// midpoint step (Bulirsch-Stoer) under the y-error step control of the
+// reference's integrator setup (abs 1e-10, rel 1e-9, Delta.cpp:59-69).
+namespace {
+
+constexpr int kOrbSize = 200;
+
+struct DeltaFit {
+    PotView P;
+    double E, Lz, Rc, R0, D2, sqDR, v0, cv, sv, Ri, zi;
+    double R[kOrbSize], z[kOrbSize];
+    int N;
+    bool bad;
+};
+
+void orbit_rhs(const DeltaFit &d, const double *y, double *f)
+{
+    double phi, dR, dz;
+    pot_grad(d.P, y[0], y[1], phi, dR, dz);
+    f[0] = y[2];
+    f[1] = y[3];
+    f[2] = -dR + pow(d.Lz, 2.0) / pow(y[0], 3.0);
+    f[3] = -dz;
+}
+
+void gbs_step(const DeltaFit &d, double h, const double *y0, double *y1, double *yerr)
+{
+    constexpr int K = 6;
+    double T[K][4], prev[4] = {0, 0, 0, 0};
+    for (int k = 0; k < K; k++) {
+        const int ns = 2 * (k + 1);
+        const double hs = h / ns;
+        double zm[4], zc[4], dy[4];
+        orbit_rhs(d, y0, dy);
+        for (int i = 0; i < 4; i++) { zm[i] = y0[i]; zc[i] = y0[i] + hs * dy[i]; }
+        for (int s = 1; s < ns; s++) {
+            orbit_rhs(d, zc, dy);
+            for (int i = 0; i < 4; i++) { const double zn = zm[i] + 2 * hs * dy[i]; zm[i] = zc[i]; zc[i] = zn; }
+        }
+        orbit_rhs(d, zc, dy);
+        for (int i = 0; i < 4; i++) T[k][i] = 0.5 * (zm[i] + zc[i] + hs * dy[i]);
+        for (int j = k - 1; j >= 0; j--) {
+            const double r = (double)(k + 1) / (double)(j + 1), fac = r * r - 1.0;
+            for (int i = 0; i < 4; i++) T[j][i] = T[j + 1][i] + (T[j + 1][i] - T[j][i]) / fac;
+        }
+        if (k == K - 2) for (int i = 0; i < 4; i++) prev[i] = T[0][i];
+    }
+    for (int i = 0; i < 4; i++) { y1[i] = T[0][i]; yerr[i] = T[0][i] - prev[i]; }
+}
+
+bool evolve_step(const DeltaFit &d, double &t, double t1, double &h, double *y)
+{
+    const double S = 0.9, ord = 8.0, epsabs = 1e-10, epsrel = 1e-9;
+    double h0 = h;
+    bool final = false;
+    if (h0 > t1 - t) { h0 = t1 - t; final = true; }
+    double y1[4], yerr[4];
+    for (int tries = 0; tries < 200; tries++) {
+        gbs_step(d, h0, y, y1, yerr);
+        double rmax = 0;
+        for (int i = 0; i < 4; i++) {
+            const double D0 = epsrel * fabs(y1[i]) + epsabs;
+            const double r = fabs(yerr[i]) / fabs(D0);
+            if (r > rmax) rmax = r;
+        }
+        if (rmax > 1.1 && h0 > 0) {
+            double r = S / pow(rmax, 1.0 / ord);
+            if (r < 0.2) r = 0.2;
+            h0 *= r;
+            final = false;
+            continue;
+        }
+        t = final ? t1 : t + h0;
+        for (int i = 0; i < 4; i++) y[i] = y1[i];
+        if (rmax < 0.5) {
+            double r = S / pow(rmax, 1.0 / (ord + 1.0));
+            if (r > 5.0) r = 5.0;
+            if (r < 1.0) r = 1.0;
+            h = r * h0;
+        } else h = h0;
+        return true;
+    }
+    return false;
+}
+
+double vsq(const DeltaFit &d, double x) { return 2 * (d.E - (pot_phi(d.P, x, 0.) + .5 * pow(d.Lz / x, 2))); }
+
+int evolve_orbit(DeltaFit &d, double x0, int cond)
+{
+    double steph = 2e-3, y[4] = {x0, 0., 0., sqrt(vsq(d, x0))}, t = 0;
+    int i = 0;
+    d.R[0] = y[0];
+    d.z[0] = y[1];
+    const double t1 = 5 * x0 / sqrt(vsq(d, x0));
+    while (i < kOrbSize - 1 && (cond == 0 ? y[1] >= 0. : y[3] >= 0.)) {
+        if (!evolve_step(d, t, t1, steph, y)) d.bad = true;
+        i++;
+        d.R[i] = y[0];
+        d.z[i] = y[1];
+    }
+    return i;
+}
+
+struct GetDRF {
+    DeltaFit *d;
+    double operator()(double x0) const
+    {
+        const int N = evolve_orbit(*d, x0, 0);
+        const double *R = d->R, *z = d->z;
+        if (fabs(z[N - 1] - z[N]) > 0 && fabs(R[N - 1] - R[N]) != 0)
+            return x0 - (R[N] - z[N] * (R[N - 1] - R[N]) / (z[N - 1] - z[N]));
+        return x0 - R[N];
+    }
+};
+
+double dphi_eff(const DeltaFit &d, double x)
+{
+    double phi, dR, dz;
+    pot_grad(d.P, x, 0, phi, dR, dz);
+    return dR - pow(d.Lz, 2) / pow(x, 3);
+}
+
+double ensure_vsq(DeltaFit &d, double x0)
+{
+    int count = 0;
+    while (vsq(d, x0) < 0) {
+        if (dphi_eff(d, x0) < 0) x0 *= 1.1; else x0 *= .9;
+        if (++count > 50) { d.bad = true; break; }
+    }
+    return x0;
+}
+
+double get_jr0(DeltaFit &d)
+{
+    GetDRF f{&d};
+    double x0 = d.Rc, x1, dx0, dx1, A = .8;
+    int k = 0;
+    x0 = ensure_vsq(d, x0); dx0 = f(x0);
+    x1 = ensure_vsq(d, x0 / A); dx1 = f(x1);
+    while (dx0 * dx1 > 0) {
+        if (fabs(dx1) < fabs(dx0)) { x0 = x1; dx0 = dx1; }
+        else A = pow(A, -0.9);
+        x1 = ensure_vsq(d, x0 * A); dx1 = f(x1);
+        if (++k == 21) {
+            if (fabs(dx0) < 1.e-7) return -x0;
+            return -1;  // Delta.cpp:145-151 goes on with -1
+        }
+    }
+    double r;
+    if (brent_root(f, x0 < x1 ? x0 : x1, x0 < x1 ? x1 : x0, r)) d.bad = true;
+    return r;
+}
+
+struct Ds2dvF {
+    DeltaFit *d;
+    double operator()(double v) const { return 2 * (d->zi * d->sqDR * sin(v) - cos(v) * (d->Ri * d->R0 + d->D2 * sin(v))); }
+};
+
+struct Ds2dD2F {
+    DeltaFit *d;
+    double operator()(double D2h) const
+    {
+        d->D2 = D2h;
+        d->sqDR = sqrt(d->D2 + d->R0 * d->R0);
+        Ds2dvF g{d};
+        double sum = 0.;
+        for (int i = 0; i < d->N; i++) {
+            d->Ri = d->R[i];
+            d->zi = d->z[i];
+            const double lo = 0, hi = kPIH;
+            if (fabs(g(lo)) < 1e-8) d->v0 = lo;
+            else if (fabs(g(hi)) < 1e-8) d->v0 = hi;
+            else if (brent_root(g, lo, hi, d->v0)) d->bad = true;
+            d->sv = sin(d->v0);
+            d->cv = cos(d->v0);
+            const double sv = d->sv, cv = d->cv, zi = d->zi, sq = d->sqDR;
+            const double dvdD2 = .5 * sv * (zi / sq - 2 * cv) / (cv * zi * sq + sv * d->Ri * d->R0 - d->D2 * (cv * cv - sv * sv));
+            sum += (cv - zi / sq) * cv + g(d->v0) * dvdD2;
+        }
+        return sum;
+    }
+};
+
+double get_rc_host(const PotView &P, double Lzsq, double R, bool &bad)
+{
+    unsigned f = 0;
+    const double r = get_rc(P, Lzsq, R, f);
+    if (f) bad = true;
+    return r;
+}
+
+struct RcEF {
+    PotView P; double E;
+    double operator()(double R) const
+    {
+        double phi, dR, dz;
+        pot_grad(P, R, 0, phi, dR, dz);
+        return .5 * R * dR + pot_phi(P, R, 0) - E;
+    }
+};
+
+}  // namespace
+
+extern "C" int fj_tabulate_delta(const fj_potential *pot, int ngrid, double *Egrid, double *Dgrid)
+{
+    if (!pot || pot->nr < 11 || pot->npoly < 1 || pot->npoly > kMaxPoly || ngrid < 2 || !Egrid || !Dgrid)
+        return FJ_ERR_ARG;
+    const PotView P = view(pot);
+    const double *ar = pot->ar;
+    const int nr = pot->nr;
+    bool bad = false;
+    const double Rmax = ar[nr - 1];
+    double phi, dRv, dzv;
+    const double Lzmax = Rmax * 0.98 * sqrt(-2 * pot_phi(P, Rmax, 0)), Rmin = 1e-3 * Rmax;
+    pot_grad(P, Rmin, 0, phi, dRv, dzv);
+    const double Lzmin = Rmin * sqrt(Rmin * dRv);
+    double R = .01 * Rmax, Lz1 = 0, Rg1 = 0, Ec1 = 0, Vmax1 = 0;
+    for (int i = 0; i < 2; i++) {  // only entries 0 and 1 of the reference's per-radius loop feed the table
+        const double Lzi = Lzmin + i * (Lzmax - Lzmin) / (double)(nr - 1);
+        R = get_rc_host(P, pow(Lzi, 2), R, bad);
+        pot_grad(P, R, 0, phi, dRv, dzv);
+        const double vc2 = R * dRv;
+        const double Ec = .5 * vc2 + pot_phi(P, R, 0);
+        Lz1 = Lzi; Rg1 = R; Ec1 = Ec; Vmax1 = .98 * sqrt(-2 * Ec);
+    }
+    std::vector<DeltaFit> fits(1);
+    DeltaFit &d = fits[0];
+    for (int nE = 0; nE < ngrid; nE++) {
+        Egrid[nE] = Ec1 + .5 * pow(Vmax1 * (nE + 1) / (double)ngrid, 2);
+        memset(&d, 0, sizeof d);
+        d.P = P;
+        d.E = Egrid[nE];
+        d.Lz = .25 * Lz1;
+        // RcE (include/Utils.h:220-236)
+        RcEF fe{P, d.E};
+        double R0 = .8 * Rg1, f0 = fe(R0);
+        for (int it = 0; f0 > 0 && it < kLoopCap; it++) { R0 *= .8; f0 = fe(R0); }
+        double R1 = 1.2 * Rg1, f1 = fe(R1);
+        for (int it = 0; f1 < 0 && it < kLoopCap; it++) { R1 *= 1.2; f1 = fe(R1); }
+        if (brent_root(fe, R0, R1, d.Rc)) bad = true;
+        // getBestDelta (Delta.cpp:248-294)
+        d.R0 = get_jr0(d);
+        d.N = evolve_orbit(d, d.R0, 1);
+        Ds2dD2F g{&d};
+        double lo = -0.001, hi = 5, D2out = 0;
+        double Dmin = g(lo), Dmax = g(hi);
+        for (int it = 0; Dmin * Dmax > 0 && fabs(Dmax) > 1e-4 && fabs(Dmin) > 1e-4; it++) {
+            if (Dmax < 0) { hi *= 5; Dmax = g(hi); } else { lo -= .1; Dmin = g(lo); }
+            if (it > 1000000) { bad = true; break; }
+        }
+        if (fabs(g(lo)) < 1e-8) D2out = lo;
+        else if (fabs(g(hi)) < 1e-8) D2out = hi;
+        else if (brent_root(g, lo, hi, D2out)) bad = true;
+        Dgrid[nE] = D2out;
+        if (d.bad) bad = true;
+    }
+    return bad ? FJ_ERR_ARG : FJ_OK;
+}
+
+// ------------------------------------------------------ coefficient file
+extern "C" int fj_write_out(const char *path, int nr, int npoly, int ngauss, const double *hdr10, const double *ar,
+                            const double *mats9)
+{
+    if (!path || nr < 1 || npoly < 1 || !hdr10 || !ar || !mats9) return FJ_ERR_ARG;
+    std::ofstream outF(path, std::ios::out);
+    if (!outF.is_open()) return FJ_ERR_IO;
+    // header (io/writeOut.cpp:81-85): sizes, h/g coefficients, chi mass r0, A B
+    outF << nr << " " << npoly << " " << ngauss << std::endl;
+    outF << hdr10[0] << " " << hdr10[1] << " " << hdr10[2] << " " << hdr10[3] << std::endl;
+    outF << hdr10[4] << " " << hdr10[5] << " " << hdr10[6] << std::endl;
+    outF << hdr10[7] << " " << hdr10[8] << std::endl;
+    for (int i = 0; i < nr; i++) outF << ar[i] << std::endl;  // writeArr (:45-49)
+    for (int m = 0; m < 9; m++)                                  // writeMat (:51-59)
+        for (int i = 0; i < nr; i++) {
+            for (int j = 0; j < npoly; j++) outF << mats9[(size_t)m * nr * npoly + (size_t)i * npoly + j] << " ";
+            outF << std::endl;
+        }
+    outF.close();
+    return outF.fail() ? FJ_ERR_IO : FJ_OK;
+}
+
+// ------------------------------------------------------------ whole model
+extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_result *res)
+{
+    if (!ctx || !cfg || !res || !res->ar || !res->coef6 || !res->phil || !res->Pr || !res->Pr2 || !res->Egrid ||
+        !res->Dgrid)
+        return fail(ctx, FJ_ERR_ARG, "run_model: missing result buffers");
+    const int nr = cfg->nr, ng = cfg->ngauss, npl = cfg->npoly, ngrid = cfg->ngrid, nt = nr * npl;
+    if (nr < 11 || ng < 1 || npl < 1 || npl > kMaxPoly || ngrid < 2 || cfg->itermax < 1)
+        return fail(ctx, FJ_ERR_ARG, "run_model: bad sizes");
+    auto t0 = std::chrono::steady_clock::now();
+    int rc;
+    if ((rc = fj_log_grid(cfg->rmin, cfg->rmax, nr, res->ar))) return fail(ctx, rc, "run_model: grid");
+    std::vector<double> rhl(nt);
+    if ((rc = fj_guess_rhl(nr, ng, npl, res->ar, cfg->guess, cfg->mass, cfg->r0, cfg->q, rhl.data())))
+        return fail(ctx, rc, "run_model: guess");
+    // device layout: ar | rhl | pot A (3 tables) | pot B (3 tables) | Eg | Dg | grids6 | coef6
+    const size_t nd = nr + nt + 6 * (size_t)nt + 2 * ngrid + 6 * (size_t)nr * ng + 6 * (size_t)nt;
+    double *dbuf = nullptr;
+    FJ_CUDA(cudaMalloc(&dbuf, nd * sizeof(double)));
+    struct Free { double *p; ~Free() { cudaFree(p); } } guard{dbuf};
+    double *d_ar = dbuf, *d_rhl = d_ar + nr, *potA = d_rhl + nt, *potB = potA + 3 * nt, *d_Eg = potB + 3 * nt,
+           *d_Dg = d_Eg + ngrid, *d_grids = d_Dg + ngrid, *d_coef = d_grids + 6 * (size_t)nr * ng;
+    cudaStream_t s = ctx->stream;
+    FJ_CUDA(cudaMemcpyAsync(d_ar, res->ar, nr * sizeof(double), cudaMemcpyHostToDevice, s));
+    FJ_CUDA(cudaMemcpyAsync(d_rhl, rhl.data(), nt * sizeof(double), cudaMemcpyHostToDevice, s));
+    if ((rc = fj_poisson(ctx, nr, npl, d_ar, d_rhl, potA, potA + nt, potA + 2 * nt))) return rc;
+    // focal-distance table from the guess potential (fJmodels.cpp:127)
+    std::vector<double> hp(3 * nt);
+    FJ_CUDA(cudaMemcpyAsync(hp.data(), potA, 3 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FJ_CUDA(cudaStreamSynchronize(s));
+    fj_potential hpot{nr, npl, res->ar, hp.data(), hp.data() + nt, hp.data() + 2 * nt};
+    fj_tabulate_delta(&hpot, ngrid, res->Egrid, res->Dgrid);
+    FJ_CUDA(cudaMemcpyAsync(d_Eg, res->Egrid, ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+    FJ_CUDA(cudaMemcpyAsync(d_Dg, res->Dgrid, ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+    fj_delta_table dt{ngrid, d_Eg, d_Dg};
+    double *cur = potA, *nxt = potB;
+    std::vector<double> old(nt), neu(nt);
+    memcpy(old.data(), hp.data(), nt * sizeof(double));
+    res->bound = res->failures = 0;
+    res->kernel_ms = 0;
+    res->last_change = -1;
+    int k = 0;
+    for (k = 0; k < cfg->itermax; k++) {
+        fj_potential pot{nr, npl, d_ar, cur, cur + nt, cur + 2 * nt};
+        fj_moment_stats st;
+        if ((rc = fj_compute_new_phi(ctx, &pot, &dt, &cfg->df, &cfg->rule, ng, d_grids, d_coef, nxt, nxt + nt,
+                                     nxt + 2 * nt, &st)))
+            return rc;
+        res->bound += st.bound;
+        res->failures += st.failures;
+        res->kernel_ms += st.kernel_ms;
+        FJ_CUDA(cudaMemcpyAsync(neu.data(), nxt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+        FJ_CUDA(cudaStreamSynchronize(s));
+        double maxd = 0;
+        for (int i = 0; i < nr; i++)
+            for (int j = 0; j < npl; j++)
+                maxd = fmax(maxd, fabs((neu[i * npl + j] - old[i * npl + j]) / neu[i * npl]));
+        res->last_change = maxd;
+        old.swap(neu);
+        std::swap(cur, nxt);
+        if (cfg->tol > 0 && maxd < cfg->tol) { k++; break; }
+    }
+    res->iterations = k;
+    fj_potential pot{nr, npl, d_ar, cur, cur + nt, cur + 2 * nt};
+    if ((rc = fj_vir2(ctx, &pot, ng, d_coef, res->vir7))) return rc;
+    FJ_CUDA(cudaMemcpyAsync(res->coef6, d_coef, 6 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FJ_CUDA(cudaMemcpyAsync(res->phil, cur, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FJ_CUDA(cudaMemcpyAsync(res->Pr, cur + nt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FJ_CUDA(cudaMemcpyAsync(res->Pr2, cur + 2 * nt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (res->grids6)
+        FJ_CUDA(cudaMemcpyAsync(res->grids6, d_grids, 6 * (size_t)nr * ng * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FJ_CUDA(cudaStreamSynchronize(s));
+    res->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return FJ_OK;
+}

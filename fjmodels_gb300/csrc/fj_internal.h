@@ -1,0 +1,52 @@
+// fj_internal.h -- launch interface between the C-ABI layer and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fj_device.cuh"
+
+namespace fj {
+
+constexpr int kMomentBlock = 128;  // threads per block of the phase-space kernel
+
+// Arguments of the phase-space (moment) kernel.  All pointers are device memory.
+struct MomentArgs {
+    PotView P;
+    const double *Eg, *Dg;
+    int ngrid;
+    const double *xq, *wq;   // velocity rule [nq]
+    int nq;
+    GLRule gl;               // momentum-integral rule (n = 0: QAGS)
+    DFDev df;
+    const double *ci;        // grid mode: ngauss polar GL nodes on (0,1); else NULL
+    int ngauss;
+    const double *Rz;        // point mode: [npts][2]; else NULL
+    int npts;
+    int blocks_per_point;
+    double *partial;         // [npts][blocks_per_point][6]
+    unsigned long long *counters;  // [0] bound nodes, [1] failed nodes
+    double *out6;            // [6][npts]
+};
+
+size_t moment_smem_bytes(const MomentArgs &a);
+cudaError_t launch_moments(const MomentArgs &a, cudaStream_t s);
+
+cudaError_t launch_actions(PotView P, const double *Eg, const double *Dg, int ngrid, GLRule gl,
+                           const double *pts, size_t n, double *out, cudaStream_t s);
+cudaError_t launch_potential_eval(PotView P, const double *Rz, size_t n, double *out, cudaStream_t s);
+
+// projection: poly [npoly][ngauss] = 2 P_2l(c_g) w_g
+cudaError_t launch_project(int nr, int ngauss, int npoly, const double *ar, const double *poly,
+                           const double *grids6, double *coef6, cudaStream_t s);
+// Poisson: ws = scratch for 2*nr*npoly QAGS interval lists of kPoissonCap entries
+constexpr int kPoissonCap = 256;
+size_t poisson_ws_bytes(int nr, int npoly);
+cudaError_t launch_poisson(int nr, int npoly, const double *ar, const double *rhl, double *phil,
+                           double *Pr, double *Pr2, void *ws, unsigned long long *counters, cudaStream_t s);
+cudaError_t launch_sum3(int n, const double *a0, const double *a1, const double *a2, const double *b0,
+                        const double *b1, const double *b2, double *o0, double *o1, double *o2, cudaStream_t s);
+// vir2: ci, wi = ngauss polar nodes/weights on (0,1); out7 device
+cudaError_t launch_vir2(PotView P, int ngauss, const double *ci, const double *wi, const double *coef6,
+                        double *out7, cudaStream_t s);
+
+}  // namespace fj

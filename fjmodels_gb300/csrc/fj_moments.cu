@@ -1,0 +1,186 @@
+// fj_moments.cu -- the phase-space kernel: one thread per (meridional point,
+// velocity node) evaluates the Staeckel-fudge actions and the DF and the
+// block reduces the six velocity moments; plus the batched action and
+// potential kernels.
+//
+// Work unit: node q = (i, j, k) of the nq^3 tensor rule (integ/GaussQuad.cpp:
+// 160-180), velocity V = 1e-6 + Ve*(x_i, x_j, x_k) (integ/Integ.cpp:46-62).
+// Blocks of kMomentBlock threads cover consecutive nodes of one point; the
+// per-block sums go to a scratch array and a second kernel adds them in a
+// fixed order, so results are deterministic run to run.
+#include "fj_internal.h"
+
+namespace fj {
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+size_t moment_smem_bytes(const MomentArgs &a)
+{
+    const size_t nd = a.P.nr + 3 * (size_t)a.P.nr * a.P.npoly + 2 * a.ngrid + 2 * a.nq + 2 * a.gl.n;
+    return nd * sizeof(double) + 6 * (kMomentBlock / 32) * sizeof(double);
+}
+
+__global__ void __launch_bounds__(kMomentBlock) k_moments(MomentArgs a)
+{
+    extern __shared__ double sm[];
+    const int nr = a.P.nr, npoly = a.P.npoly, nt = nr * npoly;
+    double *s_ar = sm, *s_phil = s_ar + nr, *s_Pr = s_phil + nt, *s_Pr2 = s_Pr + nt;
+    double *s_Eg = s_Pr2 + nt, *s_Dg = s_Eg + a.ngrid, *s_xq = s_Dg + a.ngrid, *s_wq = s_xq + a.nq;
+    double *s_glx = s_wq + a.nq, *s_glw = s_glx + a.gl.n, *s_red = s_glw + a.gl.n;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) s_ar[i] = a.P.ar[i];
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+        s_phil[i] = a.P.phil[i]; s_Pr[i] = a.P.Pr[i]; s_Pr2[i] = a.P.Pr2[i];
+    }
+    for (int i = threadIdx.x; i < a.ngrid; i += blockDim.x) { s_Eg[i] = a.Eg[i]; s_Dg[i] = a.Dg[i]; }
+    for (int i = threadIdx.x; i < a.nq; i += blockDim.x) { s_xq[i] = a.xq[i]; s_wq[i] = a.wq[i]; }
+    for (int i = threadIdx.x; i < a.gl.n; i += blockDim.x) { s_glx[i] = a.gl.x01[i]; s_glw[i] = a.gl.w01[i]; }
+    __syncthreads();
+
+    const PotView P{nr, npoly, s_ar, s_phil, s_Pr, s_Pr2};
+    const GLRule gl{a.gl.n, s_glx, s_glw};
+    const int B = a.blocks_per_point;
+    const int p = blockIdx.x / B, chunk = blockIdx.x % B;
+    const int nq = a.nq, nq3 = nq * nq * nq;
+    const int node = chunk * kMomentBlock + threadIdx.x;
+
+    double R, z;
+    if (a.Rz) { R = a.Rz[2 * p]; z = a.Rz[2 * p + 1]; }
+    else {
+        const int n = p / a.ngauss, g = p % a.ngauss;
+        const double c = a.ci[g], si = sqrt(1 - c * c);
+        R = s_ar[n] * si; z = s_ar[n] * c;
+    }
+
+    double m[6] = {0, 0, 0, 0, 0, 0};
+    unsigned bound = 0, failed = 0;
+    if (node < nq3) {
+        const int i = node / (nq * nq), j = (node / nq) % nq, k = node % nq;
+        const double Phi_h = pot_phi(P, R, z);
+        const double rmax = s_ar[nr - 1];
+        const double Ve = sqrt(-2 * (Phi_h - pot_phi(P, 10 * rmax, 10 * rmax)));
+        const double V0 = 1e-6 + Ve * s_xq[i], V1 = 1e-6 + Ve * s_xq[j], V2 = 1e-6 + Ve * s_xq[k];
+        const double jacob = Ve * Ve * Ve;
+        const double H = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h;
+        double DF = 0.;
+        if (H < 0) {
+            bound = 1;
+            unsigned fail = 0;
+            double Jr, Jz;
+            const double Delta = deltafn(s_Eg, s_Dg, a.ngrid, H);
+            fudge_actions(P, Delta, R, z, Phi_h, V0, V1, V2, gl, Jr, Jz, fail);
+            DF = df_value(a.df, P, R, Jr, Jz, R * V1, fail);
+            if (fail & (kFailBracket | kFailRoot)) DF = 0.;
+            failed = fail ? 1u : 0u;
+        }
+        const double w = s_wq[i] * s_wq[j] * s_wq[k];
+        const double jd = jacob * DF;
+        m[0] = w * jd;
+        m[1] = w * (jd * V1);
+        m[2] = w * (jd * V0 * V0);
+        m[3] = w * (jd * V1 * V1);
+        m[4] = w * (jd * V2 * V2);
+        m[5] = w * (jd * V0 * V2);
+    }
+    // block reduction in a fixed order
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        const double v = warp_sum(m[q]);
+        if (lane == 0) s_red[warp * 6 + q] = v;
+    }
+    const unsigned nb = __syncthreads_count(bound);
+    const unsigned nf = __syncthreads_count(failed);
+    if (threadIdx.x < 6) {
+        double s = 0;
+        for (int w = 0; w < kMomentBlock / 32; w++) s += s_red[w * 6 + threadIdx.x];
+        a.partial[((size_t)p * B + chunk) * 6 + threadIdx.x] = s;
+    }
+    if (threadIdx.x == 0) {
+        if (nb) atomicAdd(&a.counters[0], (unsigned long long)nb);
+        if (nf) atomicAdd(&a.counters[1], (unsigned long long)nf);
+    }
+}
+
+// sums the per-block partials of each point and normalises as rhofDF does
+// (integ/Integ.cpp:160-162)
+__global__ void k_moments_finalize(const double *partial, int npts, int B, double *out6)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npts) return;
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    for (int c = 0; c < B; c++)
+#pragma unroll
+        for (int q = 0; q < 6; q++) s[q] += partial[((size_t)p * B + c) * 6 + q];
+    out6[0 * (size_t)npts + p] = s[0];
+    out6[1 * (size_t)npts + p] = s[1] / s[0];
+    out6[2 * (size_t)npts + p] = sqrt(s[2] / s[0]);
+    out6[3 * (size_t)npts + p] = sqrt(s[3] / s[0]);
+    out6[4 * (size_t)npts + p] = sqrt(s[4] / s[0]);
+    out6[5 * (size_t)npts + p] = sqrt(fabs(s[5]) / s[0]);
+}
+
+cudaError_t launch_moments(const MomentArgs &a, cudaStream_t s)
+{
+    const size_t smem = moment_smem_bytes(a);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    const long long nblocks = (long long)a.npts * a.blocks_per_point;
+    k_moments<<<(unsigned)nblocks, kMomentBlock, smem, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_moments_finalize<<<(a.npts + 127) / 128, 128, 0, s>>>(a.partial, a.npts, a.blocks_per_point, a.out6);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- actions
+__global__ void k_actions(PotView P, const double *Eg, const double *Dg, int ngrid, GLRule gl,
+                          const double *pts, size_t n, double *out)
+{
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const double R = pts[5 * t], z = pts[5 * t + 1], vR = pts[5 * t + 2], vp = pts[5 * t + 3], vz = pts[5 * t + 4];
+    const double Phi = pot_phi(P, R, z);
+    const double H = .5 * (vR * vR + vp * vp + vz * vz) + Phi;
+    if (H >= 0) { out[2 * t] = -1; out[2 * t + 1] = -1; return; }
+    double Jr, Jz;
+    unsigned fail = 0;
+    fudge_actions(P, deltafn(Eg, Dg, ngrid, H), R, z, Phi, vR, vp, vz, gl, Jr, Jz, fail);
+    out[2 * t] = Jr;
+    out[2 * t + 1] = Jz;
+}
+
+cudaError_t launch_actions(PotView P, const double *Eg, const double *Dg, int ngrid, GLRule gl,
+                           const double *pts, size_t n, double *out, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_actions<<<(unsigned)((n + 63) / 64), 64, 0, s>>>(P, Eg, Dg, ngrid, gl, pts, n, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- potential
+__global__ void k_potential_eval(PotView P, const double *Rz, size_t n, double *out)
+{
+    const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    double phi, dR, dz;
+    pot_grad(P, Rz[2 * t], Rz[2 * t + 1], phi, dR, dz);
+    out[3 * t] = phi;
+    out[3 * t + 1] = dR;
+    out[3 * t + 2] = dz;
+}
+
+cudaError_t launch_potential_eval(PotView P, const double *Rz, size_t n, double *out, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_potential_eval<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(P, Rz, n, out);
+    return cudaGetLastError();
+}
+
+}  // namespace fj

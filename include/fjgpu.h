@@ -1,0 +1,220 @@
+/*
+ * fjgpu.h -- C ABI of the GB300 (sm_103a) implementation of the fJmodels
+ * density / moment evaluation path.
+ *
+ * Conventions
+ *   - Every table is contiguous row-major: a [nr][npoly] multipole table
+ *     stores coefficient l=2*np at radius ar[n] in t[n*npoly+np]; a
+ *     [nr][ngauss] meridional grid stores point (ar[n], cos theta_g) in
+ *     g[n*ngauss+g].  The reference keeps the same matrices as row-pointer
+ *     double** (include/Utils.h:71-75); fj_rows_to_flat / fj_flat_to_rows in
+ *     INTEGRATION.md adapt them.
+ *   - "device" pointers are CUDA global-memory pointers on the context's
+ *     device; "host" pointers are ordinary memory.  Every call is ordered on
+ *     the context's stream and returns after its work is queued unless the
+ *     comment says it synchronises.
+ *   - Return value: FJ_OK (0) or an FJ_ERR_* code; the reference's exit(n)
+ *     paths become error codes (fj_last_error gives the text).  Per-node
+ *     numerical failures (a capped bracket, Brent or QAGS limit) never abort:
+ *     the node's DF contributes 0, as the reference's NaN guard does
+ *     (df/DF.cpp:105), and the count is reported in fj_moment_stats.
+ *   - One context per host thread; calls on one context are not re-entrant.
+ */
+#ifndef FJGPU_H
+#define FJGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FJ_OK 0
+#define FJ_ERR_ARG 1
+#define FJ_ERR_CUDA 2
+#define FJ_ERR_NOMEM 3
+#define FJ_ERR_IO 4
+#define FJ_ERR_NODEVICE 5
+
+/* distribution function variants */
+#define FJ_DF_DPL 0      /* double power law + k*tanh(chi*Jphi/J0) (df/DF.cpp:65-76,108-123) */
+#define FJ_DF_QUASIISO 1 /* quasi-isothermal, the reference binary's live branch (df/DF.cpp:94-106) */
+
+/* arithmetic of the phase-space kernel */
+#define FJ_PREC_FP64 0  /* plain form: everything in FP64 */
+#define FJ_PREC_MIXED 1 /* FP32 momentum quadrature and DF, FP64 turning points */
+
+/* momentum integrals of the actions: 0 = adaptive QAGS as the reference
+   (include/Utils.h:173-185); n > 0 = fixed n-point Gauss-Legendre */
+#define FJ_JQUAD_QAGS 0
+
+/* guess densities (pot/models.cpp:40-56) */
+#define FJ_GUESS_HERNQUIST 0
+#define FJ_GUESS_ISOCHRONE 1
+#define FJ_GUESS_NFW 2
+
+typedef struct fj_ctx fj_ctx;
+
+/* Multipole potential on a radial grid: the reference's global ar/phil/Pr/Pr2
+   (include/Grid.h:19-22).  Requires 11 <= nr and 1 <= npoly <= 24. */
+typedef struct fj_potential {
+    int nr, npoly;
+    const double *ar;   /* [nr]        */
+    const double *phil; /* [nr*npoly]  */
+    const double *Pr;   /* [nr*npoly]  dPhi_l/dr   */
+    const double *Pr2;  /* [nr*npoly]  d2Phi_l/dr2 */
+} fj_potential;
+
+/* Focal-distance table of delta/tabulate.cpp (Egrid, Dgrid = Delta^2). */
+typedef struct fj_delta_table {
+    int ngrid;
+    const double *Egrid, *Dgrid;
+} fj_delta_table;
+
+/* DF parameters of one component (df/DF.cpp:18-63, pot/models.cpp:13). */
+typedef struct fj_df_params {
+    int kind;                         /* FJ_DF_DPL or FJ_DF_QUASIISO */
+    double alpha, beta;               /* slopes A, B */
+    double J0, mass;                  /* J0 = sqrt(mass*r0) */
+    double dphi_h, dz_h, dphi_g, dz_g;
+    double chi, k;                    /* rotation: f*(1 + k*tanh(chi*Jphi/J0)) when chi > 0 */
+} fj_df_params;
+
+/* Velocity quadrature (the same nq-point rule on [-1,1] for vR, vphi, vz;
+   include/GaussPts.h:79-88 is the reference's live rule), host arrays. */
+typedef struct fj_quad_rule {
+    int nq;            /* <= 64 */
+    const double *xq;  /* [nq] host */
+    const double *wq;  /* [nq] host */
+    int jquad;         /* FJ_JQUAD_QAGS or Gauss-Legendre order (<= 64) */
+    int precision;     /* FJ_PREC_FP64 or FJ_PREC_MIXED */
+} fj_quad_rule;
+
+typedef struct fj_moment_stats {
+    long long nodes;     /* phase-space evaluations (grid points x nq^3) */
+    long long bound;     /* nodes with H < 0 */
+    long long failures;  /* nodes whose action solve hit a cap */
+    double kernel_ms;    /* device time of the phase-space kernel (CUDA events) */
+} fj_moment_stats;
+
+/* ---------------------------------------------------------------- context */
+const char *fj_version(void);
+int fj_ctx_create(int device, fj_ctx **out);
+int fj_ctx_destroy(fj_ctx *ctx);
+/* Use an existing cudaStream_t (passed as void*) for subsequent work; NULL = the context's own stream. */
+int fj_ctx_set_stream(fj_ctx *ctx, void *stream);
+int fj_ctx_synchronize(fj_ctx *ctx);
+const char *fj_last_error(fj_ctx *ctx);
+
+/* ----------------------------------------------------- hot path (device) */
+
+/* Integ density/moment integrals over the meridional grid.
+   Backs rhofDF(R,z,p,&vrot,&sigR,&sigp,&sigz,&sigRz) (include/Integ.h:19,
+   integ/Integ.cpp:150-163) as called by computeRhl's grid loop
+   (pot/potLeg.cpp:54-58).  The grid points are (ar[n]*sqrt(1-c_g^2), ar[n]*c_g)
+   with c_g the ngauss Gauss-Legendre nodes on (0,1) (potLeg.cpp:43-47).
+   grids6: device [6][nr*ngauss] = rho, vrot, sigR, sigp, sigz, sigRz. */
+int fj_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta,
+               const fj_df_params *df, const fj_quad_rule *rule, int ngauss, double *grids6,
+               fj_moment_stats *stats);
+
+/* Same, for an explicit list of npts meridional points Rz (device [npts][2]);
+   out6 device [6][npts].  The one-point form backs the 8-argument rhofDF. */
+int fj_moments_points(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta,
+                      const fj_df_params *df, const fj_quad_rule *rule, const double *Rz, int npts,
+                      double *out6, fj_moment_stats *stats);
+
+/* rho[0][0] extrapolation (pot/potLeg.cpp:68) and the 6-field Legendre
+   projection get_Ylm (include/UtilsLeg.h:200-253).  grids6 device
+   [6][nr*ngauss] (read only), coef6 device [6][nr*npoly] = rhl, vrotl, sigRl,
+   sigpl, sigzl, sigRzl. */
+int fj_legendre_project(fj_ctx *ctx, int nr, int ngauss, int npoly, const double *ar,
+                        const double *grids6, double *coef6);
+
+/* Poisson solve Potential::computePhil (pot/Potential.cpp:110-200):
+   QAGS / QAGIU radial integrals with the reference's tolerances and retry
+   rule, then phil, Pr, Pr2.  All device [nr*npoly]. */
+int fj_poisson(fj_ctx *ctx, int nr, int npoly, const double *ar, const double *rhl,
+               double *phil, double *Pr, double *Pr2);
+
+/* updatePhil (pot/potLeg.cpp:21-29): out = a + b element-wise on the three
+   tables (device [nr*npoly] each). */
+int fj_sum_potentials(fj_ctx *ctx, int n, const double *phil_a, const double *Pr_a,
+                      const double *Pr2_a, const double *phil_b, const double *Pr_b,
+                      const double *Pr2_b, double *phil, double *Pr, double *Pr2);
+
+/* computeNewPhi (pot/potLeg.cpp:76-82): moments, projection and Poisson in
+   one stream-ordered call.  grids6, coef6 and the three output tables are
+   device buffers; the output tables may not alias pot's tables. */
+int fj_compute_new_phi(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta,
+                       const fj_df_params *df, const fj_quad_rule *rule, int ngauss,
+                       double *grids6, double *coef6, double *phil_out, double *Pr_out,
+                       double *Pr2_out, fj_moment_stats *stats);
+
+/* Staeckel-fudge actions: uvOrb(Delta, Lz, Phi, x, p, pot).Ju()/.Jv()
+   (include/uvOrb.h:15,23-24; uvOrb/uvOrb.cpp:15-262) for n phase points
+   pts device [n][5] = (R, z, vR, vphi, vz), with Delta = Deltafn(H)
+   (delta/tabulate.cpp:40-44) as df() does.  out device [n][2] = (Jr, Jz);
+   (-1,-1) marks H >= 0, 1e31 an unbound orbit.  jquad: FJ_JQUAD_QAGS or GL order. */
+int fj_actions(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta,
+               const double *pts, size_t n, int jquad, double *out);
+
+/* Potential::operator(), dR, dz (pot/Potential.cpp:206-276) at n points
+   Rz device [n][2]; out device [n][3] = (Phi, dPhi/dR, dPhi/dz). */
+int fj_potential_eval(fj_ctx *ctx, const fj_potential *pot, const double *Rz, size_t n, double *out);
+
+/* Tensor virial sums vir2 (libs/Stats.cpp:12-41).  coef6 device (as from
+   fj_legendre_project).  out7 HOST = KRR, Kzz, WRR, Wzz, PE, mass from Pr at
+   the last radius, mass from the density sum.  Synchronises. */
+int fj_vir2(fj_ctx *ctx, const fj_potential *pot, int ngauss, const double *coef6, double *out7);
+
+/* ------------------------------------------- host-side setup (run once) */
+
+/* Logarithmic radial grid (include/Utils.h:76-81 with an explicit rmin). */
+int fj_log_grid(double rmin, double rmax, int n, double *ar);
+/* Gauss-Legendre nodes/weights on [x1,x2] (include/UtilsLeg.h:18-39). */
+int fj_gauleg(double x1, double x2, int n, double *x, double *w);
+/* Guess-density multipoles computeGuessRhl (pot/Potential.cpp:63-80), host arrays. */
+int fj_guess_rhl(int nr, int ngauss, int npoly, const double *ar, int kind, double mass,
+                 double r0, double q, double *rhl);
+/* Focal-distance table tabulateDelta (delta/tabulate.cpp:13-38, delta/Delta.cpp),
+   evaluated on the host from HOST potential tables.  Egrid/Dgrid host [ngrid]. */
+int fj_tabulate_delta(const fj_potential *pot_host, int ngrid, double *Egrid, double *Dgrid);
+
+/* Coefficient file writer _writeOut (io/writeOut.cpp:74-138): byte-identical
+   output for identical arrays.  mats9 host [9][nr*npoly] in the file order
+   rhl, vrotl, sigRl, sigpl, sigzl, sigRzl, phil, Pr, Pr2. */
+int fj_write_out(const char *path, int nr, int npoly, int ngauss, const double *hdr10,
+                 const double *ar, const double *mats9);
+
+/* ------------------------------------------- whole model (host buffers) */
+
+/* One component of a self-consistent run (fJmodels.cpp:86-144 oneComp). */
+typedef struct fj_model_config {
+    int nr, ngauss, npoly, ngrid;
+    double rmin, rmax;
+    int guess;                   /* FJ_GUESS_* */
+    double mass, r0, q;
+    fj_df_params df;
+    fj_quad_rule rule;           /* host arrays */
+    int itermax;                 /* iterations */
+    double tol;                  /* stop when max|dphil/phil_0| < tol (UtilsLeg.h:266-278); <= 0: run itermax */
+} fj_model_config;
+
+typedef struct fj_model_result {
+    /* host arrays the caller allocated: ar [nr], coef6 [6][nr*npoly],
+       phil/Pr/Pr2 [nr*npoly], Egrid/Dgrid [ngrid], grids6 [6][nr*ngauss] (may be NULL) */
+    double *ar, *coef6, *phil, *Pr, *Pr2, *Egrid, *Dgrid, *grids6;
+    double vir7[7];              /* vir2 sums after the last iteration */
+    int iterations;
+    double last_change;          /* max|dphil/phil_0| of the last iteration */
+    long long bound, failures;
+    double wall_ms, kernel_ms;
+} fj_model_result;
+
+int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_result *res);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

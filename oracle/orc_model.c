@@ -923,8 +923,7 @@ static double getJr0(orc_delta *d)
         k++;
         if (k == 21) {
             if (fabs(dx0) < 1.e-7) return -x0;
-            d->fail = 1;
-            return -1;
+            return -1; /* the reference reports "problem in get_closed()" and goes on with -1 */
         }
     }
     double lo = x0 < x1 ? x0 : x1, hi = x0 < x1 ? x1 : x0, r;
@@ -997,7 +996,7 @@ static double getBestDelta(orc_delta *d)
     while (Dmin * Dmax > 0 && fabs(Dmax) > 1e-4 && fabs(Dmin) > 1e-4) {
         if (Dmax < 0) { hi *= 5; Dmax = ds2dD2TOT(hi, d); }
         else { lo -= .1; Dmin = ds2dD2TOT(lo, d); }
-        if (++it > 1000) { d->fail = 1; break; }
+        if (++it > 1000000) { d->fail = 1; break; }
     }
     if (fabs(ds2dD2TOT(lo, d)) < 1e-8) D2out = lo;
     else if (fabs(ds2dD2TOT(hi, d)) < 1e-8) D2out = hi;

@@ -267,6 +267,7 @@ static void qelg(double *tab, int *n_io, double *res3, int *nres, double *result
 
 /* Adaptive bisection with extrapolation (DQAGSE).  rule 21 or 15.
    Returns 0 on success, a positive QUADPACK error class otherwise. */
+_Thread_local int orc_qags_hist[8];
 static int qags_core(orc_fn f, void *p, double a, double b, double epsabs, double epsrel, int limit,
                      int rule, double *result, double *abserr)
 {
@@ -287,7 +288,7 @@ static int qags_core(orc_fn f, void *p, double a, double b, double epsabs, doubl
     double tol = epsabs > epsrel * fabs(res0) ? epsabs : epsrel * fabs(res0);
     int ier = 0;
     if (err0 <= 100 * DBL_EPSILON * resabs0 && err0 > tol) ier = 2;
-    else if ((err0 <= tol && err0 != resasc0) || err0 == 0.0) { *result = res0; *abserr = err0; free(alist); free(iord); return 0; }
+    else if ((err0 <= tol && err0 != resasc0) || err0 == 0.0) { orc_qags_hist[0]++; *result = res0; *abserr = err0; free(alist); free(iord); return 0; }
     else if (limit == 1) ier = 1;
     if (ier) { *result = res0; *abserr = err0; free(alist); free(iord); return ier; }
 
@@ -461,6 +462,10 @@ static int qags_core(orc_fn f, void *p, double a, double b, double epsabs, doubl
         *result = s;
         *abserr = errsum;
     }
+    {
+        int L = last + 1, b = L <= 1 ? 0 : L <= 4 ? 1 : L <= 8 ? 2 : L <= 16 ? 3 : L <= 32 ? 4 : L <= 64 ? 5 : L <= 128 ? 6 : 7;
+        orc_qags_hist[b]++;
+    }
     if (ier > 2) ier--;
     free(alist);
     free(iord);
@@ -471,6 +476,11 @@ int orc_qags(orc_fn f, void *p, double a, double b, double epsabs, double epsrel
              double *result, double *abserr)
 {
     return qags_core(f, p, a, b, epsabs, epsrel, limit, 21, result, abserr);
+}
+
+void orc_qags_histogram(int *out8)
+{
+    for (int i = 0; i < 8; i++) out8[i] = orc_qags_hist[i];
 }
 
 int orc_qagiu(orc_fn f, void *p, double a, double epsabs, double epsrel, int limit,

@@ -1,0 +1,89 @@
+"""The CPU oracle against fixtures produced by the reference's own sources
+(tests/golden/make_golden.py): potential, Poisson, focal-distance table,
+actions, moments, one full iteration's coefficients and the virial sums."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.conftest import load_golden
+from tests.helpers import _nan_diff, oracle_model, rel, rel_rows
+
+SCENARIOS = ["hern_dpl", "nfw_dpl_rot", "hern_qiso"]
+
+
+@pytest.mark.parametrize("name", SCENARIOS)
+def test_setup_matches_reference(name):
+    g, meta, pts = load_golden(name)
+    nr, ng, npl = meta["nr"], meta["ng"], meta["np"]
+    p = meta["p"]
+    ar = O.log_grid(meta["rmin"], meta["rmax"], nr)
+    assert rel(ar, g["ar"]) == 0.0
+    rhl = O.guess_rhl(ar, ng, npl, p["model"], p["mass"], p["r0"])
+    assert rel_rows(rhl, g["guess_rhl"].reshape(nr, npl)) < 1e-14
+    phil, Pr, Pr2 = O.compute_phil(ar, rhl)
+    for a, key in ((phil, "guess_phil"), (Pr, "guess_Pr"), (Pr2, "guess_Pr2")):
+        assert rel_rows(a, g[key].reshape(nr, npl)) < 1e-13, key
+    m = oracle_model(g, meta, phil, Pr, Pr2)
+    P = [(float(a[1]), float(a[2])) for a in pts if a[0] == "P"]
+    pv = np.array([[m.phi(R, z), m.dR(R, z), m.dz(R, z)] for R, z in P]).ravel()
+    assert rel(pv, g["pot_points"]) < 1e-13
+    E, D, fail = m.tabulate_delta(30)
+    assert rel(E, g["Egrid"]) < 1e-12 and rel(D, g["Dgrid"]) < 1e-9
+
+
+@pytest.mark.parametrize("name", SCENARIOS)
+def test_actions_match_reference(name):
+    g, meta, pts = load_golden(name)
+    nr, npl = meta["nr"], meta["np"]
+    m = oracle_model(g, meta, g["guess_phil"].reshape(nr, npl), g["guess_Pr"].reshape(nr, npl),
+                     g["guess_Pr2"].reshape(nr, npl))
+    out = []
+    for a in pts:
+        if a[0] != "A":
+            continue
+        R, z, vR, vp, vz = map(float, a[1:])
+        Phi = m.phi(R, z)
+        if 0.5 * (vR * vR + vp * vp + vz * vz) + Phi >= 0:
+            out += [-1, -1]
+        else:
+            out += list(m.actions(R, z, vR, vp, vz))
+    assert rel(out, g["actions"]) < 1e-10
+
+
+@pytest.mark.parametrize("name", SCENARIOS)
+def test_point_moments_match_reference(name):
+    g, meta, pts = load_golden(name)
+    nr, npl = meta["nr"], meta["np"]
+    m = oracle_model(g, meta, g["guess_phil"].reshape(nr, npl), g["guess_Pr"].reshape(nr, npl),
+                     g["guess_Pr2"].reshape(nr, npl))
+    M = [(float(a[1]), float(a[2])) for a in pts if a[0] == "M"]
+    got = np.array([m.rhofDF(R, z)[0] for R, z in M])
+    ref = g["moments"].reshape(-1, 6)
+    # rho and the even second moments to rounding; vrot/sigRz are differences of
+    # near-cancelling sums (the reference sums them in OpenMP order)
+    assert rel(got[:, [0, 2, 3, 4]], ref[:, [0, 2, 3, 4]]) < 1e-12
+    assert np.max(np.abs(got[:, 1] - ref[:, 1])) < 1e-8 * np.max(np.abs(ref[:, 2]))
+
+
+@pytest.mark.parametrize("name", SCENARIOS)
+def test_first_iteration_matches_reference(name):
+    g, meta, pts = load_golden(name)
+    nr, ng, npl = meta["nr"], meta["ng"], meta["np"]
+    m = oracle_model(g, meta, g["guess_phil"].reshape(nr, npl), g["guess_Pr"].reshape(nr, npl),
+                     g["guess_Pr2"].reshape(nr, npl))
+    grids, st = m.moment_grid()
+    assert st["failures"] == 0
+    coef, _ = O.project6(g["ar"], ng, npl, grids)
+    for q, key in enumerate(("rhl", "sigRl", "sigpl", "sigzl")):
+        qq = {"rhl": 0, "sigRl": 2, "sigpl": 3, "sigzl": 4}[key]
+        assert rel_rows(coef[qq], g["it0_" + key].reshape(nr, npl)) < 1e-12, key
+    phil, Pr, Pr2 = O.compute_phil(g["ar"], coef[0].reshape(nr, npl))
+    for a, key in ((phil, "it0_phil"), (Pr, "it0_Pr"), (Pr2, "it0_Pr2")):
+        assert rel_rows(a, g[key].reshape(nr, npl)) < 1e-11, key
+    # virial sums (printed by the reference with %f)
+    m1 = oracle_model(g, meta, phil, Pr, Pr2)
+    v = m1.vir2(coef)
+    K = v["KRR"] + v["Kzz"]
+    mine = [v["mass_pr"], v["mass_sum"], K, v["pot"], v["pot"] / K, v["KRR"], v["WRR"], v["WRR"] / v["KRR"],
+            v["Kzz"], v["Wzz"], v["Wzz"] / v["Kzz"]]
+    assert np.max(_nan_diff(np.array(mine), g["vir2"][0])) < 1.5e-6

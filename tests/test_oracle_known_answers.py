@@ -1,0 +1,67 @@
+"""Known-answer tests of the oracle's numerics, independent of the reference:
+Legendre recurrences, Gauss-Legendre nodes, QUADPACK QAGS/QAGIU against
+scipy's QUADPACK, Brent, and the Poisson solve of analytic densities."""
+import numpy as np
+import pytest
+from scipy import integrate, special
+
+from oracle import oracle as O
+
+
+def test_even_legendre_against_scipy():
+    import ctypes as C
+    L = O.lib()
+    for c in (0.0, 0.3, -0.77, 0.999):
+        pol = np.zeros(12)
+        L.orc_evenlegend(12, c, pol.ctypes.data_as(O.DP))
+        ref = [special.eval_legendre(2 * k, c) for k in range(12)]
+        assert np.allclose(pol, ref, rtol=1e-12, atol=1e-14)
+
+
+def test_gauleg_against_numpy():
+    x, w = O.gauleg(0, 1, 30)
+    xr, wr = np.polynomial.legendre.leggauss(30)
+    assert np.allclose(x, (xr + 1) / 2, atol=1e-15)
+    # the reference stops Newton at |dz| <= 3e-11 and takes the weight from the last derivative
+    assert np.allclose(w, wr / 2, rtol=1e-9)
+
+
+@pytest.mark.parametrize("f,a,b", [(np.sqrt, 0.0, 1.0), (lambda x: np.log(x) if x > 0 else 0.0, 0.0, 1.0),
+                                   (lambda x: x ** -0.5 if x > 0 else 0.0, 0.0, 1.0),
+                                   (lambda x: np.sin(50 * x) * x, 0.0, 3.0)])
+def test_qags_matches_quadpack(f, a, b):
+    r, e, st = O.qags(f, a, b, 1e-10, 1e-10, 1000)
+    s = integrate.quad(f, a, b, epsabs=1e-10, epsrel=1e-10, limit=1000)
+    assert st == 0 and r == pytest.approx(s[0], rel=1e-14, abs=1e-15)
+
+
+def test_qagiu_matches_quadpack():
+    f = lambda x: np.exp(-x) / (1 + x * x)  # noqa: E731
+    r, e, st = O.qagiu(f, 0.5, 1e-10, 1e-10)
+    s = integrate.quad(f, 0.5, np.inf, epsabs=1e-10, epsrel=1e-10)
+    assert st == 0 and r == pytest.approx(s[0], rel=1e-14)
+
+
+def test_brent_wrapper_rule():
+    r, st = O.brent(lambda x: x ** 3 - 2, 0.0, 3.0)
+    assert st == 0 and abs(r - 2 ** (1 / 3)) < 1e-8
+    r, st = O.brent(lambda x: x - 1e-4, 0.0, 1.0)  # |f(lo)| < 5e-4: the end point is returned
+    assert r == 0.0
+
+
+# radial force dPhi/dr = G M(<r) / r^2 of the analytic models (G = M = r0 = 1)
+@pytest.mark.parametrize("model,force", [
+    ("Hernquist", lambda r: 1 / (r + 1) ** 2),
+    ("Isochrone", lambda r: r / (np.sqrt(1 + r * r) * (1 + np.sqrt(1 + r * r)) ** 2)),
+    ("NFW", lambda r: (np.log(1 + r) - r / (1 + r)) / r ** 2),
+])
+def test_poisson_of_analytic_densities_converges(model, force):
+    errs = []
+    for nr in (60, 240):
+        ar = O.log_grid(1e-3, 200.0, nr)
+        rhl = O.guess_rhl(ar, 10, 3, model)
+        p, pr, _ = O.compute_phil(ar, rhl)
+        sel = (ar > 0.05) & (ar < 20)
+        errs.append(np.max(np.abs(pr[sel, 0] / force(ar[sel]) - 1)))
+        assert np.max(np.abs(p[sel, 1:])) < 1e-6 * np.max(np.abs(p[sel, 0]))  # spherical: no l > 0 terms
+    assert errs[1] < errs[0] / 4 and errs[1] < 5e-3  # linear interpolation of rho: ~second order
