@@ -50,18 +50,18 @@ __device__ __forceinline__ double linterp_col(const double *ar, const double *rh
     return yb + (x - ar[bot]) / (ar[top] - ar[bot]) * (yt - yb);
 }
 
-struct IInternal {  // I_internal (pot/Potential.cpp:83-89)
-    const double *ar, *rhl; int npoly, l, nr;
-    __device__ double operator()(double x) const { return pow(x, l + 2) * linterp_col(ar, rhl, npoly, l, nr, x); }
+struct IInternal {  // I_internal (pot/Potential.cpp:83-89); multipole column col, degree l = 2*col
+    const double *ar, *rhl; int npoly, col, l, nr;
+    __device__ double operator()(double x) const { return pow(x, l + 2) * linterp_col(ar, rhl, npoly, col, nr, x); }
 };
 struct IExternalT {  // I_external (pot/Potential.cpp:90-101) on x = a + (1-t)/t, divided by t^2
-    const double *ar, *rhl; int npoly, l, nr; double a;
+    const double *ar, *rhl; int npoly, col, l, nr; double a;
     __device__ double operator()(double t) const
     {
         const double x = a + (1 - t) / t;
         double rhol;
-        if (x > ar[nr - 1]) rhol = dmax(0., rhl[(nr - 1) * npoly + l] * pow(ar[nr - 1] / x, 4));
-        else rhol = linterp_col(ar, rhl, npoly, l, nr, x);
+        if (x > ar[nr - 1]) rhol = dmax(0., rhl[(nr - 1) * npoly + col] * pow(ar[nr - 1] / x, 4));
+        else rhol = linterp_col(ar, rhl, npoly, col, nr, x);
         const double y = rhol / pow(x, l - 1);
         return (y / t) / t;
     }
@@ -85,9 +85,9 @@ __global__ void k_poisson(int nr, int npoly, const double *ar, const double *rhl
     const QagsWs W{dws, dws + kPoissonCap, dws + 2 * kPoissonCap, dws + 3 * kPoissonCap, iws, kPoissonCap};
     unsigned fail = 0;
     double Iint, Iext, err;
-    IInternal fi{ar, rhl, npoly, l, nr};
+    IInternal fi{ar, rhl, npoly, np, l, nr};
     qags<21>(fi, 0., ar[n], 1e-4, 1e-3, 1000, Iint, err, fail, W);
-    IExternalT fe{ar, rhl, npoly, l, nr, ar[n]};
+    IExternalT fe{ar, rhl, npoly, np, l, nr, ar[n]};
     double epsabs = 1e-4, epsrel = 1e-3;
     int status = 1, tries = 0;
     while (status != 0 && tries < 60) {
