@@ -57,6 +57,7 @@ SIGNATURES = {
     "fj_ctx_create": ([C.c_int, P(C.c_void_p)], C.c_int),
     "fj_ctx_destroy": ([CTX], C.c_int),
     "fj_ctx_set_stream": ([CTX, C.c_void_p], C.c_int),
+    "fj_ctx_own_stream": ([CTX], C.c_void_p),
     "fj_ctx_synchronize": ([CTX], C.c_int),
     "fj_last_error": ([CTX], C.c_char_p),
     "fj_moments": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule), C.c_int,

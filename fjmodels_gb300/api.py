@@ -112,12 +112,21 @@ class Context:
         except Exception:
             pass
 
+    def _on_torch_stream(self):
+        """Order library work after torch's work on the current stream (where the
+        tensors' copies were queued)."""
+        import torch
+        self.lib.fj_ctx_set_stream(self.h, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+
     def _check(self, rc, what):
         if rc != A.FJ_OK:
             raise FJError(f"{what} failed ({rc}): {self.lib.fj_last_error(self.h).decode()}")
 
     def sync(self):
         self._check(self.lib.fj_ctx_synchronize(self.h), "synchronize")
+
+    def use_own_stream(self):
+        self.lib.fj_ctx_set_stream(self.h, self.lib.fj_ctx_own_stream(self.h))
 
     # ---------------------------------------------------------------- structs
     @staticmethod
@@ -132,12 +141,14 @@ class Context:
     # ---------------------------------------------------------------- hot path
     def moments(self, pot, delta, df, rule, ngauss, grids6):
         """rhofDF over the meridional grid (pot/potLeg.cpp:54-58)."""
+        self._on_torch_stream()
         st = A.fj_moment_stats()
         self._check(self.lib.fj_moments(self.h, C.byref(pot), C.byref(delta), C.byref(df.c), C.byref(rule.c),
                                         ngauss, _ptr(grids6), C.byref(st)), "fj_moments")
         return st
 
     def moments_points(self, pot, delta, df, rule, Rz, out6):
+        self._on_torch_stream()
         st = A.fj_moment_stats()
         self._check(self.lib.fj_moments_points(self.h, C.byref(pot), C.byref(delta), C.byref(df.c),
                                                C.byref(rule.c), _ptr(Rz), Rz.shape[0], _ptr(out6), C.byref(st)),
@@ -145,20 +156,24 @@ class Context:
         return st
 
     def legendre_project(self, nr, ngauss, npoly, ar, grids6, coef6):
+        self._on_torch_stream()
         self._check(self.lib.fj_legendre_project(self.h, nr, ngauss, npoly, _ptr(ar), _ptr(grids6), _ptr(coef6)),
                     "fj_legendre_project")
 
     def computePhil(self, ar, rhl, phil, Pr, Pr2):
+        self._on_torch_stream()
         nr = ar.numel()
         self._check(self.lib.fj_poisson(self.h, nr, rhl.numel() // nr, _ptr(ar), _ptr(rhl), _ptr(phil), _ptr(Pr),
                                         _ptr(Pr2)), "fj_poisson")
 
     def updatePhil(self, a3, b3, out3):
+        self._on_torch_stream()
         n = a3[0].numel()
         self._check(self.lib.fj_sum_potentials(self.h, n, *[_ptr(t) for t in (*a3, *b3, *out3)]),
                     "fj_sum_potentials")
 
     def computeNewPhi(self, pot, delta, df, rule, ngauss, grids6, coef6, phil, Pr, Pr2):
+        self._on_torch_stream()
         st = A.fj_moment_stats()
         self._check(self.lib.fj_compute_new_phi(self.h, C.byref(pot), C.byref(delta), C.byref(df.c),
                                                 C.byref(rule.c), ngauss, _ptr(grids6), _ptr(coef6), _ptr(phil),
@@ -166,14 +181,17 @@ class Context:
         return st
 
     def uvOrb_actions(self, pot, delta, pts, out, jquad=A.FJ_JQUAD_QAGS):
+        self._on_torch_stream()
         self._check(self.lib.fj_actions(self.h, C.byref(pot), C.byref(delta), _ptr(pts), pts.shape[0], jquad,
                                         _ptr(out)), "fj_actions")
 
     def potential_eval(self, pot, Rz, out):
+        self._on_torch_stream()
         self._check(self.lib.fj_potential_eval(self.h, C.byref(pot), _ptr(Rz), Rz.shape[0], _ptr(out)),
                     "fj_potential_eval")
 
     def vir2(self, pot, ngauss, coef6):
+        self._on_torch_stream()
         out = np.zeros(7)
         self._check(self.lib.fj_vir2(self.h, C.byref(pot), ngauss, _ptr(coef6), _dp(out)), "fj_vir2")
         return dict(zip(("KRR", "Kzz", "WRR", "Wzz", "pot", "mass_pr", "mass_sum"), out))
@@ -182,6 +200,7 @@ class Context:
     def run_model(self, nr, ngauss, npoly, rmin, rmax, df, rule, itermax, tol=0.0, ngrid=30, q=1.0,
                   keep_grids=False):
         """One-component self-consistent model (fJmodels.cpp:86-144) with host buffers."""
+        self.use_own_stream()
         cfg = A.fj_model_config(nr, ngauss, npoly, ngrid, rmin, rmax, A.FJ_GUESS.get(df.model, 0), df.mass, df.r0,
                                 q, df.c, rule.c, itermax, tol)
         out = {"ar": np.zeros(nr), "coef6": np.zeros((6, nr, npoly)), "phil": np.zeros((nr, npoly)),

@@ -260,7 +260,7 @@ int fj_ctx_create(int device, fj_ctx **out)
     if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) return FJ_ERR_NODEVICE;
     fj_ctx *c = new fj_ctx;
     c->device = device;
-    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess ||
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->own, cudaStreamDefault) != cudaSuccess ||
         cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
         delete c;
         return FJ_ERR_CUDA;
@@ -290,9 +290,11 @@ int fj_ctx_destroy(fj_ctx *ctx)
 int fj_ctx_set_stream(fj_ctx *ctx, void *stream)
 {
     if (!ctx) return FJ_ERR_ARG;
-    ctx->stream = stream ? (cudaStream_t)stream : ctx->own;
+    ctx->stream = (cudaStream_t)stream;
     return FJ_OK;
 }
+
+void *fj_ctx_own_stream(fj_ctx *ctx) { return ctx ? (void *)ctx->own : nullptr; }
 
 int fj_ctx_synchronize(fj_ctx *ctx)
 {

@@ -101,8 +101,13 @@ typedef struct fj_moment_stats {
 const char *fj_version(void);
 int fj_ctx_create(int device, fj_ctx **out);
 int fj_ctx_destroy(fj_ctx *ctx);
-/* Use an existing cudaStream_t (passed as void*) for subsequent work; NULL = the context's own stream. */
+/* Order subsequent work on the given cudaStream_t (passed as void*, used as
+   is: NULL is the legacy default stream).  A new context works on its own
+   stream, which is a blocking stream and so also orders after work on the
+   legacy default stream. */
 int fj_ctx_set_stream(fj_ctx *ctx, void *stream);
+/* The context's own stream (to go back to it with fj_ctx_set_stream). */
+void *fj_ctx_own_stream(fj_ctx *ctx);
 int fj_ctx_synchronize(fj_ctx *ctx);
 const char *fj_last_error(fj_ctx *ctx);
 

@@ -18,7 +18,7 @@ from tests.helpers import rel, rel_rows
 def declared_functions():
     src = open(os.path.join(ROOT, "include", "fjgpu.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(fj_\w+)\s*\(", src, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*|void \*)\s*(fj_\w+)\s*\(", src, flags=re.M)))
 
 
 def test_library_exports_every_declared_symbol():
