@@ -266,6 +266,22 @@ int fj_ctx_create(int device, fj_ctx **out)
         return FJ_ERR_CUDA;
     }
     c->stream = c->own;
+    // The phase-space kernels keep the QAGS interval list on the per-thread
+    // stack (about 5.5 KB); raise this process's stack limit to cover the
+    // largest kernel, as the default (1 KB) is not raised for them on launch.
+    size_t need = moments_local_bytes();
+    const size_t need2 = multipole_local_bytes();
+    if (need2 > need) need = need2;
+    need = (need + 1024 + 1023) / 1024 * 1024;
+    size_t cur = 0;
+    if (cudaDeviceGetLimit(&cur, cudaLimitStackSize) != cudaSuccess ||
+        (cur < need && cudaDeviceSetLimit(cudaLimitStackSize, need) != cudaSuccess)) {
+        cudaEventDestroy(c->ev0);
+        cudaEventDestroy(c->ev1);
+        cudaStreamDestroy(c->own);
+        delete c;
+        return FJ_ERR_CUDA;
+    }
     *out = c;
     return FJ_OK;
 }

@@ -49,4 +49,8 @@ cudaError_t launch_sum3(int n, const double *a0, const double *a1, const double 
 cudaError_t launch_vir2(PotView P, int ngauss, const double *ci, const double *wi, const double *coef6,
                         double *out7, cudaStream_t s);
 
+// largest per-thread local memory (stack) any kernel of the library needs
+size_t moments_local_bytes();
+size_t multipole_local_bytes();
+
 }  // namespace fj

@@ -183,4 +183,14 @@ cudaError_t launch_potential_eval(PotView P, const double *Rz, size_t n, double 
     return cudaGetLastError();
 }
 
+size_t moments_local_bytes()
+{
+    size_t m = 0;
+    cudaFuncAttributes at;
+    if (cudaFuncGetAttributes(&at, k_moments) == cudaSuccess && at.localSizeBytes > m) m = at.localSizeBytes;
+    if (cudaFuncGetAttributes(&at, k_actions) == cudaSuccess && at.localSizeBytes > m) m = at.localSizeBytes;
+    if (cudaFuncGetAttributes(&at, k_potential_eval) == cudaSuccess && at.localSizeBytes > m) m = at.localSizeBytes;
+    return m;
+}
+
 }  // namespace fj

@@ -227,4 +227,13 @@ cudaError_t launch_vir2(PotView P, int ngauss, const double *ci, const double *w
     return cudaGetLastError();
 }
 
+size_t multipole_local_bytes()
+{
+    size_t m = 0;
+    cudaFuncAttributes at;
+    if (cudaFuncGetAttributes(&at, k_poisson) == cudaSuccess && at.localSizeBytes > m) m = at.localSizeBytes;
+    if (cudaFuncGetAttributes(&at, k_vir2) == cudaSuccess && at.localSizeBytes > m) m = at.localSizeBytes;
+    return m;
+}
+
 }  // namespace fj
