@@ -86,6 +86,10 @@ FJ_HD void interp_setup(const PotView &P, double r, Interp &I)
 {
     const double *ar = P.ar;
     const int nr = P.nr;
+    // every field is set on both branches: the callers' ternaries read both
+    I.bot = I.top = I.thr = 0;
+    I.f1 = I.f2 = I.f3 = 0.0;
+    I.x = 0.0;
     if (r >= ar[nr - 1]) { I.ext = true; I.quad = false; I.x = ar[nr - 1] / r; return; }
     I.ext = false;
     int top = 0, bot = 0;
