@@ -90,6 +90,15 @@ class Rule:
         self.c = A.fj_quad_rule(len(self.xq), _dp(self.xq), _dp(self.wq), jquad, precision)
 
 
+class DeviceTables:
+    """A C-ABI struct of device pointers together with the tensors that own the memory
+    (the struct alone would let the caching allocator reuse it under a queued kernel)."""
+
+    def __init__(self, c, owners):
+        self.c = c
+        self.owners = owners
+
+
 class Context:
     """One CUDA context/stream of libfjgpu (fj_ctx)."""
 
@@ -131,26 +140,28 @@ class Context:
     # ---------------------------------------------------------------- structs
     @staticmethod
     def potential(ar, phil, Pr, Pr2):
-        npoly = phil.numel() // ar.numel()
-        return A.fj_potential(ar.numel(), npoly, _ptr(ar), _ptr(phil), _ptr(Pr), _ptr(Pr2))
+        """Device multipole potential; the returned object keeps the tensors alive."""
+        return DeviceTables(A.fj_potential(ar.numel(), phil.numel() // ar.numel(), _ptr(ar), _ptr(phil), _ptr(Pr),
+                                           _ptr(Pr2)), (ar, phil, Pr, Pr2))
 
     @staticmethod
     def delta(Egrid, Dgrid):
-        return A.fj_delta_table(Egrid.numel(), _ptr(Egrid), _ptr(Dgrid))
+        """Device focal-distance table; the returned object keeps the tensors alive."""
+        return DeviceTables(A.fj_delta_table(Egrid.numel(), _ptr(Egrid), _ptr(Dgrid)), (Egrid, Dgrid))
 
     # ---------------------------------------------------------------- hot path
     def moments(self, pot, delta, df, rule, ngauss, grids6):
         """rhofDF over the meridional grid (pot/potLeg.cpp:54-58)."""
         self._on_torch_stream()
         st = A.fj_moment_stats()
-        self._check(self.lib.fj_moments(self.h, C.byref(pot), C.byref(delta), C.byref(df.c), C.byref(rule.c),
+        self._check(self.lib.fj_moments(self.h, C.byref(pot.c), C.byref(delta.c), C.byref(df.c), C.byref(rule.c),
                                         ngauss, _ptr(grids6), C.byref(st)), "fj_moments")
         return st
 
     def moments_points(self, pot, delta, df, rule, Rz, out6):
         self._on_torch_stream()
         st = A.fj_moment_stats()
-        self._check(self.lib.fj_moments_points(self.h, C.byref(pot), C.byref(delta), C.byref(df.c),
+        self._check(self.lib.fj_moments_points(self.h, C.byref(pot.c), C.byref(delta.c), C.byref(df.c),
                                                C.byref(rule.c), _ptr(Rz), Rz.shape[0], _ptr(out6), C.byref(st)),
                     "fj_moments_points")
         return st
@@ -175,25 +186,25 @@ class Context:
     def computeNewPhi(self, pot, delta, df, rule, ngauss, grids6, coef6, phil, Pr, Pr2):
         self._on_torch_stream()
         st = A.fj_moment_stats()
-        self._check(self.lib.fj_compute_new_phi(self.h, C.byref(pot), C.byref(delta), C.byref(df.c),
+        self._check(self.lib.fj_compute_new_phi(self.h, C.byref(pot.c), C.byref(delta.c), C.byref(df.c),
                                                 C.byref(rule.c), ngauss, _ptr(grids6), _ptr(coef6), _ptr(phil),
                                                 _ptr(Pr), _ptr(Pr2), C.byref(st)), "fj_compute_new_phi")
         return st
 
     def uvOrb_actions(self, pot, delta, pts, out, jquad=A.FJ_JQUAD_QAGS):
         self._on_torch_stream()
-        self._check(self.lib.fj_actions(self.h, C.byref(pot), C.byref(delta), _ptr(pts), pts.shape[0], jquad,
+        self._check(self.lib.fj_actions(self.h, C.byref(pot.c), C.byref(delta.c), _ptr(pts), pts.shape[0], jquad,
                                         _ptr(out)), "fj_actions")
 
     def potential_eval(self, pot, Rz, out):
         self._on_torch_stream()
-        self._check(self.lib.fj_potential_eval(self.h, C.byref(pot), _ptr(Rz), Rz.shape[0], _ptr(out)),
+        self._check(self.lib.fj_potential_eval(self.h, C.byref(pot.c), _ptr(Rz), Rz.shape[0], _ptr(out)),
                     "fj_potential_eval")
 
     def vir2(self, pot, ngauss, coef6):
         self._on_torch_stream()
         out = np.zeros(7)
-        self._check(self.lib.fj_vir2(self.h, C.byref(pot), ngauss, _ptr(coef6), _dp(out)), "fj_vir2")
+        self._check(self.lib.fj_vir2(self.h, C.byref(pot.c), ngauss, _ptr(coef6), _dp(out)), "fj_vir2")
         return dict(zip(("KRR", "Kzz", "WRR", "Wzz", "pot", "mass_pr", "mass_sum"), out))
 
     # ---------------------------------------------------------------- whole model
@@ -245,7 +256,7 @@ def tabulate_delta(ar, phil, Pr, Pr2, ngrid=30):
     pot = A.fj_potential(len(ar), phil.size // len(ar), ar.ctypes.data, phil.ctypes.data, Pr.ctypes.data,
                          Pr2.ctypes.data)
     E, D = np.zeros(ngrid), np.zeros(ngrid)
-    rc = A.load().fj_tabulate_delta(C.byref(pot), ngrid, _dp(E), _dp(D))
+    rc = A.load().fj_tabulate_delta(C.byref(pot.c), ngrid, _dp(E), _dp(D))
     return E, D, rc
 
 
