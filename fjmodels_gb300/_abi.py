@@ -41,7 +41,8 @@ class fj_model_config(C.Structure):
     _fields_ = [("nr", C.c_int), ("ngauss", C.c_int), ("npoly", C.c_int), ("ngrid", C.c_int),
                 ("rmin", C.c_double), ("rmax", C.c_double), ("guess", C.c_int),
                 ("mass", C.c_double), ("r0", C.c_double), ("q", C.c_double),
-                ("df", fj_df_params), ("rule", fj_quad_rule), ("itermax", C.c_int), ("tol", C.c_double)]
+                ("df", fj_df_params), ("rule", fj_quad_rule), ("itermax", C.c_int), ("tol", C.c_double),
+                ("Egrid_in", DP), ("Dgrid_in", DP)]
 
 
 class fj_model_result(C.Structure):

@@ -209,11 +209,13 @@ class Context:
 
     # ---------------------------------------------------------------- whole model
     def run_model(self, nr, ngauss, npoly, rmin, rmax, df, rule, itermax, tol=0.0, ngrid=30, q=1.0,
-                  keep_grids=False):
-        """One-component self-consistent model (fJmodels.cpp:86-144) with host buffers."""
+                  keep_grids=False, delta_table=None):
+        """One-component self-consistent model (fJmodels.cpp:86-144) with host buffers.
+        delta_table = (Egrid, Dgrid) uses a given focal-distance table instead of tabulating one."""
         self.use_own_stream()
+        din = [None, None] if delta_table is None else [_f64(delta_table[0]), _f64(delta_table[1])]
         cfg = A.fj_model_config(nr, ngauss, npoly, ngrid, rmin, rmax, A.FJ_GUESS.get(df.model, 0), df.mass, df.r0,
-                                q, df.c, rule.c, itermax, tol)
+                                q, df.c, rule.c, itermax, tol, *[_dp(d) if d is not None else None for d in din])
         out = {"ar": np.zeros(nr), "coef6": np.zeros((6, nr, npoly)), "phil": np.zeros((nr, npoly)),
                "Pr": np.zeros((nr, npoly)), "Pr2": np.zeros((nr, npoly)), "Egrid": np.zeros(ngrid),
                "Dgrid": np.zeros(ngrid)}
@@ -256,7 +258,7 @@ def tabulate_delta(ar, phil, Pr, Pr2, ngrid=30):
     pot = A.fj_potential(len(ar), phil.size // len(ar), ar.ctypes.data, phil.ctypes.data, Pr.ctypes.data,
                          Pr2.ctypes.data)
     E, D = np.zeros(ngrid), np.zeros(ngrid)
-    rc = A.load().fj_tabulate_delta(C.byref(pot.c), ngrid, _dp(E), _dp(D))
+    rc = A.load().fj_tabulate_delta(C.byref(pot), ngrid, _dp(E), _dp(D))
     return E, D, rc
 
 

@@ -14,10 +14,16 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfjgpu.so")
-SOURCES = ["fj_moments.cu", "fj_multipole.cu", "fj_api.cu"]
+# Per translation unit: the FP64 plain form and the multipole kernels are built
+# without FMA contraction.  The reference's algorithm has rounding-sensitive
+# branches (bracket sign tests, the |f| < 5e-4 root shortcut, the switch of the
+# quadratic interpolation point at mid-interval); with contracted arithmetic
+# they take the other branch at a few nodes and densities move by ~1e-7,
+# exactly as the reference's own sources do when compiled with contraction.
+SOURCES = {"fj_moments.cu": ["--fmad=false"], "fj_multipole.cu": ["--fmad=false"], "fj_api.cu": []}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-         "-Xcompiler", "-Wall,-Wno-unused-function"]
+         "-Xcompiler", "-Wall,-Wno-unused-function,-ffp-contract=off"]
 
 
 def nvcc():
@@ -49,7 +55,7 @@ def build(verbose=False, force=False):
 
     def one(src):
         obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-        cmd = [cc, *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [cc, *ARCH, *FLAGS, *SOURCES[src], "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         r = subprocess.run(cmd, capture_output=True, text=True)

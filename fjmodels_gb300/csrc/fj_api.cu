@@ -267,12 +267,13 @@ int fj_ctx_create(int device, fj_ctx **out)
     }
     c->stream = c->own;
     // The phase-space kernels keep the QAGS interval list on the per-thread
-    // stack (about 5.5 KB); raise this process's stack limit to cover the
-    // largest kernel, as the default (1 KB) is not raised for them on launch.
+    // call stack (about 5.5 KB, ptxas "cumulative stack size"); the function
+    // attributes do not report call-stack frames, so the floor is explicit.
     size_t need = moments_local_bytes();
     const size_t need2 = multipole_local_bytes();
     if (need2 > need) need = need2;
     need = (need + 1024 + 1023) / 1024 * 1024;
+    if (need < kStackBytes) need = kStackBytes;
     size_t cur = 0;
     if (cudaDeviceGetLimit(&cur, cudaLimitStackSize) != cudaSuccess ||
         (cur < need && cudaDeviceSetLimit(cudaLimitStackSize, need) != cudaSuccess)) {
@@ -782,7 +783,10 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
     FJ_CUDA(cudaMemcpyAsync(hp.data(), potA, 3 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
     FJ_CUDA(cudaStreamSynchronize(s));
     fj_potential hpot{nr, npl, res->ar, hp.data(), hp.data() + nt, hp.data() + 2 * nt};
-    fj_tabulate_delta(&hpot, ngrid, res->Egrid, res->Dgrid);
+    if (cfg->Egrid_in && cfg->Dgrid_in) {
+        memcpy(res->Egrid, cfg->Egrid_in, ngrid * sizeof(double));
+        memcpy(res->Dgrid, cfg->Dgrid_in, ngrid * sizeof(double));
+    } else fj_tabulate_delta(&hpot, ngrid, res->Egrid, res->Dgrid);
     FJ_CUDA(cudaMemcpyAsync(d_Eg, res->Egrid, ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
     FJ_CUDA(cudaMemcpyAsync(d_Dg, res->Dgrid, ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
     fj_delta_table dt{ngrid, d_Eg, d_Dg};

@@ -8,6 +8,11 @@
 namespace fj {
 
 constexpr int kMomentBlock = 128;  // threads per block of the phase-space kernel
+// per-thread stack the kernels need: the QAGS interval list (kQagsCap entries
+// of four doubles and an int), the epsilon table and the call frames
+constexpr size_t kStackBytes = 8192;
+static_assert(kQagsCap * (4 * sizeof(double) + sizeof(int)) + 52 * sizeof(double) + 1024 < kStackBytes,
+              "stack floor below the QAGS workspace");
 
 // Arguments of the phase-space (moment) kernel.  All pointers are device memory.
 struct MomentArgs {

@@ -204,6 +204,8 @@ typedef struct fj_model_config {
     fj_quad_rule rule;           /* host arrays */
     int itermax;                 /* iterations */
     double tol;                  /* stop when max|dphil/phil_0| < tol (UtilsLeg.h:266-278); <= 0: run itermax */
+    const double *Egrid_in;      /* optional host focal-distance table [ngrid] to use instead of */
+    const double *Dgrid_in;      /* tabulating it from the guess potential; NULL: tabulate       */
 } fj_model_config;
 
 typedef struct fj_model_result {

@@ -10,6 +10,8 @@
  *
  * Points file lines: "P R z" (potential and gradient), "A R z vR vphi vz"
  * (actions with Delta from the table, as df() does), "M R z" (rhofDF).
+ * FJREF_DELTA_FILE, when set, names a file with a focal-distance table
+ * (Egrid then Dgrid) used instead of tabulateDelta.
  */
 #include <cstdio>
 #include <cstdlib>
@@ -94,7 +96,13 @@ int main(int argc, char **argv)
         if ((char)v[0] == 'P') { pv.push_back(p(v[1], v[2])); pv.push_back(p.dR(v[1], v[2])); pv.push_back(p.dz(v[1], v[2])); }
     dumpv("pot_points", pv.data(), (int)pv.size());
 
-    tabulateDelta(&p);
+    const char *dfile = getenv("FJREF_DELTA_FILE");
+    if (dfile) {  /* use a given focal-distance table (2*NGRID values: Egrid then Dgrid) */
+        FILE *df = fopen(dfile, "r");
+        for (int i = 0; i < NGRID; i++) if (fscanf(df, "%lf", &Egrid[i]) != 1) return 3;
+        for (int i = 0; i < NGRID; i++) if (fscanf(df, "%lf", &Dgrid[i]) != 1) return 3;
+        fclose(df);
+    } else tabulateDelta(&p);
     dumpv("Egrid", Egrid, NGRID);
     dumpv("Dgrid", Dgrid, NGRID);
 
