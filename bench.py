@@ -1,0 +1,359 @@
+#!/usr/bin/env python
+"""Benchmark: wall-seconds per converged self-consistent model.
+
+Workload (the rotating NFW configuration): one NFW component with the
+double-power-law DF (dphi_h = dz_h = 0.55, dphi_g = dz_g = 1, chi = 1,
+k = 0.5, M = r0 = 1), 80 log radii in [1e-3, 300], 40 polar Gauss-Legendre
+nodes, even multipoles to l = 12 (npoly = 7), the 22-point-per-axis
+tanh-sinh velocity rule (22^3 = 10648 phase-space nodes per grid point) and
+20 self-consistency iterations per model.  Inputs are synthetic: the
+analytic NFW guess density seeds the first potential (pot/models.cpp:53-56).
+
+A step is one self-consistency iteration over the whole meridional grid
+(computeNewPhi: phase-space kernel, Legendre projection, Poisson), chained on
+the device as the reference's loop chains them.  value = wall-seconds per
+converged model = seconds per step x 20 (whole job: / N for N replicas).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form plain|gl]
+  python bench.py --impl reference ...   (the CPU path on this host's cores)
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CFG = dict(model="NFW", nr=80, ngauss=40, npoly=7, rmin=1e-3, rmax=300.0, dphi_h=0.55, dz_h=0.55, dphi_g=1.0,
+           dz_g=1.0, chi=1.0, k=0.5, mass=1.0, r0=1.0, iters_per_model=20, nq=22)
+METRIC = "wall-s per converged model at rho err<=1e-4, chosen vs plain FP64, same GB300"
+UNIT = "s/model"
+# FP64 operations per phase-space evaluation executed by active threads of the
+# phase-space kernel (dadd + dmul + 2*dfma from ncu on the nfw_80x40 workload,
+# profiles/moments_fp64_nfw_80x40.md); the algorithmic work unit of the roofline.
+FP64_FLOPS_PER_EVAL = {"plain": None, "gl": None}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="plain", choices=["plain", "gl"])
+    ap.add_argument("--cpu-sample", type=int, default=os.cpu_count(), help="grid points timed for the CPU baseline")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile-points", type=int, default=0,
+                    help="profiling case: one phase-space launch over this many grid points, no bench line")
+    return ap.parse_args()
+
+
+def dist_init():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+    return rank, world
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            self.p.wait()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        for line in open(self.f.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                try:
+                    rows.append((float(parts[1]), float(parts[2]), parts[4:8]))
+                except ValueError:
+                    pass
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for _, _, r in rows for n, v in zip(names, r) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def velocity_rule():
+    import fjmodels_gb300 as F
+    return F.tanh_sinh_rule(CFG["nq"])
+
+
+def setup_host():
+    """Grid, guess multipoles (host, as the reference does once)."""
+    import fjmodels_gb300 as F
+    ar = F.log_grid(CFG["rmin"], CFG["rmax"], CFG["nr"])
+    rhl = F.guess_rhl(ar, CFG["ngauss"], CFG["npoly"], CFG["model"], CFG["mass"], CFG["r0"])
+    return ar, rhl
+
+
+def run_ours(args, rank, world):
+    import torch
+
+    import fjmodels_gb300 as F
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    ctx = F.Context(dev.index)
+    nr, ng, npl = CFG["nr"], CFG["ngauss"], CFG["npoly"]
+    f64 = dict(dtype=torch.float64, device=dev)
+    ar, rhl = setup_host()
+    d_ar = torch.tensor(ar, **f64)
+    tabs = [torch.zeros((nr, npl), **f64) for _ in range(3)]
+    ctx.computePhil(d_ar, torch.tensor(rhl, **f64), *tabs)
+    torch.cuda.synchronize()
+    E, D, _ = F.tabulate_delta(ar, *[t.cpu().numpy() for t in tabs])
+    delta = ctx.delta(torch.tensor(E, **f64), torch.tensor(D, **f64))
+    x, w = velocity_rule()
+    rule = F.Rule(x, w, jquad=0 if args.form == "plain" else 16)
+    df = F.DFParams(CFG["model"], CFG["dphi_h"], CFG["dz_h"], CFG["dphi_g"], CFG["dz_g"], CFG["chi"], CFG["mass"],
+                    CFG["r0"], k=CFG["k"])
+    grids = torch.zeros((6, nr, ng), **f64)
+    coef = torch.zeros((6, nr, npl), **f64)
+    nxt = [torch.zeros((nr, npl), **f64) for _ in range(3)]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+    state = {"cur": tabs, "nxt": nxt}
+    kernel_ms, changes = [], []
+
+    def step():
+        cur, nx = state["cur"], state["nxt"]
+        pot = ctx.potential(d_ar, *cur)
+        st = ctx.computeNewPhi(pot, delta, df, rule, ng, grids, coef, *nx)
+        kernel_ms.append(st.kernel_ms)
+        changes.append((nx[0] - cur[0]).abs().div(nx[0][:, :1].abs()).max())
+        state["cur"], state["nxt"] = nx, cur
+        flush.zero_()
+        return st
+
+    for _ in range(args.warmup):
+        step()
+    kernel_ms.clear()
+    torch.cuda.synchronize()
+    barrier(world)
+    with ClockSampler(dev.index) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        last = None
+        for _ in range(args.steps):
+            last = step()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+    barrier(world)
+    elapsed = max_over_ranks(t1 - t0, world)
+    ms_per_step = elapsed / args.steps * 1e3
+    value = ms_per_step / 1e3 * CFG["iters_per_model"] / world
+    nodes = last.nodes
+    k_ms = float(np.mean(kernel_ms))
+    peak = np.zeros(1)
+    F.load_library().fj_measure_fma_peak(0, peak.ctypes.data_as(F._abi.DP))
+    flops = FP64_FLOPS_PER_EVAL.get(args.form)
+    achieved = flops * nodes / (k_ms * 1e-3) / 1e12 if flops else None
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic NFW guess density, seeded by construction)",
+        "config": {"workload": f"NFW rotating (chi=1,k=0.5) {nr}x{ng} grid, l<=12, 22^3 tanh-sinh nodes, "
+                               f"{CFG['iters_per_model']} iterations/model",
+                   "form": "plain FP64, QAGS momentum integrals" if args.form == "plain" else
+                   "FP64, 16-point Gauss-Legendre momentum integrals",
+                   "phase_space_evals_per_step": nodes, "bound_evals_per_step": last.bound,
+                   "l2": "256 MiB buffer written between steps", "parallelism": f"replicas{world}"},
+        "phase_space_evals_per_s": nodes / (ms_per_step * 1e-3) * world,
+        "kernel_ms_per_step": k_ms,
+        "potential_change_last": float(changes[-1].item()) if changes else None,
+        "gpu_launches": 4 * args.steps,
+        "roofline": {"bound": "fp64", "kernel": "k_moments", "achieved": achieved, "peak": float(peak[0]),
+                     "unit": "TFLOP/s", "frac": (achieved / peak[0]) if achieved else None,
+                     "peak_source": "fj_measure_fma_peak (FP64 FMA chains, this GPU)",
+                     "flops_per_eval": flops, "traffic": None},
+        "clocks": clk.summary(),
+    }
+    ctx.close()
+    return out, (ar, tabs, delta, rule, df)
+
+
+def e2e_ours(args):
+    """Same metric through the host-buffer C-ABI call (fj_run_model): host inputs, device
+    compute, host outputs, copies inside the timed region.  Two runs (1 and 2 iterations)
+    split the one-time setup from the per-iteration cost."""
+    import torch
+
+    import fjmodels_gb300 as F
+    ctx = F.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    x, w = velocity_rule()
+    rule = F.Rule(x, w, jquad=0 if args.form == "plain" else 16)
+    df = F.DFParams(CFG["model"], CFG["dphi_h"], CFG["dz_h"], CFG["dphi_g"], CFG["dz_g"], CFG["chi"], CFG["mass"],
+                    CFG["r0"], k=CFG["k"])
+    walls = {}
+    for its in (1, 2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.run_model(CFG["nr"], CFG["ngauss"], CFG["npoly"], CFG["rmin"], CFG["rmax"], df, rule, itermax=its)
+        walls[its] = time.perf_counter() - t0
+    ctx.close()
+    per_iter = walls[2] - walls[1]
+    setup = walls[1] - per_iter
+    nr, ng, npl, ngrid = CFG["nr"], CFG["ngauss"], CFG["npoly"], 30
+    h2d = 8 * (nr + nr * npl + 2 * ngrid + 2 * CFG["nq"])
+    d2h_step = 8 * nr * npl
+    return {"value": setup + CFG["iters_per_model"] * per_iter, "unit": UNIT, "setup_s": setup,
+            "s_per_iteration": per_iter, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h_step,
+            "note": "fj_run_model with host buffers; setup (guess, Poisson, focal-distance table) counted once"}
+
+
+def cpu_sample(args, sample=16):
+    """The CPU restatement of the reference (oracle) on a bounded sample of grid points,
+    all host threads (one point per thread), extrapolated to a full iteration and a
+    20-iteration model."""
+    import ctypes as C
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+    nr, ng, npl = CFG["nr"], CFG["ngauss"], CFG["npoly"]
+    ar = O.log_grid(CFG["rmin"], CFG["rmax"], nr)
+    rhl = O.guess_rhl(ar, ng, npl, CFG["model"], CFG["mass"], CFG["r0"])
+    phil, Pr, Pr2 = O.compute_phil(ar, rhl)
+    x, w = velocity_rule()
+    m = O.Model(ar, phil, Pr, Pr2, np.zeros(30), np.zeros(30), ng, alpha=1.667, beta=3.0, mass=CFG["mass"],
+                r0=CFG["r0"], dphi_h=CFG["dphi_h"], dz_h=CFG["dz_h"], dphi_g=CFG["dphi_g"], dz_g=CFG["dz_g"],
+                chi=CFG["chi"], k=CFG["k"], xq=x, wq=w, jquad=0 if args.form == "plain" else 16)
+    E, D, _ = m.tabulate_delta(30)
+    m.Egrid, m.Dgrid = E, D
+    npts = nr * ng
+    idx = np.linspace(0, npts - 1, sample).astype(int)
+    threads = os.cpu_count()
+    out = np.zeros((6, npts))
+    mc = m.c()
+    lib = O.lib()
+
+    def one(p):  # ctypes drops the GIL for the call
+        lib.orc_moment_grid(mc, int(p), int(p) + 1, out.ctypes.data_as(O.DP), 1, C.byref(O.Stats()))
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(one, idx))
+    dt = time.perf_counter() - t0
+    per_iter = dt * npts / sample  # sample points took dt on the host's threads
+    return {"value": per_iter * CFG["iters_per_model"], "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{sample} of {npts} grid points spread over the grid (22^3 nodes each) on "
+                      f"{threads} host threads, one point per thread; extrapolated to {npts} points x "
+                      f"{CFG['iters_per_model']} iterations", "sample_s": dt}
+
+
+def profile_case(args):
+    """One phase-space launch over a spread subset of the workload's grid points
+    (the small case captured by ncu)."""
+    import torch
+
+    import fjmodels_gb300 as F
+    ctx = F.Context(0)
+    nr, ng, npl = CFG["nr"], CFG["ngauss"], CFG["npoly"]
+    f64 = dict(dtype=torch.float64, device="cuda")
+    ar, rhl = setup_host()
+    d_ar = torch.tensor(ar, **f64)
+    tabs = [torch.zeros((nr, npl), **f64) for _ in range(3)]
+    ctx.computePhil(d_ar, torch.tensor(rhl, **f64), *tabs)
+    torch.cuda.synchronize()
+    E, D, _ = F.tabulate_delta(ar, *[t.cpu().numpy() for t in tabs])
+    delta = ctx.delta(torch.tensor(E, **f64), torch.tensor(D, **f64))
+    x, w = velocity_rule()
+    rule = F.Rule(x, w, jquad=0 if args.form == "plain" else 16)
+    df = F.DFParams(CFG["model"], CFG["dphi_h"], CFG["dz_h"], CFG["dphi_g"], CFG["dz_g"], CFG["chi"], CFG["mass"],
+                    CFG["r0"], k=CFG["k"])
+    ci, _ = F.gauleg(0, 1, ng)
+    allp = np.array([[ar[n] * np.sqrt(1 - c * c), ar[n] * c] for n in range(nr) for c in ci])
+    pts = torch.tensor(allp[np.linspace(0, nr * ng - 1, args.profile_points).astype(int)], **f64)
+    out = torch.zeros((6, pts.shape[0]), **f64)
+    st = ctx.moments_points(ctx.potential(d_ar, *tabs), delta, df, rule, pts, out)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_points": pts.shape[0], "nodes": st.nodes, "bound": st.bound,
+                      "kernel_ms": st.kernel_ms, "failures": st.failures}))
+
+
+def main():
+    args = parse()
+    if args.profile_points:
+        profile_case(args)
+        return
+    rank, world = dist_init()
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        res = []
+        for _ in range(args.warmup):
+            cpu_sample(args, sample=min(args.cpu_sample, 4))
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            res.append(cpu_sample(args, sample=args.cpu_sample))
+        wall = time.perf_counter() - t0
+        v = float(np.mean([r["value"] for r in res]))
+        cb = dict(res[-1], value=v)
+        print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+                          "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                          "data": "synthetic", "config": {"workload": "NFW rotating 80x40, l<=12, 22^3 tanh-sinh",
+                                                          "form": args.form},
+                          "cpu_baseline": cb,
+                          "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    out, _ = run_ours(args, rank, world)
+    if rank == 0:
+        if not args.no_e2e:
+            out["e2e"] = e2e_ours(args)
+        if not args.no_cpu and world == 1:
+            out["cpu_baseline"] = cpu_sample(args, sample=args.cpu_sample)
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

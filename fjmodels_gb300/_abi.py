@@ -73,6 +73,7 @@ SIGNATURES = {
     "fj_actions": ([CTX, P(fj_potential), P(fj_delta_table), C.c_void_p, C.c_size_t, C.c_int, C.c_void_p], C.c_int),
     "fj_potential_eval": ([CTX, P(fj_potential), C.c_void_p, C.c_size_t, C.c_void_p], C.c_int),
     "fj_vir2": ([CTX, P(fj_potential), C.c_int, C.c_void_p, DP], C.c_int),
+    "fj_measure_fma_peak": ([C.c_int, DP], C.c_int),
     "fj_log_grid": ([C.c_double, C.c_double, C.c_int, DP], C.c_int),
     "fj_gauleg": ([C.c_double, C.c_double, C.c_int, DP, DP], C.c_int),
     "fj_guess_rhl": ([C.c_int, C.c_int, C.c_int, DP, C.c_int, C.c_double, C.c_double, C.c_double, DP], C.c_int),

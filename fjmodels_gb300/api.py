@@ -52,20 +52,25 @@ def _ptr(t):
     return t.data_ptr()
 
 
-def tanh_sinh_rule(n=22, h=None):
-    """Symmetric n-point tanh-sinh rule on [-1,1] (Takahasi & Mori 1974):
-    x_k = tanh(pi/2 sinh(k h)), w_k = h pi/2 cosh(k h) / cosh^2(pi/2 sinh(k h)),
-    with k = -(n-1)/2 .. (n-1)/2 in steps of 1 and h chosen so the outermost
-    node sits at 1 - 1e-5.  Weights are renormalised to sum to 2."""
-    ks = np.arange(n) - (n - 1) / 2.0
-    if h is None:
-        kmax = ks[-1]
-        t = np.arctanh(1 - 1e-5) * 2 / np.pi
-        h = np.arcsinh(t) / kmax
+def tanh_sinh_rule(n=22, eps=1e-5):
+    """n-point composite tanh-sinh (double-exponential) rule on [-1,1]
+    (Takahasi & Mori 1974): n/2 nodes of the rule on [0,1],
+    x_k = (1 + tanh(pi/2 sinh(k h)))/2, w_k = h pi/4 cosh(k h) / cosh^2(pi/2 sinh(k h)),
+    k = -(m-1)/2 .. (m-1)/2, mirrored onto [-1,0].  Nodes cluster at v = 0 and at
+    |v| = 1 like the reference's [0,1] tanh-sinh table (include/GaussPts.h:91-134);
+    h puts the outermost node at distance eps from the ends.  Each half's weights
+    are normalised to 1."""
+    if n % 2:
+        raise ValueError("n must be even")
+    m = n // 2
+    ks = np.arange(m) - (m - 1) / 2.0
+    kmax = ks[-1]
+    h = np.arcsinh(np.arctanh(1 - 2 * eps) * 2 / np.pi) / kmax
     u = np.pi / 2 * np.sinh(ks * h)
-    x = np.tanh(u)
-    w = h * np.pi / 2 * np.cosh(ks * h) / np.cosh(u) ** 2
-    return x, w * (2.0 / w.sum())
+    x = 0.5 * (1 + np.tanh(u))
+    w = h * np.pi / 4 * np.cosh(ks * h) / np.cosh(u) ** 2
+    w = w / w.sum()
+    return np.concatenate([-x[::-1], x]), np.concatenate([w[::-1], w])
 
 
 class DFParams:

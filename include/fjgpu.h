@@ -173,6 +173,11 @@ int fj_potential_eval(fj_ctx *ctx, const fj_potential *pot, const double *Rz, si
    the last radius, mass from the density sum.  Synchronises. */
 int fj_vir2(fj_ctx *ctx, const fj_potential *pot, int ngauss, const double *coef6, double *out7);
 
+/* FMA throughput of the current device in TFLOP/s (fp32 = 0: FP64, 1: FP32),
+   from a kernel of independent FMA chains; the roofline denominator of the
+   phase-space kernel.  No counterpart in the reference (a measurement aid). */
+int fj_measure_fma_peak(int fp32, double *tflops);
+
 /* ------------------------------------------- host-side setup (run once) */
 
 /* Logarithmic radial grid (include/Utils.h:76-81 with an explicit rmin). */
