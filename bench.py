@@ -37,7 +37,7 @@ UNIT = "s/model"
 # FP64 operations per phase-space evaluation executed by active threads of the
 # phase-space kernel (dadd + dmul + 2*dfma from ncu on the nfw_80x40 workload,
 # profiles/moments_fp64_nfw_80x40.md); the algorithmic work unit of the roofline.
-FP64_FLOPS_PER_EVAL = {"plain": None, "gl": None}
+FP64_FLOPS_PER_EVAL = {"plain": 1.23e5, "gl": None}
 
 
 def parse():
