@@ -67,6 +67,7 @@ SIGNATURES = {
                            C.c_void_p, C.c_int, C.c_void_p, P(fj_moment_stats)], C.c_int),
     "fj_legendre_project": ([CTX, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "fj_poisson": ([CTX, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "fj_poisson_noalloc": ([C.c_int, C.c_int] + [C.c_void_p] * 6, C.c_int),
     "fj_sum_potentials": ([CTX, C.c_int] + [C.c_void_p] * 9, C.c_int),
     "fj_compute_new_phi": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule), C.c_int,
                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, P(fj_moment_stats)], C.c_int),

@@ -21,7 +21,7 @@ LIB = os.path.join(HERE, "libfjgpu.so")
 # they take the other branch at a few nodes and densities move by ~1e-7,
 # exactly as the reference's own sources do when compiled with contraction.
 SOURCES = {"fj_moments.cu": ["--fmad=false"], "fj_multipole.cu": ["--fmad=false"], "fj_api.cu": [],
-           "fj_peak.cu": []}
+           "fj_peak.cu": [], "fj_noalloc.cu": []}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xcompiler", "-Wall,-Wno-unused-function,-ffp-contract=off"]

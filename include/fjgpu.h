@@ -142,6 +142,23 @@ int fj_legendre_project(fj_ctx *ctx, int nr, int ngauss, int npoly, const double
 int fj_poisson(fj_ctx *ctx, int nr, int npoly, const double *ar, const double *rhl,
                double *phil, double *Pr, double *Pr2);
 
+/* Poisson solve that allocates nothing.  It has no counterpart in the
+   reference: it is fj_poisson for callers that cannot allocate device memory
+   on their call path (an application whose device memory belongs to its own
+   pool allocator, a latency-bound loop).  The quadrature workspace is a
+   file-scope device array of the library, sized for nr*npoly <=
+   FJ_POISSON_NOALLOC_MAX_COEFS (9 MiB, held on every device that loads the
+   library until exit); larger requests return FJ_ERR_ARG.  No context:
+   inputs and outputs are device pointers on the current device, work is
+   queued on `stream` (a cudaStream_t; NULL = legacy default stream).  The
+   first call on a device looks up the array's address on that device, so
+   make that first call before any stream capture.  All calls share the
+   array: calls whose work overlaps on the GPU race and must be serialised by
+   the caller. */
+#define FJ_POISSON_NOALLOC_MAX_COEFS 1024
+int fj_poisson_noalloc(int nr, int npoly, const double *ar, const double *rhl, double *phil,
+                       double *Pr, double *Pr2, void *stream);
+
 /* updatePhil (pot/potLeg.cpp:21-29): out = a + b element-wise on the three
    tables (device [nr*npoly] each). */
 int fj_sum_potentials(fj_ctx *ctx, int n, const double *phil_a, const double *Pr_a,
