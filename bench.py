@@ -14,7 +14,13 @@ A step is one self-consistency iteration over the whole meridional grid
 the device as the reference's loop chains them.  value = wall-seconds per
 converged model = seconds per step x 20 (whole job: / N for N replicas).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--form plain|gl]
+The chosen form is the mixed-precision one (FP32 turning points, momentum
+integrals and DF; FP64 node setup, turning points at the u/v limits and
+accumulation).  Its density error is measured in the same run: one iteration
+from the same input potential in the mixed and the plain FP64 form, max
+relative rho difference over all grid points, and the plain form's time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed|plain|gl]
   python bench.py --impl reference ...   (the CPU path on this host's cores)
 """
 import argparse
@@ -38,6 +44,9 @@ UNIT = "s/model"
 # phase-space kernel (dadd + dmul + 2*dfma from ncu on the nfw_80x40 workload,
 # profiles/moments_fp64_nfw_80x40.md); the algorithmic work unit of the roofline.
 FP64_FLOPS_PER_EVAL = {"plain": 1.23e5, "gl": None}
+# FP32 operations (fadd + fmul + 2*ffma) per phase-space evaluation of the mixed
+# form, from ncu on the same workload (profiles/moments_mixed_nfw_80x40.md)
+FP32_FLOPS_PER_EVAL = {"mixed": None}
 
 
 def parse():
@@ -46,7 +55,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="plain", choices=["plain", "gl"])
+    ap.add_argument("--form", default="mixed", choices=["mixed", "plain", "gl"])
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison step")
     ap.add_argument("--cpu-sample", type=int, default=os.cpu_count(), help="grid points timed for the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -125,6 +135,19 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def make_rule(F, form, x, w):
+    from fjmodels_gb300 import _abi as A
+    if form == "gl":
+        return F.Rule(x, w, jquad=16)
+    return F.Rule(x, w, precision=A.FJ_PREC_MIXED if form == "mixed" else A.FJ_PREC_FP64)
+
+
+FORM_TEXT = {"mixed": "mixed precision (FP32 turning points, QAGS momentum integrals and DF; FP64 setup, "
+                      "limit turning points and accumulation)",
+             "plain": "plain FP64, QAGS momentum integrals",
+             "gl": "FP64, 16-point Gauss-Legendre momentum integrals"}
+
+
 def velocity_rule():
     import fjmodels_gb300 as F
     return F.tanh_sinh_rule(CFG["nq"])
@@ -155,7 +178,7 @@ def run_ours(args, rank, world):
     E, D, _ = F.tabulate_delta(ar, *[t.cpu().numpy() for t in tabs])
     delta = ctx.delta(torch.tensor(E, **f64), torch.tensor(D, **f64))
     x, w = velocity_rule()
-    rule = F.Rule(x, w, jquad=0 if args.form == "plain" else 16)
+    rule = make_rule(F, args.form, x, w)
     df = F.DFParams(CFG["model"], CFG["dphi_h"], CFG["dz_h"], CFG["dphi_g"], CFG["dz_g"], CFG["chi"], CFG["mass"],
                     CFG["r0"], k=CFG["k"])
     grids = torch.zeros((6, nr, ng), **f64)
@@ -194,27 +217,34 @@ def run_ours(args, rank, world):
     value = ms_per_step / 1e3 * CFG["iters_per_model"] / world
     nodes = last.nodes
     k_ms = float(np.mean(kernel_ms))
+    fp32 = args.form == "mixed"
     peak = np.zeros(1)
-    F.load_library().fj_measure_fma_peak(0, peak.ctypes.data_as(F._abi.DP))
-    flops = FP64_FLOPS_PER_EVAL.get(args.form)
+    F.load_library().fj_measure_fma_peak(1 if fp32 else 0, peak.ctypes.data_as(F._abi.DP))
+    flops = FP32_FLOPS_PER_EVAL.get(args.form) if fp32 else FP64_FLOPS_PER_EVAL.get(args.form)
     achieved = flops * nodes / (k_ms * 1e-3) / 1e12 if flops else None
+    vs_plain = None
+    if args.form != "plain" and not args.no_plain:
+        vs_plain = compare_plain(F, ctx, d_ar, state["cur"], delta, df, x, w, ng, grids, f64)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (analytic NFW guess density, seeded by construction)",
+        "vs_baseline": None, "dtype": "f32+f64" if fp32 else "f64",
+        "data": "synthetic (analytic NFW guess density, seeded by construction)",
         "config": {"workload": f"NFW rotating (chi=1,k=0.5) {nr}x{ng} grid, l<=12, 22^3 tanh-sinh nodes, "
                                f"{CFG['iters_per_model']} iterations/model",
-                   "form": "plain FP64, QAGS momentum integrals" if args.form == "plain" else
-                   "FP64, 16-point Gauss-Legendre momentum integrals",
+                   "form": FORM_TEXT[args.form],
                    "phase_space_evals_per_step": nodes, "bound_evals_per_step": last.bound,
                    "l2": "256 MiB buffer written between steps", "parallelism": f"replicas{world}"},
         "phase_space_evals_per_s": nodes / (ms_per_step * 1e-3) * world,
         "kernel_ms_per_step": k_ms,
         "potential_change_last": float(changes[-1].item()) if changes else None,
         "gpu_launches": 4 * args.steps,
-        "roofline": {"bound": "fp64", "kernel": "k_moments", "achieved": achieved, "peak": float(peak[0]),
+        "escalated_evals_per_step": last.escalated, "failed_evals_per_step": last.failures,
+        "vs_plain_fp64": vs_plain,
+        "roofline": {"bound": "fp32" if fp32 else "fp64", "kernel": "k_moments_mixed" if fp32 else "k_moments",
+                     "achieved": achieved, "peak": float(peak[0]),
                      "unit": "TFLOP/s", "frac": (achieved / peak[0]) if achieved else None,
-                     "peak_source": "fj_measure_fma_peak (FP64 FMA chains, this GPU)",
+                     "peak_source": f"fj_measure_fma_peak ({'FP32' if fp32 else 'FP64'} FMA chains, this GPU)",
                      "flops_per_eval": flops, "traffic": None},
         "clocks": clk.summary(),
     }
@@ -222,33 +252,61 @@ def run_ours(args, rank, world):
     return out, (ar, tabs, delta, rule, df)
 
 
+def compare_plain(F, ctx, d_ar, cur, delta, df, x, w, ng, grids, f64):
+    """One iteration from the same potential in the plain FP64 form: its time per model and
+    the chosen form's density error against it (max over all grid points of |rho - rho64| /
+    rho64; dispersions likewise)."""
+    import torch
+    pot = ctx.potential(d_ar, *cur)
+    nr, npl = cur[0].shape
+    coef = torch.zeros((6, nr, npl), **f64)
+    outs = [torch.zeros((nr, npl), **f64) for _ in range(3)]
+    g64 = torch.zeros_like(grids)
+    ctx.computeNewPhi(pot, delta, df, make_rule(F, "mixed", x, w), ng, grids, coef, *outs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st = ctx.computeNewPhi(pot, delta, df, make_rule(F, "plain", x, w), ng, g64, coef, *outs)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    a, b = grids.cpu().numpy().reshape(6, -1), g64.cpu().numpy().reshape(6, -1)
+    ok = b[0] > 0
+    err = lambda q: float(np.max(np.abs(a[q][ok] - b[q][ok]) / np.abs(b[q][ok])))
+    sig_ok = ok & np.isfinite(b[2]) & np.isfinite(b[3]) & np.isfinite(b[4])
+    sig = max(float(np.max(np.abs(a[q][sig_ok] - b[q][sig_ok]) / np.abs(b[q][sig_ok]))) for q in (2, 3, 4))
+    return {"plain_value": t64 * CFG["iters_per_model"], "unit": UNIT, "plain_kernel_ms": st.kernel_ms,
+            "rho_max_rel_err": err(0), "sigma_max_rel_err": sig,
+            "note": "one iteration from the same input potential in both forms, all grid points"}
+
+
 def e2e_ours(args):
     """Same metric through the host-buffer C-ABI call (fj_run_model): host inputs, device
-    compute, host outputs, copies inside the timed region.  Two runs (1 and 2 iterations)
-    split the one-time setup from the per-iteration cost."""
+    compute, host outputs, copies inside the timed region.  One run of K iterations: the
+    one-time setup (grid, guess density, Poisson, focal-distance table) once plus 20 times
+    the measured per-iteration wall time (which includes each iteration's copy of the new
+    multipoles back to the host for the convergence test)."""
     import torch
 
     import fjmodels_gb300 as F
     ctx = F.Context(int(os.environ.get("LOCAL_RANK", "0")))
     x, w = velocity_rule()
-    rule = F.Rule(x, w, jquad=0 if args.form == "plain" else 16)
+    rule = make_rule(F, args.form, x, w)
     df = F.DFParams(CFG["model"], CFG["dphi_h"], CFG["dz_h"], CFG["dphi_g"], CFG["dz_g"], CFG["chi"], CFG["mass"],
                     CFG["r0"], k=CFG["k"])
-    walls = {}
-    for its in (1, 2):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ctx.run_model(CFG["nr"], CFG["ngauss"], CFG["npoly"], CFG["rmin"], CFG["rmax"], df, rule, itermax=its)
-        walls[its] = time.perf_counter() - t0
+    its = max(1, args.steps)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = ctx.run_model(CFG["nr"], CFG["ngauss"], CFG["npoly"], CFG["rmin"], CFG["rmax"], df, rule, itermax=its)
+    wall = time.perf_counter() - t0
     ctx.close()
-    per_iter = walls[2] - walls[1]
-    setup = walls[1] - per_iter
+    setup = r["setup_ms"] * 1e-3
+    per_iter = (wall - setup) / its
     nr, ng, npl, ngrid = CFG["nr"], CFG["ngauss"], CFG["npoly"], 30
     h2d = 8 * (nr + nr * npl + 2 * ngrid + 2 * CFG["nq"])
     d2h_step = 8 * nr * npl
     return {"value": setup + CFG["iters_per_model"] * per_iter, "unit": UNIT, "setup_s": setup,
-            "s_per_iteration": per_iter, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h_step,
-            "note": "fj_run_model with host buffers; setup (guess, Poisson, focal-distance table) counted once"}
+            "s_per_iteration": per_iter, "iterations_run": its, "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h_step,
+            "note": "fj_run_model with host buffers: setup once + 20 x measured wall per iteration"}
 
 
 def cpu_sample(args, sample=16):
@@ -266,7 +324,7 @@ def cpu_sample(args, sample=16):
     x, w = velocity_rule()
     m = O.Model(ar, phil, Pr, Pr2, np.zeros(30), np.zeros(30), ng, alpha=1.667, beta=3.0, mass=CFG["mass"],
                 r0=CFG["r0"], dphi_h=CFG["dphi_h"], dz_h=CFG["dz_h"], dphi_g=CFG["dphi_g"], dz_g=CFG["dz_g"],
-                chi=CFG["chi"], k=CFG["k"], xq=x, wq=w, jquad=0 if args.form == "plain" else 16)
+                chi=CFG["chi"], k=CFG["k"], xq=x, wq=w, jquad=16 if args.form == "gl" else 0)
     E, D, _ = m.tabulate_delta(30)
     m.Egrid, m.Dgrid = E, D
     npts = nr * ng
@@ -307,7 +365,7 @@ def profile_case(args):
     E, D, _ = F.tabulate_delta(ar, *[t.cpu().numpy() for t in tabs])
     delta = ctx.delta(torch.tensor(E, **f64), torch.tensor(D, **f64))
     x, w = velocity_rule()
-    rule = F.Rule(x, w, jquad=0 if args.form == "plain" else 16)
+    rule = make_rule(F, args.form, x, w)
     df = F.DFParams(CFG["model"], CFG["dphi_h"], CFG["dz_h"], CFG["dphi_g"], CFG["dz_g"], CFG["chi"], CFG["mass"],
                     CFG["r0"], k=CFG["k"])
     ci, _ = F.gauleg(0, 1, ng)

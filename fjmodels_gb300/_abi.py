@@ -34,7 +34,7 @@ class fj_quad_rule(C.Structure):
 
 class fj_moment_stats(C.Structure):
     _fields_ = [("nodes", C.c_longlong), ("bound", C.c_longlong), ("failures", C.c_longlong),
-                ("kernel_ms", C.c_double)]
+                ("kernel_ms", C.c_double), ("escalated", C.c_longlong)]
 
 
 class fj_model_config(C.Structure):
@@ -48,7 +48,8 @@ class fj_model_config(C.Structure):
 class fj_model_result(C.Structure):
     _fields_ = [(n, DP) for n in ("ar", "coef6", "phil", "Pr", "Pr2", "Egrid", "Dgrid", "grids6")] + [
         ("vir7", C.c_double * 7), ("iterations", C.c_int), ("last_change", C.c_double),
-        ("bound", C.c_longlong), ("failures", C.c_longlong), ("wall_ms", C.c_double), ("kernel_ms", C.c_double)]
+        ("bound", C.c_longlong), ("failures", C.c_longlong), ("wall_ms", C.c_double), ("kernel_ms", C.c_double),
+        ("setup_ms", C.c_double)]
 
 
 P = C.POINTER

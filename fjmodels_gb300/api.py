@@ -229,7 +229,8 @@ class Context:
                                 _dp(grids) if keep_grids else None)
         self._check(self.lib.fj_run_model(self.h, C.byref(cfg), C.byref(res)), "fj_run_model")
         out.update(vir7=np.array(res.vir7[:]), iterations=res.iterations, last_change=res.last_change,
-                   bound=res.bound, failures=res.failures, wall_ms=res.wall_ms, kernel_ms=res.kernel_ms)
+                   bound=res.bound, failures=res.failures, wall_ms=res.wall_ms, kernel_ms=res.kernel_ms,
+                   setup_ms=res.setup_ms)
         if keep_grids:
             out["grids6"] = grids
         return out

@@ -207,7 +207,11 @@ int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delt
     if (!delta || delta->ngrid < 2 || !delta->Egrid || !delta->Dgrid) return fail(ctx, FJ_ERR_ARG, "delta table");
     if (!df || !rule || rule->nq < 1 || rule->nq > 64 || rule->jquad < 0 || rule->jquad > 64 || !out6 || npts < 1)
         return fail(ctx, FJ_ERR_ARG, "moments: bad rule, df or sizes");
-    if (rule->precision != FJ_PREC_FP64) return fail(ctx, FJ_ERR_ARG, "moments: precision mode not available");
+    if (rule->precision != FJ_PREC_FP64 && rule->precision != FJ_PREC_MIXED)
+        return fail(ctx, FJ_ERR_ARG, "moments: unknown precision mode");
+    const bool mixed = rule->precision == FJ_PREC_MIXED;
+    if (mixed && (df->kind != FJ_DF_DPL || rule->jquad != FJ_JQUAD_QAGS))
+        return fail(ctx, FJ_ERR_ARG, "moments: the mixed form takes the double-power-law DF and QAGS momentum integrals");
     MomentArgs a;
     a.P = view(pot);
     a.Eg = delta->Egrid; a.Dg = delta->Dgrid; a.ngrid = delta->ngrid;
@@ -230,7 +234,7 @@ int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delt
     a.out6 = out6;
     FJ_CUDA(cudaMemsetAsync(a.counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    FJ_CUDA(launch_moments(a, ctx->stream));
+    FJ_CUDA(mixed ? launch_moments_mixed(a, ctx->stream) : launch_moments(a, ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     if (stats) {
         unsigned long long h[4];
@@ -242,6 +246,7 @@ int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delt
         stats->bound = (long long)h[0];
         stats->failures = (long long)h[1];
         stats->kernel_ms = ms;
+        stats->escalated = (long long)h[3];
     }
     return FJ_OK;
 }
@@ -270,8 +275,9 @@ int fj_ctx_create(int device, fj_ctx **out)
     // call stack (about 5.5 KB, ptxas "cumulative stack size"); the function
     // attributes do not report call-stack frames, so the floor is explicit.
     size_t need = moments_local_bytes();
-    const size_t need2 = multipole_local_bytes();
+    const size_t need2 = multipole_local_bytes(), need3 = moments_mixed_local_bytes();
     if (need2 > need) need = need2;
+    if (need3 > need) need = need3;
     need = (need + 1024 + 1023) / 1024 * 1024;
     if (need < kStackBytes) need = kStackBytes;
     size_t cur = 0;
@@ -796,6 +802,8 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
     res->bound = res->failures = 0;
     res->kernel_ms = 0;
     res->last_change = -1;
+    FJ_CUDA(cudaStreamSynchronize(s));
+    res->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     int k = 0;
     for (k = 0; k < cfg->itermax; k++) {
         fj_potential pot{nr, npl, d_ar, cur, cur + nt, cur + 2 * nt};

@@ -29,12 +29,18 @@ struct MomentArgs {
     int npts;
     int blocks_per_point;
     double *partial;         // [npts][blocks_per_point][6]
-    unsigned long long *counters;  // [0] bound nodes, [1] failed nodes
+    unsigned long long *counters;  // [0] bound nodes, [1] failed nodes, [3] FP64 escalations
     double *out6;            // [6][npts]
 };
 
 size_t moment_smem_bytes(const MomentArgs &a);
 cudaError_t launch_moments(const MomentArgs &a, cudaStream_t s);
+// the per-point sums of the block partials (shared by both forms)
+cudaError_t launch_moments_finalize(const MomentArgs &a, cudaStream_t s);
+// mixed-precision form (FJ_PREC_MIXED, double-power-law DF, QAGS momentum
+// integrals); counters[3] gets the nodes whose turning points ran in FP64
+size_t moment_mixed_smem_bytes(const MomentArgs &a);
+cudaError_t launch_moments_mixed(const MomentArgs &a, cudaStream_t s);
 
 cudaError_t launch_actions(PotView P, const double *Eg, const double *Dg, int ngrid, GLRule gl,
                            const double *pts, size_t n, double *out, cudaStream_t s);
@@ -56,6 +62,7 @@ cudaError_t launch_vir2(PotView P, int ngauss, const double *ci, const double *w
 
 // largest per-thread local memory (stack) any kernel of the library needs
 size_t moments_local_bytes();
+size_t moments_mixed_local_bytes();
 size_t multipole_local_bytes();
 
 }  // namespace fj

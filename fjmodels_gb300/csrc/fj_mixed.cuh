@@ -1,0 +1,927 @@
+// fj_mixed.cuh -- mixed-precision phase-space evaluation.
+//
+// The same algorithm as the plain form (fj_device.cuh: the reference's
+// bracketing, Brent roots, QAGS momentum integrals with its tolerances, the
+// double-power-law DF) with the bulk arithmetic in FP32:
+//   FP64  per-point setup (Phi, escape speed), the node's velocity, energy
+//         and focal distance, the prolate-spheroidal transform, the moment
+//         accumulation, and the turning-point search whenever it reaches the
+//         u/v limits (the bracket refinement below FP32 resolution, v within
+//         1e-6 of the equatorial or polar limit), which reruns in FP64;
+//   FP32  potential and gradient evaluations from FP32 copies of the tables,
+//         the u/v turning-point functions, the bracket search and Brent
+//         iterations away from the limits, QAGS (GK21) and the DF.
+// The reference point u0 of the u-equation is the orbit's own u instead of
+// the root of d/du (uvOrb.cpp:109-129): the u-equation does not depend on u0
+// (it cancels exactly), and u0 = 58 overflows FP32 (sinh(58)^2 > FLT_MAX).
+// With u0 = u, Er*cosh^2(u0) reduces to pu^2/(2 Delta^2) exactly.
+#pragma once
+
+#include "fj_device.cuh"
+
+namespace fj {
+
+constexpr float kPIHf = 1.570796326794897f;
+constexpr float kPIf = 3.141592653589793f;
+
+// FP32 view of the multipole potential.  The monopole column of phil holds
+// Phi_0(r) - shift (shift = the potential at the phase point of the block):
+// the u and v equations only involve E - Phi, and near the point the
+// shifted values are small, so their FP32 rounding is relative to the local
+// potential differences rather than to |Phi|.  out0 = the unshifted outer
+// monopole phil[nr-1][0] for the r >= ar[nr-1] extrapolation.
+// The interpolation of pot/Potential.cpp:206-276 (linear, plus the quadratic
+// correction in the ten innermost intervals) uses per-interval constants:
+// ih[n] = 1/(ar[n+1]-ar[n]) and, for n < kQuadIntervals, qc[4n..4n+3] =
+// {q, f3} with the third point below (n-1) and above (n+2), where
+// q = 1/((ar[thr]-ar[n+1])(ar[thr]-ar[n])), f3 = (ar[thr]-ar[n])/(ar[n+1]-ar[n]).
+// The interval of r is found from the logarithmic spacing of the grid
+// (lr0 = log ar[0], idl = (nr-1)/log(ar[nr-1]/ar[0])) and corrected by
+// neighbour tests, so any increasing grid gives the bracketing interval.
+constexpr int kQuadIntervals = 9;  // intervals whose top node is below 10
+struct PotViewF {
+    int nr, npoly;
+    const float *ar, *phil, *Pr, *ih, *qc;
+    float out0, shift, lr0, idl;
+};
+
+// even-Legendre recurrence P_2k from P_2k-2, P_2k-4 (include/UtilsLeg.h:43-50)
+// as P_2k = (P_2k-2 (c^2 - B_k) - A_k P_2k-4) C_k, constants per k
+struct LegCoefF { float A[kMaxPoly], B[kMaxPoly], C[kMaxPoly], inv[2 * kMaxPoly + 1]; };
+constexpr LegCoefF make_leg_f()
+{
+    LegCoefF o{};
+    for (int k = 0; k < kMaxPoly; k++) {
+        const double l = 2.0 * (k - 1), l2 = 2 * l;
+        o.A[k] = k >= 2 ? (float)(l * (l - 1) / ((l2 + 1) * (l2 - 1))) : 0.f;
+        o.B[k] = k >= 2 ? (float)((l2 * l + l2 - 1) / ((l2 - 1) * (l2 + 3))) : 0.f;
+        o.C[k] = k >= 2 ? (float)((l2 + 1) * (l2 + 3) / ((l + 1) * (l + 2))) : 0.f;
+    }
+    for (int i = 0; i <= 2 * kMaxPoly; i++) o.inv[i] = i ? (float)(1.0 / i) : 0.f;
+    return o;
+}
+static __constant__ LegCoefF kLegF_d = make_leg_f();
+static constexpr LegCoefF kLegF_h = make_leg_f();
+FJ_HD const LegCoefF &leg_f()
+{
+#ifdef __CUDA_ARCH__
+    return kLegF_d;
+#else
+    return kLegF_h;
+#endif
+}
+
+struct InterpF {
+    int bot, thr;
+    bool ext, quad;
+    float f1, f2, f3, q, x;
+};
+
+FJ_HD void interp_setup_f(const PotViewF &P, float r, InterpF &I)
+{
+    const float *ar = P.ar;
+    const int nr = P.nr;
+    I.bot = I.thr = 0;
+    I.f1 = I.f2 = I.f3 = I.q = 0.f;
+    I.quad = false;
+    I.x = 0.f;
+    if (r >= ar[nr - 1]) { I.ext = true; I.x = ar[nr - 1] / r; return; }
+    I.ext = false;
+    int b = (int)((logf(r) - P.lr0) * P.idl);
+    b = b < 0 ? 0 : (b > nr - 2 ? nr - 2 : b);
+    while (b > 0 && r < ar[b]) --b;
+    while (b < nr - 2 && r > ar[b + 1]) ++b;
+    I.bot = b;
+    I.f1 = (r - ar[b]) * P.ih[b];
+    I.quad = b < kQuadIntervals;
+    if (I.quad) {
+        const bool lo = I.f1 < 0.5f && b > 0;
+        I.thr = lo ? b - 1 : b + 2;
+        const float *q = P.qc + 4 * b + (lo ? 0 : 2);
+        I.q = q[0];
+        I.f2 = (r - ar[b + 1]) * (r - ar[b]) * q[0];
+        I.f3 = q[1];
+    }
+}
+
+FJ_HD float interp_in_f(const InterpF &I, const float *T, int npoly, int k)
+{
+    const float vb = T[I.bot * npoly + k], d = T[(I.bot + 1) * npoly + k] - vb;
+    float v = vb + I.f1 * d;
+    if (I.quad) v += I.f2 * (T[I.thr * npoly + k] - vb - I.f3 * d);
+    return v;
+}
+
+FJ_HDNI float pot_phi_f(const PotViewF &P, float R, float z)
+{
+    const float r = sqrtf(R * R + z * z);
+    const float c = z / r;
+    InterpF I;
+    interp_setup_f(P, (r >= P.ar[P.nr - 1]) ? r : fmaxf(r, P.ar[0]), I);
+    const int np_ = P.npoly;
+    const float *T = P.phil;
+    const LegCoefF &L = leg_f();
+    const float x2 = I.x * I.x;
+    float xp = I.x;
+    float phi = I.ext ? P.out0 * xp - P.shift : interp_in_f(I, T, np_, 0);
+    if (np_ < 2) return phi;
+    const float c2 = c * c;
+    float pm2 = 1.f, pm1 = 1.5f * c2 - .5f;
+    xp *= x2;
+    phi += (I.ext ? T[(P.nr - 1) * np_ + 1] * xp : interp_in_f(I, T, np_, 1)) * pm1;
+    for (int k = 2; k < np_; k++) {
+        const float pk = (pm1 * (c2 - L.B[k]) - L.A[k] * pm2) * L.C[k];
+        xp *= x2;
+        phi += (I.ext ? T[(P.nr - 1) * np_ + k] * xp : interp_in_f(I, T, np_, k)) * pk;
+        pm2 = pm1; pm1 = pk;
+    }
+    return phi;
+}
+
+// Phi, dPhi/dR, dPhi/dz (pot/Potential.cpp:206-276) in FP32
+FJ_HDNI void pot_grad_f(const PotViewF &P, float R, float z, float &phi, float &dR, float &dz)
+{
+    const float *ar = P.ar;
+    const int np_ = P.npoly, nr = P.nr;
+    const LegCoefF &L = leg_f();
+    const float r0 = sqrtf(R * R + z * z);
+    const float cphi = z / r0;
+    float r = r0 < ar[0] ? ar[0] : r0;
+    const float s = R / r;
+    float c = z / r;
+    if (c >= 1.f) c = 1.f - 1e-7f;
+    InterpF I;
+    interp_setup_f(P, r, I);
+    const float x2 = I.x * I.x;
+    float xp = I.x;
+    const float cp2 = cphi * cphi, cc2 = c * c, i1mc2 = 1.f / (1.f - cc2);
+    float ep2 = 1, ep1 = 0, ec2 = 1, ec1 = 0, Pl_m1 = 0, Pl = 1;
+    int nfull = 0;
+    float gphi = 0, gdr = 0, gdth = 0;
+    for (int k = 0; k < np_; k++) {
+        float ph, dph;
+        if (I.ext) {
+            const float t = k == 0 ? P.out0 : P.phil[(nr - 1) * np_ + k];
+            ph = k == 0 ? t * xp - P.shift : t * xp;
+            dph = -(float)(2 * k + 1) * t * xp / r;
+            xp *= x2;
+        } else {
+            ph = interp_in_f(I, P.phil, np_, k);
+            dph = interp_in_f(I, P.Pr, np_, k);
+        }
+        float pe_phi, pe_c;
+        if (k == 0) { pe_phi = 1; pe_c = 1; }
+        else if (k == 1) { pe_phi = 1.5f * cp2 - .5f; pe_c = 1.5f * cc2 - .5f; ep1 = pe_phi; ec1 = pe_c; }
+        else {
+            pe_phi = (ep1 * (cp2 - L.B[k]) - L.A[k] * ep2) * L.C[k]; ep2 = ep1; ep1 = pe_phi;
+            pe_c = (ec1 * (cc2 - L.B[k]) - L.A[k] * ec2) * L.C[k]; ec2 = ec1; ec1 = pe_c;
+        }
+        float dleg = 0;
+        if (k > 0) {
+            const int n = 2 * k;
+            while (nfull < n) {
+                const int i = nfull + 1;
+                const float Pn = (i == 1) ? c : ((float)(2 * i - 1) * c * Pl - (float)(i - 1) * Pl_m1) * L.inv[i];
+                Pl_m1 = Pl; Pl = Pn; nfull = i;
+            }
+            dleg = (float)n * (Pl_m1 - c * Pl) * i1mc2;
+        }
+        if (k == 0) gphi = ph; else gphi += ph * pe_phi;
+        gdr += dph * pe_c;
+        gdth += ph * dleg;
+    }
+    gdth *= -sqrtf(1.f - c * c);
+    phi = gphi;
+    dR = gdth * (c / r) + gdr * s;
+    dz = gdth * (-s / r) + gdr * c;
+}
+
+// Phi(R, z) - Phi(point) for a position on a coordinate line through the
+// phase point, with the differences of the geometry given exactly:
+// dr2 = r^2 - rpt^2 and dc2 = c^2 - c2pt (c = z/r).  When r and the point share
+// an interpolation interval (the point may sit on its end node) the
+// difference is formed inside the interpolation formula and by the difference
+// recurrence of the even Legendre polynomials,
+//   d_k = C_k ((x - B_k) d_k-1 + (x - y) P_k-1(y) - A_k d_k-2),  x = c^2, y = c2pt,
+// so it keeps its relative precision however close the position is to the
+// point; otherwise it is the difference of two evaluations (Phipt = the FP32
+// potential at the point).
+FJ_HDNI float pot_dphi_f(const PotViewF &P, float R, float z, float rpt, float c2pt, float dr2, float dc2,
+                         float Phipt)
+{
+    const float r = sqrtf(R * R + z * z);
+    const float *ar = P.ar;
+    const float a0 = ar[0];
+    if (r >= ar[P.nr - 1] || rpt >= ar[P.nr - 1]) return pot_phi_f(P, R, z) - Phipt;
+    const float re = fmaxf(r, a0), rpe = fmaxf(rpt, a0);
+    InterpF I;
+    interp_setup_f(P, re, I);
+    const int b = I.bot;
+    const float ab = ar[b], at = ar[b + 1];
+    if (rpe < ab || rpe > at) return pot_phi_f(P, R, z) - Phipt;
+    const float f1p = (rpe - ab) * P.ih[b];
+    float f2p = 0.f;
+    if (I.quad) {
+        const int thr_p = (f1p < 0.5f && b > 0) ? b - 1 : b + 2;
+        if (thr_p != I.thr && rpe != ab && rpe != at) return pot_phi_f(P, R, z) - Phipt;
+        f2p = (rpe - at) * (rpe - ab) * I.q;
+    }
+    const float dr = (r >= a0 && rpt >= a0) ? dr2 / (r + rpt) : re - rpe;
+    const float df1 = dr * P.ih[b];
+    const float df2 = I.quad ? I.q * dr * (re + rpe - ab - at) : 0.f;
+    const int np_ = P.npoly;
+    const float *T = P.phil;
+    const LegCoefF &L = leg_f();
+    const float y = c2pt, x = c2pt + dc2;
+    float px1 = 1.f, px2 = 0.f, py1 = 1.f, py2 = 0.f, d1 = 0.f, d2 = 0.f, sum = 0.f;
+    for (int k = 0; k < np_; k++) {
+        const float vb = T[b * np_ + k], d = T[(b + 1) * np_ + k] - vb;
+        const float e = I.quad ? T[I.thr * np_ + k] - vb - I.f3 * d : 0.f;
+        const float ph_p = vb + f1p * d + f2p * e;  // phi_k at the point
+        const float dph = df1 * d + df2 * e;         // phi_k(r) - phi_k(point)
+        float px, py, dk;
+        if (k == 0) { px = 1.f; py = 1.f; dk = 0.f; }
+        else if (k == 1) { px = 1.5f * x - .5f; py = 1.5f * y - .5f; dk = 1.5f * dc2; }
+        else {
+            px = ((x - L.B[k]) * px1 - L.A[k] * px2) * L.C[k];
+            py = ((y - L.B[k]) * py1 - L.A[k] * py2) * L.C[k];
+            dk = ((x - L.B[k]) * d1 + dc2 * py1 - L.A[k] * d2) * L.C[k];
+        }
+        sum += dph * px + ph_p * dk;
+        px2 = px1; px1 = px; py2 = py1; py1 = py; d2 = d1; d1 = dk;
+    }
+    return sum;
+}
+
+// Brent root (wrp_GSLroots rule, include/Utils.h:134-167) in FP32; the
+// absolute bracket tolerance is raised to the FP32 resolution of the root.
+template <class F>
+FJ_HDNI unsigned brent_root_f(F &f, float lo, float hi, float &root)
+{
+    const float flo = f(lo);
+    if (fabsf(flo) < 5e-4f) { root = lo; return 0; }
+    const float fhi = f(hi);
+    if (fabsf(fhi) < 5e-4f) { root = hi; return 0; }
+    float a = lo, fa = flo, b = hi, fb = fhi, c = hi, fc = fhi, d = hi - lo, e = hi - lo;
+    float xr = 0.5f * (lo + hi), xlo = lo, xhi = hi;
+    for (int it = 0; it < kRootMaxIt; it++) {
+        bool secant = false;
+        if ((fb < 0 && fc < 0) || (fb > 0 && fc > 0)) { secant = true; c = a; fc = fa; d = b - a; e = b - a; }
+        if (fabsf(fc) < fabsf(fb)) { secant = true; a = b; b = c; c = a; fa = fb; fb = fc; fc = fa; }
+        const float tol = 0.5f * FLT_EPSILON * fabsf(b);
+        const float m = 0.5f * (c - b);
+        if (fb == 0) { xr = b; xlo = b; xhi = b; }
+        else if (fabsf(m) <= tol) { xr = b; xlo = fminf(b, c); xhi = fmaxf(b, c); }
+        else {
+            if (fabsf(e) < tol || fabsf(fa) <= fabsf(fb)) { d = m; e = m; }
+            else {
+                const float sr = fb / fa;
+                float pn, q;
+                if (secant) { pn = 2 * m * sr; q = 1 - sr; }
+                else {
+                    q = fa / fc;
+                    const float r = fb / fc;
+                    pn = sr * (2 * m * q * (q - r) - (b - a) * (r - 1));
+                    q = (q - 1) * (r - 1) * (sr - 1);
+                }
+                if (pn > 0) q = -q; else pn = -pn;
+                if (2 * pn < fminf(3 * m * q - fabsf(tol * q), fabsf(e * q))) { e = d; d = pn / q; }
+                else { d = m; e = m; }
+            }
+            a = b; fa = fb;
+            if (fabsf(d) > tol) b += d; else b += (m > 0 ? +tol : -tol);
+            fb = f(b);
+            xr = b;
+            const float cc = ((fb < 0 && fc < 0) || (fb > 0 && fc > 0)) ? a : c;
+            xlo = fminf(b, cc);
+            xhi = fmaxf(b, cc);
+        }
+        const float alo = fabsf(xlo), ahi = fabsf(xhi);
+        const float mn = ((xlo > 0 && xhi > 0) || (xlo < 0 && xhi < 0)) ? fminf(alo, ahi) : 0.f;
+        const float abstol = fmaxf(1e-8f, 4.f * FLT_EPSILON * fmaxf(alo, ahi));
+        if (fabsf(xhi - xlo) < abstol + 1e-6f * mn && !(xhi - xlo > abstol)) { root = xr; return 0; }
+    }
+    root = xr;
+    return kFailRoot;
+}
+
+// ---------------------------------------------------------------- QAGS, FP32
+FJ_HD float rescale_err_f(float err, float resabs, float resasc)
+{
+    err = fabsf(err);
+    if (resasc != 0 && err != 0) {
+        const float scale = powf(200 * err / resasc, 1.5f);
+        err = scale < 1 ? resasc * scale : resasc;
+    }
+    if (resabs > FLT_MIN / (50 * FLT_EPSILON)) {
+        const float min_err = 50 * FLT_EPSILON * resabs;
+        if (min_err > err) err = min_err;
+    }
+    return err;
+}
+
+struct GK21f { float xgk[11], wgk[11], wg[5]; };
+
+template <class F>
+FJ_HD void gk21_f(F &f, const GK21f &K, float a, float b, float &res, float &abserr, float &resabs, float &resasc)
+{
+    float fv1[11], fv2[11];
+    const float center = 0.5f * (a + b), half = 0.5f * (b - a), ahalf = fabsf(half);
+    const float fc = f(center);
+    float rg = 0, rk = fc * K.wgk[10], ra = fabsf(rk);
+    FJ_UNROLL
+    for (int j = 0; j < 5; j++) {
+        const int jj = 2 * j + 1;
+        const float x = half * K.xgk[jj];
+        const float f1 = f(center - x), f2 = f(center + x);
+        fv1[jj] = f1; fv2[jj] = f2;
+        rg += K.wg[j] * (f1 + f2);
+        rk += K.wgk[jj] * (f1 + f2);
+        ra += K.wgk[jj] * (fabsf(f1) + fabsf(f2));
+    }
+    FJ_UNROLL
+    for (int j = 0; j < 5; j++) {
+        const int jj = 2 * j;
+        const float x = half * K.xgk[jj];
+        const float f1 = f(center - x), f2 = f(center + x);
+        fv1[jj] = f1; fv2[jj] = f2;
+        rk += K.wgk[jj] * (f1 + f2);
+        ra += K.wgk[jj] * (fabsf(f1) + fabsf(f2));
+    }
+    const float mean = 0.5f * rk;
+    float rasc = K.wgk[10] * fabsf(fc - mean);
+    FJ_UNROLL
+    for (int j = 0; j < 10; j++) rasc += K.wgk[j] * (fabsf(fv1[j] - mean) + fabsf(fv2[j] - mean));
+    const float err = (rk - rg) * half;
+    rk *= half; ra *= ahalf; rasc *= ahalf;
+    res = rk; resabs = ra; resasc = rasc;
+    abserr = rescale_err_f(err, ra, rasc);
+}
+
+FJ_HD void qelg_f(float *tab, int &n_io, float *res3, int &nres, float &result, float &abserr)
+{
+    const int n = n_io - 1;
+    const float current = tab[n];
+    result = current;
+    abserr = FLT_MAX;
+    if (n < 2) return;
+    tab[n + 2] = tab[n];
+    tab[n] = FLT_MAX;
+    const int newelm = n / 2;
+    int n_final = n;
+    for (int i = 0; i < newelm; i++) {
+        float res = tab[n - 2 * i + 2];
+        const float e0 = tab[n - 2 * i - 2], e1 = tab[n - 2 * i - 1], e2 = res;
+        const float e1abs = fabsf(e1);
+        const float delta2 = e2 - e1, err2 = fabsf(delta2);
+        const float tol2 = fmaxf(fabsf(e2), e1abs) * FLT_EPSILON;
+        const float delta3 = e1 - e0, err3 = fabsf(delta3);
+        const float tol3 = fmaxf(e1abs, fabsf(e0)) * FLT_EPSILON;
+        if (err2 <= tol2 && err3 <= tol3) {
+            result = res;
+            abserr = fmaxf(err2 + err3, 5 * FLT_EPSILON * fabsf(res));
+            return;
+        }
+        const float e3 = tab[n - 2 * i];
+        tab[n - 2 * i] = e1;
+        const float delta1 = e1 - e3, err1 = fabsf(delta1);
+        const float tol1 = fmaxf(e1abs, fabsf(e3)) * FLT_EPSILON;
+        if (err1 <= tol1 || err2 <= tol2 || err3 <= tol3) { n_final = 2 * i; break; }
+        const float ss = (1 / delta1 + 1 / delta2) - 1 / delta3;
+        if (fabsf(ss * e1) <= 0.0001f) { n_final = 2 * i; break; }
+        res = e1 + 1 / ss;
+        tab[n - 2 * i] = res;
+        const float error = err2 + fabsf(res - e2) + err3;
+        if (error <= abserr) { abserr = error; result = res; }
+    }
+    if (n_final == 49) n_final = 48;
+    if (n % 2 == 1) { for (int i = 0; i <= newelm; i++) tab[1 + 2 * i] = tab[2 * i + 3]; }
+    else { for (int i = 0; i <= newelm; i++) tab[2 * i] = tab[2 * i + 2]; }
+    if (n != n_final) for (int i = 0; i <= n_final; i++) tab[i] = tab[n - n_final + i];
+    n_io = n_final + 1;
+    if (nres < 3) { res3[nres] = result; abserr = FLT_MAX; }
+    else {
+        abserr = fabsf(result - res3[2]) + fabsf(result - res3[1]) + fabsf(result - res3[0]);
+        res3[0] = res3[1]; res3[1] = res3[2]; res3[2] = result;
+    }
+    nres += 1;
+    abserr = fmaxf(abserr, 5 * FLT_EPSILON * fabsf(result));
+}
+
+constexpr int kQagsCapF = 64;
+
+// QAGS (DQAGSE) in FP32 on [a,b] with the reference's tolerances; interval
+// list of kQagsCapF entries on the thread's stack.
+template <class F>
+FJ_HDNI float qags_f(F &f, const GK21f &K, float a, float b, float epsabs, float epsrel, unsigned &fail)
+{
+    const int limit = 1000;
+    float res0, err0, resabs0, resasc0;
+    gk21_f(f, K, a, b, res0, err0, resabs0, resasc0);
+    const float tol = fmaxf(epsabs, epsrel * fabsf(res0));
+    if (err0 <= 100 * FLT_EPSILON * resabs0 && err0 > tol) return res0;
+    if ((err0 <= tol && err0 != resasc0) || err0 == 0.0f) return res0;
+
+    float alist[kQagsCapF], blist[kQagsCapF], rlist[kQagsCapF], elist[kQagsCapF];
+    int iord[kQagsCapF];
+    float rlist2[52], res3la[3];
+    int nres = 0, numrl2 = 1;
+    alist[0] = a; blist[0] = b; rlist[0] = res0; elist[0] = err0; iord[0] = 0;
+    rlist2[0] = res0;
+    float area = res0, errsum = err0, errmax = err0;
+    int maxerr = 0, nrmax = 0, last = 1, ier = 0;
+    float res_ext = res0, err_ext = FLT_MAX, correc = 0, ertest = 0, erlarg = 0, small = 0;
+    int ktmin = 0, ierro = 0, iroff1 = 0, iroff2 = 0, iroff3 = 0;
+    bool extrap = false, noext = false, done_sum = false;
+    const int ksgn = fabsf(res0) >= (1 - 50 * FLT_EPSILON) * resabs0 ? 1 : -1;
+    for (last = 1; last < limit; last++) {
+        if (last >= kQagsCapF) { fail |= kFailQuad; last = kQagsCapF - 1; done_sum = true; break; }
+        const float a1 = alist[maxerr], b1 = 0.5f * (alist[maxerr] + blist[maxerr]);
+        const float a2 = b1, b2 = blist[maxerr];
+        const float erlast = errmax;
+        float area1, error1, ra1, rasc1, area2, error2, ra2, rasc2;
+        gk21_f(f, K, a1, b1, area1, error1, ra1, rasc1);
+        gk21_f(f, K, a2, b2, area2, error2, ra2, rasc2);
+        const float area12 = area1 + area2, erro12 = error1 + error2;
+        errsum = errsum + erro12 - errmax;
+        area = area + area12 - rlist[maxerr];
+        if (!(rasc1 == error1 || rasc2 == error2)) {
+            if (fabsf(rlist[maxerr] - area12) <= 1e-5f * fabsf(area12) && erro12 >= 0.99f * errmax) {
+                if (extrap) iroff2++; else iroff1++;
+            }
+            if (last > 9 && erro12 > errmax) iroff3++;
+        }
+        rlist[maxerr] = area1;
+        rlist[last] = area2;
+        const float errbnd = fmaxf(epsabs, epsrel * fabsf(area));
+        if (iroff1 + iroff2 >= 10 || iroff3 >= 20) ier = 2;
+        if (iroff2 >= 5) ierro = 3;
+        if (fmaxf(fabsf(a1), fabsf(b2)) <= (1 + 100 * FLT_EPSILON) * (fabsf(a2) + 1000 * FLT_MIN)) ier = 4;
+        if (!(error2 > error1)) {
+            alist[last] = a2; blist[maxerr] = b1; blist[last] = b2;
+            elist[maxerr] = error1; elist[last] = error2;
+        } else {
+            alist[maxerr] = a2; alist[last] = a1; blist[last] = b1;
+            rlist[maxerr] = area2; rlist[last] = area1;
+            elist[maxerr] = error2; elist[last] = error1;
+        }
+        {   // DQPSRT
+            const int L = last + 1;
+            if (L <= 2) { iord[0] = 0; iord[1] = 1; }
+            else {
+                const float em = elist[maxerr];
+                int nr1 = nrmax + 1;
+                if (nr1 != 1) {
+                    const int ido = nr1 - 1;
+                    for (int i = 1; i <= ido; i++) {
+                        const int isucc = iord[nr1 - 2];
+                        if (em <= elist[isucc]) break;
+                        iord[nr1 - 1] = isucc;
+                        nr1--;
+                    }
+                }
+                const int jupbn = L, jbnd = jupbn - 1, ibeg = nr1 + 1;
+                const float errmin = elist[L - 1];
+                int i = ibeg;
+                bool found = false;
+                if (ibeg <= jbnd) {
+                    for (i = ibeg; i <= jbnd; i++) {
+                        const int isucc = iord[i - 1];
+                        if (em >= elist[isucc]) { found = true; break; }
+                        iord[i - 2] = isucc;
+                    }
+                }
+                if (!found) { iord[jbnd - 1] = maxerr; iord[jupbn - 1] = L - 1; }
+                else {
+                    iord[i - 2] = maxerr;
+                    int k = jbnd;
+                    bool ins = false;
+                    for (int j = i; j <= jbnd; j++) {
+                        const int isucc = iord[k - 1];
+                        if (errmin < elist[isucc]) { iord[k] = L - 1; ins = true; break; }
+                        iord[k] = isucc;
+                        k--;
+                    }
+                    if (!ins) iord[i - 1] = L - 1;
+                }
+                nrmax = nr1 - 1;
+            }
+            maxerr = iord[nrmax];
+            errmax = elist[maxerr];
+        }
+        if (errsum <= errbnd) { done_sum = true; break; }
+        if (ier) break;
+        if (last == 1) {
+            small = fabsf(b - a) * 0.375f;
+            erlarg = errsum;
+            ertest = errbnd;
+            rlist2[1] = area; numrl2 = 2;
+            continue;
+        }
+        if (noext) continue;
+        erlarg -= erlast;
+        if (fabsf(b1 - a1) > small) erlarg += erro12;
+        if (!extrap) {
+            if (fabsf(blist[maxerr] - alist[maxerr]) > small) continue;
+            extrap = true;
+            nrmax = 1;
+        }
+        bool do_ext = true;
+        if (!(ierro == 3 || erlarg <= ertest)) {
+            for (int k = nrmax + 1; k <= last + 1; k++) {
+                maxerr = iord[nrmax];
+                errmax = elist[maxerr];
+                if (fabsf(blist[maxerr] - alist[maxerr]) > small) { do_ext = false; break; }
+                nrmax++;
+            }
+        }
+        if (!do_ext) continue;
+        rlist2[numrl2] = area; numrl2++;
+        float reseps, abseps;
+        qelg_f(rlist2, numrl2, res3la, nres, reseps, abseps);
+        ktmin++;
+        if (ktmin > 5 && err_ext < 1e-3f * errsum) ier = 5;
+        if (abseps < err_ext) {
+            ktmin = 0;
+            err_ext = abseps;
+            res_ext = reseps;
+            correc = erlarg;
+            ertest = fmaxf(epsabs, epsrel * fabsf(reseps));
+            if (err_ext <= ertest) break;
+        }
+        if (numrl2 == 1) noext = true;
+        if (ier == 5) break;
+        maxerr = iord[0];
+        errmax = elist[maxerr];
+        nrmax = 0;
+        extrap = false;
+        small *= 0.5f;
+        erlarg = errsum;
+    }
+    bool take_sum = done_sum;
+    float result = res_ext;
+    if (!done_sum) {
+        if (err_ext == FLT_MAX) take_sum = true;
+        else if (ier + ierro != 0) {
+            if (ierro == 3) err_ext += correc;
+            if (res_ext != 0.0f && area != 0.0f) {
+                if (err_ext / fabsf(res_ext) > errsum / fabsf(area)) take_sum = true;
+            } else if (err_ext > errsum) take_sum = true;
+        }
+    }
+    if (take_sum) {
+        float s = 0;
+        for (int k = 0; k <= last; k++) s += rlist[k];
+        result = s;
+    }
+    (void)ksgn;
+    return result;
+}
+
+// ----------------------------------------------------------- fudge, FP32
+// The u and v equations of uvOrb.cpp:38-52 written about the phase point
+// itself, in offsets that keep their relative precision when the orbit's
+// excursion is small (a near-circular orbit, a thin disc orbit):
+//   u = u_pt + t:  U(t) = Ds K + EC + Lt Ds / (s^2 sh^2) - (s^2 + sv^2) dPhi,
+//                  s = sinh(u), sh = sinh(u_pt), Ds = s^2 - sh^2 formed for
+//                  |t| < 1/2 from sinh(t) and cosh(t) - 1 = 2 sinh^2(t/2); for
+//                  |t| >= 1/2, Ds K + EC = s^2 K + C0 with C0 = EC - sh^2 K
+//                  formed in FP64 (far from the focus sh^2 K and EC are ~(r/Delta)^2
+//                  times larger than U);
+//   v = pi/2 - w:  V(w) = Dv (K + Lt / (sv^2 cos^2 w)) + pv^2/(2 Delta^2) - (sh^2 + cos^2 w) dPhi,
+//                  Dv = cos^2 v_pt - sin^2 w = (|cos v_pt| - sin w)(|cos v_pt| + sin w);
+// Lt = Lz^2/(2 Delta^2), EC = pu^2/(2 Delta^2), K = E - Phi_pt the kinetic
+// energy of the node, dPhi = Phi - Phi_pt from pot_dphi_f (on these lines
+// r^2 - r_pt^2 = Delta^2 Ds and -Delta^2 Dv).  Both follow from the reference's equations with the
+// reference point u0 = u_pt (the u-equation does not depend on u0; it cancels
+// exactly) and the Phi(pi/2) terms of Iv and dV cancelled.  The v-equation
+// near the pole (v -> 0) keeps v itself as the variable, with
+// Dv = sin^2 v - sin^2 v_pt formed as (sin v - sin v_pt)(sin v + sin v_pt).
+struct FudgeF {
+    PotViewF P;
+    float Delta, D2, K, EC, C0, Lt, shu2, sv2, swp, svp, sinv, cosv, sinhu, coshu, pvterm;
+    float rpt, c2pt, Phipt;  // the point: radius, cos^2 of its polar angle, FP32 potential
+    double u_pt;
+    float tb, Dt;  // Ju: centre and half-width of [t_in, t_out]
+    float wt;      // Jv: turning point in w
+    FJ_HD float uturn_t(float t) const
+    {
+        float s, c, Ds, KE;
+        if (fabsf(t) < .5f) {  // offsets: no cancellation for |t| < 1/2
+            const float st = sinhf(t), h = sinhf(.5f * t), cm1 = 2.f * h * h;
+            const float ds = sinhu * cm1 + coshu * st;  // sinh(u_pt + t) - sinh(u_pt)
+            s = sinhu + ds;
+            c = coshu + coshu * cm1 + sinhu * st;
+            Ds = ds * (s + sinhu);
+            KE = Ds * K + EC;
+        } else {  // far from the point the direct form has no cancellation
+            const float u = (float)u_pt + t;
+            s = sinhf(u);
+            c = coshf(u);
+            Ds = s * s - shu2;
+            KE = s * s * K + C0;
+        }
+        const float s2 = s * s, cv2 = swp * swp;
+        const float dc2 = -cv2 * sv2 * Ds / ((s2 + cv2) * (shu2 + cv2));
+        const float dphi = pot_dphi_f(P, Delta * s * sinv, Delta * c * cosv, rpt, c2pt, D2 * Ds, dc2, Phipt);
+        const float lz = Lt > 0.f ? Lt * Ds / (s2 * shu2) : 0.f;
+        return KE + lz - (s2 + sv2) * dphi;
+    }
+    // dU/du for the bracket's slope tests (uvOrb.cpp:54-61); E - Phi = K - (Phi - Phi_pt)
+    FJ_HD float duturnfn(float u) const
+    {
+        const float shu = sinhf(u), chu = coshf(u), s2 = shu * shu;
+        const float sv = sqrtf(sv2), cv = cosv < 0.f ? -swp : swp;
+        float phi0, f0, f1;
+        pot_grad_f(P, Delta * shu * sinv, Delta * chu * cosv, phi0, f0, f1);
+        const float dPhidu = Delta * (f0 * chu * sv + f1 * shu * cv);
+        return 2.f * (K - (phi0 - Phipt)) * shu * chu - (s2 + sv2) * dPhidu + 2.f * Lt * chu / (s2 * shu);
+    }
+    FJ_HD float vturn_w(float w) const
+    {
+        float sw, cw;
+        sincosf(w, &sw, &cw);
+        const float Dv = (swp - sw) * (swp + sw), s2 = cw * cw, sw2 = sw * sw;
+        const float dc2 = -(1.f + shu2) * shu2 * Dv / ((shu2 + sw2) * (shu2 + swp * swp));
+        const float dphi = pot_dphi_f(P, Delta * sinhu * cw, Delta * coshu * sw, rpt, c2pt, -D2 * Dv, dc2, Phipt);
+        const float lz = Lt > 0.f ? Lt / (sv2 * s2) : 0.f;
+        return Dv * (K + lz) + pvterm - (shu2 + s2) * dphi;
+    }
+    // the same function of v itself, for orbits reaching the pole
+    FJ_HD float vturn_v(float v) const
+    {
+        float sn, cs;
+        sincosf(v, &sn, &cs);
+        const float s2 = sn * sn;
+        const float Dv = (sn - svp) * (sn + svp);  // sin^2 v - sin^2 v_pt
+        const float dc2 = -(1.f + shu2) * shu2 * Dv / ((shu2 + cs * cs) * (shu2 + swp * swp));
+        const float dphi = pot_dphi_f(P, Delta * sinhu * sn, Delta * coshu * cs, rpt, c2pt, -D2 * Dv, dc2, Phipt);
+        const float lz = Lt > 0.f ? Lt / (sv2 * s2) : 0.f;
+        return Dv * (K + lz) + pvterm - (shu2 + s2) * dphi;
+    }
+};
+
+struct UturnTf { const FudgeF *o; FJ_HD float operator()(float t) const { return o->uturn_t(t); } };
+struct VturnWf { const FudgeF *o; FJ_HD float operator()(float w) const { return o->vturn_w(w); } };
+struct VturnVf { const FudgeF *o; FJ_HD float operator()(float v) const { return o->vturn_v(v); } };
+// Ju integrand (uvOrb.cpp:226-239): u = ubar - Deltau cos(psi)
+struct JuIntFf {
+    const FudgeF *o;
+    FJ_HD float operator()(float psi) const
+    {
+        float sn, cs;
+        sincosf(psi, &sn, &cs);
+        return sqrtf(fmaxf(0.f, o->uturn_t(o->tb - o->Dt * cs))) * sn;
+    }
+};
+// Jv integrand (uvOrb.cpp:247-257): v = pi/2 - (pi/2 - vturn) cos(psi)
+struct JvIntFf {
+    const FudgeF *o;
+    FJ_HD float operator()(float psi) const
+    {
+        float sn, cs;
+        sincosf(psi, &sn, &cs);
+        const float w = o->wt * cs;
+        const float V = w <= .5f * kPIHf ? o->vturn_w(w) : o->vturn_v(kPIHf - w);
+        return sqrtf(fmaxf(0.f, V)) * sn;
+    }
+};
+
+// uvOrb::GetTurnu (uvOrb.cpp:131-201): the bracket walk in FP64 positions
+// (cheap scalar steps, the same step sequence as the reference down to its
+// 1e-12 refinement limit, where Jr = 0), the u-equation in FP32, Brent in
+// t = u - u_pt.  Returns false when the u-equation leaves the FP32 range
+// (sinh(u)^2 overflows beyond u ~ 44) or at the step cap; the caller then
+// redoes the u solve in FP64.
+FJ_HDNI bool get_turn_u_f(FudgeF &o, double utry, float &tin, float &tout, unsigned &fail)
+{
+    UturnTf U{&o};
+    const double u0 = o.u_pt;
+    double u1 = utry, u2 = utry, uin = utry, uout = utry, eps = .1;
+    float ut = U((float)(utry - u0)), dut = o.duturnfn((float)utry);
+    int it = 0;
+#define FJ_STEP_U(x) { ut = U((float)((x) - u0)); if (++it > kLoopCap || !isfinite(ut)) return false; }
+#define FJ_STEP_UD(x) { ut = U((float)((x) - u0)); dut = o.duturnfn((float)(x)); \
+                        if (++it > kLoopCap || !isfinite(ut)) return false; }
+    if (!isfinite(ut)) return false;
+    if (ut < 0) {
+        if (dut > 0) {
+            uin = utry;
+            for (;;) {
+                while (ut < 0 && dut > 0) { uin = utry; utry *= (1 + eps); FJ_STEP_UD(utry); }
+                if (ut >= 0) { u1 = utry; break; }
+                utry /= (1 + eps); eps *= .2;
+                if (eps < kTINY) { tin = tout = (float)(utry - u0); return true; }
+                utry *= (1 + eps);
+                FJ_STEP_UD(utry);
+            }
+            while (ut > 0) { u2 = utry; utry *= 1.1; FJ_STEP_U(utry); }
+            uout = utry;
+        } else {
+            for (;;) {
+                while (ut < 0 && dut < 0) { uout = utry; utry /= (1 + eps); FJ_STEP_UD(utry); }
+                if (ut >= 0) { u2 = utry; break; }
+                utry *= (1 + eps); eps *= .2;
+                if (eps < kTINY) { tin = tout = (float)(utry - u0); return true; }
+                utry /= (1 + eps);
+                FJ_STEP_UD(utry);
+            }
+            while (ut > 0) { u1 = utry; utry *= .9; FJ_STEP_U(utry); }
+            uin = utry;
+        }
+    } else {
+        const float fu1 = ut;
+        while (ut > 0) { u2 = utry; utry *= 1.1; FJ_STEP_U(utry); }
+        uout = utry;
+        ut = fu1;
+        while (ut > 0) { u1 = utry; utry *= .9; FJ_STEP_U(utry); }
+        uin = utry;
+    }
+#undef FJ_STEP_U
+#undef FJ_STEP_UD
+    fail |= brent_root_f(U, (float)(uin - u0), (float)(u1 - u0), tin);
+    fail |= brent_root_f(U, (float)(u2 - u0), (float)(uout - u0), tout);
+    return true;
+}
+
+// uvOrb::GetTurnv (uvOrb.cpp:203-224) with the turning point returned as
+// w = pi/2 - v.  Towards the equator the walk halves w, towards the pole it
+// halves v (both exact in FP32), down to the reference's 1e-12 limits.
+// Returns false at the step cap (the caller redoes the v solve in FP64).
+FJ_HDNI bool get_turn_v_f(FudgeF &o, float &wturn, unsigned &fail)
+{
+    const float q = .5f * kPIHf;  // vtry = pi/4
+    int it = 0;
+    if (o.vturn_w(q) < 0) {
+        VturnWf V{&o};
+        float wbot = q;
+        while (V(wbot) < 0) {
+            wbot *= .5f;
+            if (wbot < 1e-12f) { wturn = 0.f; return true; }
+            if (++it > kLoopCap) return false;
+        }
+        fail |= brent_root_f(V, q, wbot, wturn);
+    } else {
+        VturnVf V{&o};
+        float vtop = q;
+        while (V(vtop) > 0) {
+            vtop *= .5f;
+            if (vtop < 1e-12f) { wturn = kPIHf; return true; }
+            if (++it > kLoopCap) return false;
+        }
+        float vt;
+        fail |= brent_root_f(V, vtop, q, vt);
+        wturn = kPIHf - vt;
+    }
+    return true;
+}
+
+// FP64 fudge state with the reference point u0 at the orbit's own u
+// (the u-equation does not depend on u0), for turning points at the limits.
+FJ_HDNI void fudge64_at_point(Fudge &o, const PotView &P, double Delta, double Lzsq, double E, double u, double v,
+                              double shu2, double sv, double cv, double sv2, double pu, double pv)
+{
+    o.P = P; o.fail = 0; o.Delta = Delta; o.Lzsq = Lzsq; o.E = E;
+    o.u = u; o.v = v; o.shu2 = shu2; o.sv = sv; o.cv = cv; o.sv2 = sv2;
+    sincos(v, &o.sinv, &o.cosv);
+    o.sinhu = sinh(u);
+    o.coshu = cosh(u);
+    o.sh1sq = o.sinhu * o.sinhu;
+    o.ch1sq = o.coshu * o.coshu;
+    o.umid = u;
+    o.Phiu1 = o.Phiu(o.sinhu, o.coshu);
+    o.PhivPIH = o.Phiv(sin(kPIH), cos(kPIH));
+    const double D2 = Delta * Delta;
+    o.Er = .5 * (pu * pu) / (D2 * o.ch1sq);
+    double sn, cs;
+    sincos(v, &sn, &cs);
+    const double dVv = (1 + shu2) * o.PhivPIH - (shu2 + sn * sn) * o.Phiv(sn, cs);
+    o.Iv = .5 * (pv * pv) / D2 - E * sv2 + .5 * Lzsq / (D2 * sv2) - dVv;
+}
+
+// FP32 tables of PotViewF for the phase point whose potential is Phi_h;
+// entries i0, i0 + stride, ... (a block's threads share the work).  ih has
+// nr-1 entries, qc 4*kQuadIntervals.
+FJ_HD void mixed_tables_f(int nr, int npoly, const double *ar, const double *phil, const double *Pr, double Phi_h,
+                          float *far, float *fphil, float *fPr, float *ih, float *qc, int i0, int stride)
+{
+    for (int i = i0; i < nr; i += stride) far[i] = (float)ar[i];
+    for (int i = i0; i < nr - 1; i += stride) ih[i] = (float)(1.0 / (ar[i + 1] - ar[i]));
+    for (int i = i0; i < 4 * kQuadIntervals; i += stride) {
+        const int n = i / 4, j = i % 4, thr = j < 2 ? n - 1 : n + 2;
+        double v = 0;
+        if (thr >= 0 && thr < nr && n + 1 < nr)
+            v = j % 2 == 0 ? 1.0 / ((ar[thr] - ar[n + 1]) * (ar[thr] - ar[n])) : (ar[thr] - ar[n]) / (ar[n + 1] - ar[n]);
+        qc[i] = (float)v;
+    }
+    for (int i = i0; i < nr * npoly; i += stride) {
+        fphil[i] = (float)(i % npoly == 0 ? phil[i] - Phi_h : phil[i]);
+        fPr[i] = (float)Pr[i];
+    }
+}
+
+// PotViewF over tables built by mixed_tables_f
+FJ_HD PotViewF mixed_view_f(int nr, int npoly, const double *ar, const double *phil, double Phi_h, const float *far,
+                            const float *fphil, const float *fPr, const float *ih, const float *qc)
+{
+    PotViewF v;
+    v.nr = nr; v.npoly = npoly; v.ar = far; v.phil = fphil; v.Pr = fPr; v.ih = ih; v.qc = qc;
+    v.out0 = (float)phil[(nr - 1) * npoly];
+    v.shift = (float)Phi_h;
+    v.lr0 = (float)log(ar[0]);
+    v.idl = (float)((nr - 1) / log(ar[nr - 1] / ar[0]));
+    return v;
+}
+
+// One velocity node of the mixed form: the prolate-spheroidal transform of
+// the phase point (Uvpt.cpp:11-24) in FP64, Ju and Jv (uvOrb.cpp:226-257)
+// with FP32 turning points and QAGS, FP64 turning points at the limits, and
+// the double-power-law DF (DF.cpp:65-76,108-119) in FP32.  PF is shifted by
+// PF.shift = Phi_h (mixed_tables_f); the node's energy enters shifted too.
+// Returns the DF (NaN -> 0 as DF.cpp:105); fail gets the kFail* bits,
+// esc = 1 when the FP64 turning-point path ran; J (optional) the actions.
+FJ_HDNI double mixed_node_df(const PotView &P, const PotViewF &PF, const GK21f &K, const DFDev &d, double Delta,
+                             double R, double z, double Phi_h, double V0, double V1, double V2, unsigned &fail,
+                             unsigned &esc, double *J = nullptr)
+{
+    const double Lz = R * V1, Lzsq = Lz * Lz;
+    const double D2 = Delta * Delta, R2 = R * R, z2 = z * z, r2 = R2 + z2;
+    const double dmr = D2 - r2, dpr = D2 + r2;
+    const double shu2 = .5 * (r2 - D2 + sqrt(dmr * dmr + 4 * D2 * R2)) / D2;
+    const double shu = sqrt(shu2), chu = sqrt(1 + shu2);
+    const double u = asinh(shu);
+    const double cv2 = .5 * (r2 + D2 - sqrt(dpr * dpr - 4 * D2 * z2)) / D2;
+    const double cv = z < 0 ? -sqrt(cv2) : sqrt(cv2);
+    const double v = acos(cv), sv = sin(v), sv2 = 1 - cv2;
+    const double pu = Delta * (V0 * chu * sv + V2 * shu * cv);
+    const double pv = Delta * (V0 * shu * cv - V2 * chu * sv);
+    const double E = .5 * (V0 * V0 + V2 * V2) + .5 * Lzsq / R2 + Phi_h;
+    double Jr = 1e31, Jz = 1e31;
+    if (!(E >= 0 || isnan(E))) {
+        FudgeF o;
+        o.P = PF;
+        o.Delta = (float)Delta;
+        o.D2 = (float)D2;
+        o.K = (float)(.5 * (V0 * V0 + V2 * V2) + .5 * Lzsq / R2);
+        o.EC = (float)(.5 * (pu * pu) / D2);
+        o.C0 = (float)(.5 * (pu * pu) / D2 - shu2 * (.5 * (V0 * V0 + V2 * V2) + .5 * Lzsq / R2));
+        o.Lt = (float)(.5 * Lzsq / D2);
+        o.shu2 = (float)shu2;
+        o.sv2 = (float)sv2;
+        o.swp = (float)fabs(cv);
+        o.svp = (float)sqrt(sv2);
+        double sn, cs;
+        sincos(v, &sn, &cs);
+        o.sinv = (float)sn; o.cosv = (float)cs;
+        o.sinhu = (float)shu; o.coshu = (float)chu;
+        o.pvterm = (float)(.5 * (pv * pv) / D2);
+        o.u_pt = u;
+        o.rpt = (float)(Delta * sqrt(shu2 + cv2));
+        o.c2pt = (float)((1 + shu2) * cv2 / (shu2 + cv2));
+        o.Phipt = pot_phi_f(PF, o.Delta * o.sinhu * o.sinv, o.Delta * o.coshu * o.cosv);
+        Fudge o64;
+        bool have64 = false;
+        const float rtwo = 1.41421356237309505f;
+        float tin, tout;
+        if (!get_turn_u_f(o, 1.0, tin, tout, fail)) {  // u limit: FP64 (uvOrb.cpp:131-201)
+            fudge64_at_point(o64, P, Delta, Lzsq, E, u, v, shu2, sv, cv, sv2, pu, pv);
+            have64 = true;
+            get_turn_u(o64, 1);
+            fail |= o64.fail;
+            tin = (float)(o64.uinner - u); tout = (float)(o64.uouter - u);
+            esc = 1u;
+        }
+        if (fabsf(tout - tin) < 1e-12f) Jr = 0;
+        else {
+            o.tb = .5f * (tin + tout);
+            o.Dt = .5f * (tout - tin);
+            JuIntFf fju{&o};
+            Jr = (double)(rtwo * o.Delta * o.Dt * qags_f(fju, K, 0.f, kPIf, 1e-5f, 1e-3f, fail) / kPIf);
+        }
+        float wt;
+        if (!get_turn_v_f(o, wt, fail)) {  // v at the pole: FP64 (uvOrb.cpp:203-224)
+            if (!have64) fudge64_at_point(o64, P, Delta, Lzsq, E, u, v, shu2, sv, cv, sv2, pu, pv);
+            const double v64 = get_turn_v(o64, .5 * kPIH);
+            fail |= o64.fail;
+            wt = (float)(kPIH - v64);
+            esc = 1u;
+        }
+        if (wt < 1e-12f) Jz = 0;
+        else {
+            o.wt = wt;
+            JvIntFf fjv{&o};
+            Jz = (double)(2.f * rtwo * o.Delta * wt * qags_f(fjv, K, 0.f, kPIHf, 1e-5f, 1e-3f, fail) / kPIf);
+        }
+    }
+    if (J) { J[0] = Jr; J[1] = Jz; }
+    const float Jphi = (float)Lz, jr = (float)Jr, jz = (float)Jz, J0 = (float)d.J0;
+    const float h = jr + (float)d.dphi_h * fabsf(Jphi) + (float)d.dz_h * jz;
+    const float g = jr + (float)d.dphi_g * fabsf(Jphi) + (float)d.dz_g * jz;
+    const float ev = (float)d.norm * fmaxf(0.f, powf(1.f + J0 / h, (float)d.alpha) / powf(1.f + g / J0, (float)d.beta)) /
+                     (float)d.tpi3;
+    float f = d.chi == 0. ? ev : ev + (float)d.k * tanhf((float)d.chi * Jphi / J0) * ev;
+    if (isnan(f)) f = 0.f;
+    return (double)f;
+}
+
+}  // namespace fj

@@ -135,6 +135,11 @@ cudaError_t launch_moments(const MomentArgs &a, cudaStream_t s)
     k_moments<<<(unsigned)nblocks, kMomentBlock, smem, s>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    return launch_moments_finalize(a, s);
+}
+
+cudaError_t launch_moments_finalize(const MomentArgs &a, cudaStream_t s)
+{
     k_moments_finalize<<<(a.npts + 127) / 128, 128, 0, s>>>(a.partial, a.npts, a.blocks_per_point, a.out6);
     return cudaGetLastError();
 }

@@ -1,0 +1,138 @@
+// fj_moments_mixed.cu -- the mixed-precision phase-space kernel (FJ_PREC_MIXED).
+//
+// Same decomposition as k_moments (one thread per node, fixed-order block
+// partials); the per-node arithmetic follows fj_mixed.cuh: FP64 for the
+// node's velocity, energy, focal distance and prolate-spheroidal transform,
+// FP32 for the turning-point searches, the QAGS momentum integrals and the
+// DF, FP64 again for turning points at the u/v limits and for the moments.
+// Built with FMA contraction (the plain form is the rounding-faithful one).
+#include <cstdint>
+
+#include "fj_internal.h"
+#include "fj_mixed.cuh"
+
+namespace fj {
+
+size_t moment_mixed_smem_bytes(const MomentArgs &a)
+{
+    const size_t nt = (size_t)a.P.nr * a.P.npoly;
+    return (a.P.nr + 3 * nt + 2 * a.ngrid + 2 * a.nq + 6 * (kMomentBlock / 32) + 4) * sizeof(double) +
+           (2 * a.P.nr + 2 * nt + 4 * kQuadIntervals) * sizeof(float) + sizeof(GK21f) + 16;
+}
+
+__global__ void __launch_bounds__(kMomentBlock) k_moments_mixed(MomentArgs a)
+{
+    extern __shared__ double sm[];
+    const int nr = a.P.nr, npoly = a.P.npoly, nt = nr * npoly;
+    double *s_ar = sm, *s_phil = s_ar + nr, *s_Pr = s_phil + nt, *s_Pr2 = s_Pr + nt;
+    double *s_Eg = s_Pr2 + nt, *s_Dg = s_Eg + a.ngrid, *s_xq = s_Dg + a.ngrid, *s_wq = s_xq + a.nq;
+    double *s_red = s_wq + a.nq, *s_pt = s_red + 6 * (kMomentBlock / 32);
+    float *f_ar = (float *)(s_pt + 4), *f_phil = f_ar + nr, *f_Pr = f_phil + nt, *f_ih = f_Pr + nt;
+    float *f_qc = f_ih + nr;
+    GK21f *sK = (GK21f *)(((uintptr_t)(f_qc + 4 * kQuadIntervals) + 15) & ~(uintptr_t)15);
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) s_ar[i] = a.P.ar[i];
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+        s_phil[i] = a.P.phil[i]; s_Pr[i] = a.P.Pr[i]; s_Pr2[i] = a.P.Pr2[i];
+    }
+    for (int i = threadIdx.x; i < a.ngrid; i += blockDim.x) { s_Eg[i] = a.Eg[i]; s_Dg[i] = a.Dg[i]; }
+    for (int i = threadIdx.x; i < a.nq; i += blockDim.x) { s_xq[i] = a.xq[i]; s_wq[i] = a.wq[i]; }
+    if (threadIdx.x < 11) {
+        sK->xgk[threadIdx.x] = (float)fj_xgk21_d[threadIdx.x];
+        sK->wgk[threadIdx.x] = (float)fj_wgk21_d[threadIdx.x];
+        if (threadIdx.x < 5) sK->wg[threadIdx.x] = (float)fj_wg10_d[threadIdx.x];
+    }
+    const PotView P{nr, npoly, s_ar, s_phil, s_Pr, s_Pr2};
+    const int B = a.blocks_per_point;
+    const int p = blockIdx.x / B, chunk = blockIdx.x % B;
+    __syncthreads();
+    if (threadIdx.x == 0) {  // per-point FP64 setup, shared by the block (integ/Integ.cpp:46-62,150-151)
+        double R, z;
+        if (a.Rz) { R = a.Rz[2 * p]; z = a.Rz[2 * p + 1]; }
+        else {
+            const int n = p / a.ngauss, g = p % a.ngauss;
+            const double c = a.ci[g], si = sqrt(1 - c * c);
+            R = s_ar[n] * si; z = s_ar[n] * c;
+        }
+        const double rmax = s_ar[nr - 1];
+        const double Phi_h = pot_phi(P, R, z);
+        s_pt[0] = R; s_pt[1] = z; s_pt[2] = Phi_h;
+        s_pt[3] = sqrt(-2 * (Phi_h - pot_phi(P, 10 * rmax, 10 * rmax)));
+    }
+    __syncthreads();
+    const double R = s_pt[0], z = s_pt[1], Phi_h = s_pt[2], Ve = s_pt[3];
+    mixed_tables_f(nr, npoly, s_ar, s_phil, s_Pr, Phi_h, f_ar, f_phil, f_Pr, f_ih, f_qc, threadIdx.x, blockDim.x);
+    __syncthreads();
+    const PotViewF PF = mixed_view_f(nr, npoly, s_ar, s_phil, Phi_h, f_ar, f_phil, f_Pr, f_ih, f_qc);
+    const int nq = a.nq, nq3 = nq * nq * nq;
+    const int node = chunk * kMomentBlock + threadIdx.x;
+
+    double m[6] = {0, 0, 0, 0, 0, 0};
+    unsigned bound = 0, failed = 0, esc = 0;
+    if (node < nq3) {
+        const int i = node / (nq * nq), j = (node / nq) % nq, k = node % nq;
+        const double V0 = 1e-6 + Ve * s_xq[i], V1 = 1e-6 + Ve * s_xq[j], V2 = 1e-6 + Ve * s_xq[k];
+        const double jacob = Ve * Ve * Ve;
+        const double H = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h;
+        double DF = 0.;
+        if (H < 0) {
+            bound = 1;
+            unsigned fail = 0, e = 0;
+            const double Delta = deltafn(s_Eg, s_Dg, a.ngrid, H);
+            const double f = mixed_node_df(P, PF, *sK, a.df, Delta, R, z, Phi_h, V0, V1, V2, fail, e);
+            esc = e;
+            DF = (fail & (kFailBracket | kFailRoot)) ? 0. : f;
+            failed = fail ? 1u : 0u;
+        }
+        const double w = s_wq[i] * s_wq[j] * s_wq[k];
+        const double jd = jacob * DF;
+        m[0] = w * jd;
+        m[1] = w * (jd * V1);
+        m[2] = w * (jd * V0 * V0);
+        m[3] = w * (jd * V1 * V1);
+        m[4] = w * (jd * V2 * V2);
+        m[5] = w * (jd * V0 * V2);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        double v = m[q];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane == 0) s_red[warp * 6 + q] = v;
+    }
+    const unsigned nb = __syncthreads_count(bound);
+    const unsigned nf = __syncthreads_count(failed);
+    const unsigned ne = __syncthreads_count(esc);
+    if (threadIdx.x < 6) {
+        double s = 0;
+        for (int w = 0; w < kMomentBlock / 32; w++) s += s_red[w * 6 + threadIdx.x];
+        a.partial[((size_t)p * B + chunk) * 6 + threadIdx.x] = s;
+    }
+    if (threadIdx.x == 0) {
+        if (nb) atomicAdd(&a.counters[0], (unsigned long long)nb);
+        if (nf) atomicAdd(&a.counters[1], (unsigned long long)nf);
+        if (ne) atomicAdd(&a.counters[3], (unsigned long long)ne);
+    }
+}
+
+cudaError_t launch_moments_mixed(const MomentArgs &a, cudaStream_t s)
+{
+    const size_t smem = moment_mixed_smem_bytes(a);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_moments_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    const long long nblocks = (long long)a.npts * a.blocks_per_point;
+    k_moments_mixed<<<(unsigned)nblocks, kMomentBlock, smem, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return launch_moments_finalize(a, s);
+}
+
+size_t moments_mixed_local_bytes()
+{
+    cudaFuncAttributes at;
+    return cudaFuncGetAttributes(&at, k_moments_mixed) == cudaSuccess ? at.localSizeBytes : 0;
+}
+
+}  // namespace fj

@@ -42,7 +42,8 @@ extern "C" {
 
 /* arithmetic of the phase-space kernel */
 #define FJ_PREC_FP64 0  /* plain form: everything in FP64 */
-#define FJ_PREC_MIXED 1 /* FP32 momentum quadrature and DF, FP64 turning points */
+#define FJ_PREC_MIXED 1 /* FP32 turning points, momentum quadrature and DF; FP64 node setup,
+                           turning points at the u/v limits and accumulation (DPL DF, QAGS only) */
 
 /* momentum integrals of the actions: 0 = adaptive QAGS as the reference
    (include/Utils.h:173-185); n > 0 = fixed n-point Gauss-Legendre */
@@ -95,6 +96,7 @@ typedef struct fj_moment_stats {
     long long bound;     /* nodes with H < 0 */
     long long failures;  /* nodes whose action solve hit a cap */
     double kernel_ms;    /* device time of the phase-space kernel (CUDA events) */
+    long long escalated; /* FJ_PREC_MIXED: nodes whose turning points were solved in FP64 */
 } fj_moment_stats;
 
 /* ---------------------------------------------------------------- context */
@@ -239,6 +241,7 @@ typedef struct fj_model_result {
     double last_change;          /* max|dphil/phil_0| of the last iteration */
     long long bound, failures;
     double wall_ms, kernel_ms;
+    double setup_ms;             /* wall time before the first iteration (grid, guess, Poisson, Delta table) */
 } fj_model_result;
 
 int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_result *res);
