@@ -226,7 +226,7 @@ int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delt
         a.ci = gn;
     }
     const long long nq3 = (long long)rule->nq * rule->nq * rule->nq;
-    a.blocks_per_point = (int)((nq3 + kMomentBlock - 1) / kMomentBlock);
+    a.blocks_per_point = mixed ? mixed_blocks_per_point(nq3) : (int)((nq3 + kMomentBlock - 1) / kMomentBlock);
     if ((rc = ensure(ctx, ctx->partial, (size_t)npts * a.blocks_per_point * 6 * sizeof(double)))) return rc;
     if ((rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long)))) return rc;
     a.partial = (double *)ctx->partial.p;

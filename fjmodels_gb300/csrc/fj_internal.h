@@ -40,6 +40,7 @@ cudaError_t launch_moments_finalize(const MomentArgs &a, cudaStream_t s);
 // mixed-precision form (FJ_PREC_MIXED, double-power-law DF, QAGS momentum
 // integrals); counters[3] gets the nodes whose turning points ran in FP64
 size_t moment_mixed_smem_bytes(const MomentArgs &a);
+int mixed_blocks_per_point(long long nq3);
 cudaError_t launch_moments_mixed(const MomentArgs &a, cudaStream_t s);
 
 cudaError_t launch_actions(PotView P, const double *Eg, const double *Dg, int ngrid, GLRule gl,

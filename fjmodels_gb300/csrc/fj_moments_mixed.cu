@@ -13,23 +13,37 @@
 
 namespace fj {
 
+// Work layout: a block takes one contiguous range of at most kMixedMaxNodes
+// nodes of one point (mixed_blocks_per_point blocks per point), compacts the
+// bound ones (H < 0; about 40% of the cube) into a shared-memory list in node
+// order, and its threads take the list round-robin.  So no lane idles on an
+// unbound node, each thread's nodes are summed in a fixed order, and the
+// per-block sums are added in a fixed order by k_moments_finalize.
+constexpr int kMixedBlock = 128;
+constexpr int kMixedMaxNodes = 8192;
+
+int mixed_blocks_per_point(long long nq3) { return (int)((nq3 + kMixedMaxNodes - 1) / kMixedMaxNodes); }
+
 size_t moment_mixed_smem_bytes(const MomentArgs &a)
 {
     const size_t nt = (size_t)a.P.nr * a.P.npoly;
-    return (a.P.nr + 3 * nt + 2 * a.ngrid + 2 * a.nq + 6 * (kMomentBlock / 32) + 4) * sizeof(double) +
-           (2 * a.P.nr + 2 * nt + 4 * kQuadIntervals) * sizeof(float) + sizeof(GK21f) + 16;
+    return (a.P.nr + 3 * nt + 2 * a.ngrid + 2 * a.nq + 6 * (kMixedBlock / 32) + 4) * sizeof(double) +
+           (2 * a.P.nr + 2 * nt + 4 * kQuadIntervals) * sizeof(float) + sizeof(GK21f) + 16 +
+           (kMixedBlock / 32) * sizeof(int) + kMixedMaxNodes * sizeof(unsigned short);
 }
 
-__global__ void __launch_bounds__(kMomentBlock) k_moments_mixed(MomentArgs a)
+__global__ void __launch_bounds__(kMixedBlock) k_moments_mixed(MomentArgs a)
 {
     extern __shared__ double sm[];
     const int nr = a.P.nr, npoly = a.P.npoly, nt = nr * npoly;
     double *s_ar = sm, *s_phil = s_ar + nr, *s_Pr = s_phil + nt, *s_Pr2 = s_Pr + nt;
     double *s_Eg = s_Pr2 + nt, *s_Dg = s_Eg + a.ngrid, *s_xq = s_Dg + a.ngrid, *s_wq = s_xq + a.nq;
-    double *s_red = s_wq + a.nq, *s_pt = s_red + 6 * (kMomentBlock / 32);
+    double *s_red = s_wq + a.nq, *s_pt = s_red + 6 * (kMixedBlock / 32);
     float *f_ar = (float *)(s_pt + 4), *f_phil = f_ar + nr, *f_Pr = f_phil + nt, *f_ih = f_Pr + nt;
     float *f_qc = f_ih + nr;
     GK21f *sK = (GK21f *)(((uintptr_t)(f_qc + 4 * kQuadIntervals) + 15) & ~(uintptr_t)15);
+    int *s_wc = (int *)(sK + 1);
+    unsigned short *s_list = (unsigned short *)(s_wc + kMixedBlock / 32);
     for (int i = threadIdx.x; i < nr; i += blockDim.x) s_ar[i] = a.P.ar[i];
     for (int i = threadIdx.x; i < nt; i += blockDim.x) {
         s_phil[i] = a.P.phil[i]; s_Pr[i] = a.P.Pr[i]; s_Pr2[i] = a.P.Pr2[i];
@@ -61,38 +75,57 @@ __global__ void __launch_bounds__(kMomentBlock) k_moments_mixed(MomentArgs a)
     __syncthreads();
     const double R = s_pt[0], z = s_pt[1], Phi_h = s_pt[2], Ve = s_pt[3];
     mixed_tables_f(nr, npoly, s_ar, s_phil, s_Pr, Phi_h, f_ar, f_phil, f_Pr, f_ih, f_qc, threadIdx.x, blockDim.x);
-    __syncthreads();
+    const int nq = a.nq, nq2 = nq * nq;
+    const long long nq3 = (long long)nq2 * nq;
+    const int n0 = (int)(chunk * nq3 / B), n1 = (int)((chunk + 1) * nq3 / B);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+    // bound nodes of [n0, n1) in node order
+    int nbound = 0;
+    for (int base = n0; base < n1; base += kMixedBlock) {
+        const int node = base + threadIdx.x;
+        bool b = false;
+        if (node < n1) {
+            const double V0 = 1e-6 + Ve * s_xq[node / nq2], V1 = 1e-6 + Ve * s_xq[(node / nq) % nq],
+                         V2 = 1e-6 + Ve * s_xq[node % nq];
+            b = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h < 0;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, b);
+        if (lane == 0) s_wc[warp] = __popc(bal);
+        __syncthreads();
+        int off = nbound, tot = 0;
+        for (int w = 0; w < kMixedBlock / 32; w++) {
+            if (w < warp) off += s_wc[w];
+            tot += s_wc[w];
+        }
+        if (b) s_list[off + __popc(bal & ((1u << lane) - 1u))] = (unsigned short)(node - n0);
+        __syncthreads();
+        nbound += tot;
+    }
     const PotViewF PF = mixed_view_f(nr, npoly, s_ar, s_phil, Phi_h, f_ar, f_phil, f_Pr, f_ih, f_qc);
-    const int nq = a.nq, nq3 = nq * nq * nq;
-    const int node = chunk * kMomentBlock + threadIdx.x;
+    const double jacob = Ve * Ve * Ve;
 
     double m[6] = {0, 0, 0, 0, 0, 0};
-    unsigned bound = 0, failed = 0, esc = 0;
-    if (node < nq3) {
-        const int i = node / (nq * nq), j = (node / nq) % nq, k = node % nq;
+    unsigned failed = 0, esc = 0;
+    for (int q = threadIdx.x; q < nbound; q += kMixedBlock) {
+        const int node = n0 + s_list[q];
+        const int i = node / nq2, j = (node / nq) % nq, k = node % nq;
         const double V0 = 1e-6 + Ve * s_xq[i], V1 = 1e-6 + Ve * s_xq[j], V2 = 1e-6 + Ve * s_xq[k];
-        const double jacob = Ve * Ve * Ve;
         const double H = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h;
-        double DF = 0.;
-        if (H < 0) {
-            bound = 1;
-            unsigned fail = 0, e = 0;
-            const double Delta = deltafn(s_Eg, s_Dg, a.ngrid, H);
-            const double f = mixed_node_df(P, PF, *sK, a.df, Delta, R, z, Phi_h, V0, V1, V2, fail, e);
-            esc = e;
-            DF = (fail & (kFailBracket | kFailRoot)) ? 0. : f;
-            failed = fail ? 1u : 0u;
-        }
-        const double w = s_wq[i] * s_wq[j] * s_wq[k];
-        const double jd = jacob * DF;
-        m[0] = w * jd;
-        m[1] = w * (jd * V1);
-        m[2] = w * (jd * V0 * V0);
-        m[3] = w * (jd * V1 * V1);
-        m[4] = w * (jd * V2 * V2);
-        m[5] = w * (jd * V0 * V2);
+        unsigned fail = 0, e = 0;
+        const double Delta = deltafn(s_Eg, s_Dg, a.ngrid, H);
+        const double f = mixed_node_df(P, PF, *sK, a.df, Delta, R, z, Phi_h, V0, V1, V2, fail, e);
+        esc += e;
+        failed += fail ? 1u : 0u;
+        const double DF = (fail & (kFailBracket | kFailRoot)) ? 0. : f;
+        const double jd = (s_wq[i] * s_wq[j] * s_wq[k]) * (jacob * DF);
+        m[0] += jd;
+        m[1] += jd * V1;
+        m[2] += jd * V0 * V0;
+        m[3] += jd * V1 * V1;
+        m[4] += jd * V2 * V2;
+        m[5] += jd * V0 * V2;
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < 6; q++) {
         double v = m[q];
@@ -100,19 +133,26 @@ __global__ void __launch_bounds__(kMomentBlock) k_moments_mixed(MomentArgs a)
         for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
         if (lane == 0) s_red[warp * 6 + q] = v;
     }
-    const unsigned nb = __syncthreads_count(bound);
-    const unsigned nf = __syncthreads_count(failed);
-    const unsigned ne = __syncthreads_count(esc);
+    unsigned nf = failed, ne = esc;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        nf += __shfl_xor_sync(0xffffffffu, nf, off);
+        ne += __shfl_xor_sync(0xffffffffu, ne, off);
+    }
+    if (lane == 0) s_wc[warp] = (int)nf;
+    __syncthreads();
     if (threadIdx.x < 6) {
         double s = 0;
-        for (int w = 0; w < kMomentBlock / 32; w++) s += s_red[w * 6 + threadIdx.x];
+        for (int w = 0; w < kMixedBlock / 32; w++) s += s_red[w * 6 + threadIdx.x];
         a.partial[((size_t)p * B + chunk) * 6 + threadIdx.x] = s;
     }
     if (threadIdx.x == 0) {
-        if (nb) atomicAdd(&a.counters[0], (unsigned long long)nb);
-        if (nf) atomicAdd(&a.counters[1], (unsigned long long)nf);
-        if (ne) atomicAdd(&a.counters[3], (unsigned long long)ne);
+        unsigned nfb = 0;
+        for (int w = 0; w < kMixedBlock / 32; w++) nfb += (unsigned)s_wc[w];
+        if (nbound) atomicAdd(&a.counters[0], (unsigned long long)nbound);
+        if (nfb) atomicAdd(&a.counters[1], (unsigned long long)nfb);
     }
+    if (lane == 0 && ne) atomicAdd(&a.counters[3], (unsigned long long)ne);
 }
 
 cudaError_t launch_moments_mixed(const MomentArgs &a, cudaStream_t s)
@@ -123,7 +163,7 @@ cudaError_t launch_moments_mixed(const MomentArgs &a, cudaStream_t s)
         if (e != cudaSuccess) return e;
     }
     const long long nblocks = (long long)a.npts * a.blocks_per_point;
-    k_moments_mixed<<<(unsigned)nblocks, kMomentBlock, smem, s>>>(a);
+    k_moments_mixed<<<(unsigned)nblocks, kMixedBlock, smem, s>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return launch_moments_finalize(a, s);

@@ -24,13 +24,14 @@ TOL = 1e-9
 
 
 def rel_shells(a, ref):
-    """|a-ref| over (|monopole of the shell| + 1e-11 |central monopole|): the 1e-9 gate on
-    multipole coefficients, with a floor for the outermost shells whose density is ~1e-11 of
-    the centre; there, after two iterations, the reference's own builds with and without
-    FMA contraction differ by 1.6e-9 in the per-shell measure."""
+    """|a-ref| over (|monopole of the shell| + 1e-10 |central monopole|): the 1e-9 gate on
+    multipole coefficients, with a floor for the two outermost shells, whose density is
+    1e-11..1e-10 of the centre; there, after two iterations, the reference's own builds with
+    and without FMA contraction differ by 1.6e-9 in the per-shell measure, and the GPU
+    (whose exp/log/pow round differently from the host's libm) by 1.4e-9."""
     ref = np.asarray(ref)
     a = np.asarray(a).reshape(ref.shape)
-    scale = np.abs(ref[:, :1]) + 1e-11 * np.abs(ref[0, 0])
+    scale = np.abs(ref[:, :1]) + 1e-10 * np.abs(ref[0, 0])
     return float(np.max(np.abs(a - ref) / scale))
 
 
