@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="mixed", choices=["mixed", "plain", "gl"])
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison step")
+    ap.add_argument("--mixed-config", default=None,
+                    help="variant,nodes_per_block of the mixed kernel (default: autotuned before warm-up)")
     ap.add_argument("--cpu-sample", type=int, default=os.cpu_count(), help="grid points timed for the CPU baseline")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -185,6 +187,15 @@ def run_ours(args, rank, world):
     coef = torch.zeros((6, nr, npl), **f64)
     nxt = [torch.zeros((nr, npl), **f64) for _ in range(3)]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+    tuned = None
+    if args.form == "mixed" and args.mixed_config:
+        ctx.set_mixed_config(*[int(v) for v in args.mixed_config.split(",")])
+        tuned = {"variant": ctx.mixed_config()[0], "nodes_per_block": ctx.mixed_config()[1], "source": "given"}
+    elif args.form == "mixed":  # pick the kernel configuration on every 7th grid point (untimed)
+        ci, _ = F.gauleg(0, 1, ng)
+        allp = np.array([[ar[n] * np.sqrt(1 - c * c), ar[n] * c] for n in range(nr) for c in ci])
+        v, c, ms = ctx.autotune_mixed(ctx.potential(d_ar, *tabs), delta, df, rule, torch.tensor(allp[::7], **f64))
+        tuned = {"variant": v, "nodes_per_block": c, "sample_kernel_ms": ms, "sample_points": len(allp[::7])}
     state = {"cur": tabs, "nxt": nxt}
     kernel_ms, changes = [], []
 
@@ -240,6 +251,7 @@ def run_ours(args, rank, world):
         "potential_change_last": float(changes[-1].item()) if changes else None,
         "gpu_launches": 4 * args.steps,
         "escalated_evals_per_step": last.escalated, "failed_evals_per_step": last.failures,
+        "mixed_kernel_config": tuned,
         "vs_plain_fp64": vs_plain,
         "roofline": {"bound": "fp32" if fp32 else "fp64", "kernel": "k_moments_mixed" if fp32 else "k_moments",
                      "achieved": achieved, "peak": float(peak[0]),
@@ -278,7 +290,7 @@ def compare_plain(F, ctx, d_ar, cur, delta, df, x, w, ng, grids, f64):
             "note": "one iteration from the same input potential in both forms, all grid points"}
 
 
-def e2e_ours(args):
+def e2e_ours(args, mixed_cfg=None):
     """Same metric through the host-buffer C-ABI call (fj_run_model): host inputs, device
     compute, host outputs, copies inside the timed region.  One run of K iterations: the
     one-time setup (grid, guess density, Poisson, focal-distance table) once plus 20 times
@@ -288,6 +300,8 @@ def e2e_ours(args):
 
     import fjmodels_gb300 as F
     ctx = F.Context(int(os.environ.get("LOCAL_RANK", "0")))
+    if mixed_cfg:
+        ctx.set_mixed_config(mixed_cfg["variant"], mixed_cfg["nodes_per_block"])
     x, w = velocity_rule()
     rule = make_rule(F, args.form, x, w)
     df = F.DFParams(CFG["model"], CFG["dphi_h"], CFG["dz_h"], CFG["dphi_g"], CFG["dz_g"], CFG["chi"], CFG["mass"],
@@ -372,6 +386,8 @@ def profile_case(args):
     allp = np.array([[ar[n] * np.sqrt(1 - c * c), ar[n] * c] for n in range(nr) for c in ci])
     pts = torch.tensor(allp[np.linspace(0, nr * ng - 1, args.profile_points).astype(int)], **f64)
     out = torch.zeros((6, pts.shape[0]), **f64)
+    if args.form == "mixed" and args.mixed_config:
+        ctx.set_mixed_config(*[int(v) for v in args.mixed_config.split(",")])
     st = ctx.moments_points(ctx.potential(d_ar, *tabs), delta, df, rule, pts, out)
     torch.cuda.synchronize()
     print(json.dumps({"profile_points": pts.shape[0], "nodes": st.nodes, "bound": st.bound,
@@ -407,7 +423,7 @@ def main():
     out, _ = run_ours(args, rank, world)
     if rank == 0:
         if not args.no_e2e:
-            out["e2e"] = e2e_ours(args)
+            out["e2e"] = e2e_ours(args, out.get("mixed_kernel_config"))
         if not args.no_cpu and world == 1:
             out["cpu_baseline"] = cpu_sample(args, sample=args.cpu_sample)
         print(json.dumps(out))

@@ -66,6 +66,10 @@ SIGNATURES = {
                     C.c_void_p, P(fj_moment_stats)], C.c_int),
     "fj_moments_points": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule),
                            C.c_void_p, C.c_int, C.c_void_p, P(fj_moment_stats)], C.c_int),
+    "fj_set_mixed_config": ([CTX, C.c_int, C.c_int], C.c_int),
+    "fj_get_mixed_config": ([CTX, P(C.c_int), P(C.c_int)], C.c_int),
+    "fj_autotune_mixed": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule), C.c_void_p,
+                           C.c_int, C.c_void_p, DP], C.c_int),
     "fj_legendre_project": ([CTX, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "fj_poisson": ([CTX, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "fj_poisson_noalloc": ([C.c_int, C.c_int] + [C.c_void_p] * 6, C.c_int),

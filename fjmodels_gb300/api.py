@@ -171,6 +171,26 @@ class Context:
                     "fj_moments_points")
         return st
 
+    def set_mixed_config(self, variant, nodes_per_block):
+        self._check(self.lib.fj_set_mixed_config(self.h, variant, nodes_per_block), "fj_set_mixed_config")
+
+    def mixed_config(self):
+        v, c = C.c_int(), C.c_int()
+        self._check(self.lib.fj_get_mixed_config(self.h, C.byref(v), C.byref(c)), "fj_get_mixed_config")
+        return v.value, c.value
+
+    def autotune_mixed(self, pot, delta, df, rule, Rz):
+        """Time the mixed kernel's configurations on sample points Rz [n][2] (device) and keep
+        the fastest; returns (variant, nodes_per_block, kernel_ms)."""
+        import torch
+        self._on_torch_stream()
+        out = torch.zeros((6, Rz.shape[0]), dtype=torch.float64, device=Rz.device)
+        ms = np.zeros(1)
+        self._check(self.lib.fj_autotune_mixed(self.h, C.byref(pot.c), C.byref(delta.c), C.byref(df.c),
+                                               C.byref(rule.c), _ptr(Rz), Rz.shape[0], _ptr(out), _dp(ms)),
+                    "fj_autotune_mixed")
+        return (*self.mixed_config(), float(ms[0]))
+
     def legendre_project(self, nr, ngauss, npoly, ar, grids6, coef6):
         self._on_torch_stream()
         self._check(self.lib.fj_legendre_project(self.h, nr, ngauss, npoly, _ptr(ar), _ptr(grids6), _ptr(coef6)),

@@ -37,6 +37,7 @@ struct fj_ctx {
     std::map<int, DevBuf> gl_rules;                    // jquad -> [2][n]
     std::vector<double> rule_host;                     // last uploaded velocity rule
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int mixed_variant = 0, mixed_chunk = kMixedMaxNodes;  // mixed kernel configuration (fj_autotune_mixed)
 };
 
 namespace {
@@ -226,7 +227,9 @@ int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delt
         a.ci = gn;
     }
     const long long nq3 = (long long)rule->nq * rule->nq * rule->nq;
-    a.blocks_per_point = mixed ? mixed_blocks_per_point(nq3) : (int)((nq3 + kMomentBlock - 1) / kMomentBlock);
+    a.mixed_chunk = ctx->mixed_chunk;
+    a.blocks_per_point =
+        mixed ? mixed_blocks_per_point(nq3, a.mixed_chunk) : (int)((nq3 + kMomentBlock - 1) / kMomentBlock);
     if ((rc = ensure(ctx, ctx->partial, (size_t)npts * a.blocks_per_point * 6 * sizeof(double)))) return rc;
     if ((rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long)))) return rc;
     a.partial = (double *)ctx->partial.p;
@@ -234,7 +237,7 @@ int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delt
     a.out6 = out6;
     FJ_CUDA(cudaMemsetAsync(a.counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    FJ_CUDA(mixed ? launch_moments_mixed(a, ctx->stream) : launch_moments(a, ctx->stream));
+    FJ_CUDA(mixed ? launch_moments_mixed(a, ctx->mixed_variant, ctx->stream) : launch_moments(a, ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     if (stats) {
         unsigned long long h[4];
@@ -340,6 +343,48 @@ int fj_moments_points(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table
 {
     if (!ctx || !Rz) return fail(ctx, FJ_ERR_ARG, "moments_points: bad arguments");
     return run_moments(ctx, pot, delta, df, rule, 0, Rz, npts, out6, stats);
+}
+
+int fj_set_mixed_config(fj_ctx *ctx, int variant, int nodes_per_block)
+{
+    if (!ctx || variant < 0 || variant >= kMixedVariants || nodes_per_block < kMixedBlock ||
+        nodes_per_block > kMixedMaxNodes)
+        return fail(ctx, FJ_ERR_ARG, "set_mixed_config: variant or nodes per block out of range");
+    ctx->mixed_variant = variant;
+    ctx->mixed_chunk = nodes_per_block;
+    return FJ_OK;
+}
+
+int fj_get_mixed_config(fj_ctx *ctx, int *variant, int *nodes_per_block)
+{
+    if (!ctx || !variant || !nodes_per_block) return FJ_ERR_ARG;
+    *variant = ctx->mixed_variant;
+    *nodes_per_block = ctx->mixed_chunk;
+    return FJ_OK;
+}
+
+int fj_autotune_mixed(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
+                      const fj_quad_rule *rule, const double *Rz, int npts, double *out6, double *best_ms)
+{
+    if (!ctx || !rule || rule->precision != FJ_PREC_MIXED || !Rz || npts < 1 || !out6)
+        return fail(ctx, FJ_ERR_ARG, "autotune_mixed: needs a mixed-precision rule and sample points");
+    static const int chunks[] = {2048, 4096, 8192};
+    const int v0 = ctx->mixed_variant, c0 = ctx->mixed_chunk;
+    int bv = v0, bc = c0;
+    double best = -1;
+    for (int v = 0; v < kMixedVariants; v++)
+        for (int c : chunks) {
+            ctx->mixed_variant = v;
+            ctx->mixed_chunk = c;
+            fj_moment_stats st;
+            int rc = run_moments(ctx, pot, delta, df, rule, 0, Rz, npts, out6, &st);
+            if (rc) { ctx->mixed_variant = v0; ctx->mixed_chunk = c0; return rc; }
+            if (best < 0 || st.kernel_ms < best) { best = st.kernel_ms; bv = v; bc = c; }
+        }
+    ctx->mixed_variant = bv;
+    ctx->mixed_chunk = bc;
+    if (best_ms) *best_ms = best;
+    return FJ_OK;
 }
 
 int fj_legendre_project(fj_ctx *ctx, int nr, int ngauss, int npoly, const double *ar, const double *grids6,

@@ -28,6 +28,7 @@ struct MomentArgs {
     const double *Rz;        // point mode: [npts][2]; else NULL
     int npts;
     int blocks_per_point;
+    int mixed_chunk;         // mixed form: nodes per block (<= kMixedMaxNodes)
     double *partial;         // [npts][blocks_per_point][6]
     unsigned long long *counters;  // [0] bound nodes, [1] failed nodes, [3] FP64 escalations
     double *out6;            // [6][npts]
@@ -39,9 +40,12 @@ cudaError_t launch_moments(const MomentArgs &a, cudaStream_t s);
 cudaError_t launch_moments_finalize(const MomentArgs &a, cudaStream_t s);
 // mixed-precision form (FJ_PREC_MIXED, double-power-law DF, QAGS momentum
 // integrals); counters[3] gets the nodes whose turning points ran in FP64
+constexpr int kMixedBlock = 128;     // threads per block of the mixed kernel
+constexpr int kMixedMaxNodes = 8192; // largest node range of one block (shared-memory list)
+constexpr int kMixedVariants = 4;    // register budgets the mixed kernel is built in
 size_t moment_mixed_smem_bytes(const MomentArgs &a);
-int mixed_blocks_per_point(long long nq3);
-cudaError_t launch_moments_mixed(const MomentArgs &a, cudaStream_t s);
+int mixed_blocks_per_point(long long nq3, int chunk);
+cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, cudaStream_t s);
 
 cudaError_t launch_actions(PotView P, const double *Eg, const double *Dg, int ngrid, GLRule gl,
                            const double *pts, size_t n, double *out, cudaStream_t s);

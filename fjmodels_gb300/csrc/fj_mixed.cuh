@@ -323,7 +323,7 @@ FJ_HD float rescale_err_f(float err, float resabs, float resasc)
 struct GK21f { float xgk[11], wgk[11], wg[5]; };
 
 template <class F>
-FJ_HD void gk21_f(F &f, const GK21f &K, float a, float b, float &res, float &abserr, float &resabs, float &resasc)
+FJ_HDNI void gk21_f(F &f, const GK21f &K, float a, float b, float &res, float &abserr, float &resabs, float &resasc)
 {
     float fv1[11], fv2[11];
     const float center = 0.5f * (a + b), half = 0.5f * (b - a), ahalf = fabsf(half);
@@ -604,87 +604,95 @@ struct FudgeF {
     double u_pt;
     float tb, Dt;  // Ju: centre and half-width of [t_in, t_out]
     float wt;      // Jv: turning point in w
-    FJ_HD float uturn_t(float t) const
-    {
-        float s, c, Ds, KE;
-        if (fabsf(t) < .5f) {  // offsets: no cancellation for |t| < 1/2
-            const float st = sinhf(t), h = sinhf(.5f * t), cm1 = 2.f * h * h;
-            const float ds = sinhu * cm1 + coshu * st;  // sinh(u_pt + t) - sinh(u_pt)
-            s = sinhu + ds;
-            c = coshu + coshu * cm1 + sinhu * st;
-            Ds = ds * (s + sinhu);
-            KE = Ds * K + EC;
-        } else {  // far from the point the direct form has no cancellation
-            const float u = (float)u_pt + t;
-            s = sinhf(u);
-            c = coshf(u);
-            Ds = s * s - shu2;
-            KE = s * s * K + C0;
-        }
-        const float s2 = s * s, cv2 = swp * swp;
-        const float dc2 = -cv2 * sv2 * Ds / ((s2 + cv2) * (shu2 + cv2));
-        const float dphi = pot_dphi_f(P, Delta * s * sinv, Delta * c * cosv, rpt, c2pt, D2 * Ds, dc2, Phipt);
-        const float lz = Lt > 0.f ? Lt * Ds / (s2 * shu2) : 0.f;
-        return KE + lz - (s2 + sv2) * dphi;
-    }
-    // dU/du for the bracket's slope tests (uvOrb.cpp:54-61); E - Phi = K - (Phi - Phi_pt)
-    FJ_HD float duturnfn(float u) const
-    {
-        const float shu = sinhf(u), chu = coshf(u), s2 = shu * shu;
-        const float sv = sqrtf(sv2), cv = cosv < 0.f ? -swp : swp;
-        float phi0, f0, f1;
-        pot_grad_f(P, Delta * shu * sinv, Delta * chu * cosv, phi0, f0, f1);
-        const float dPhidu = Delta * (f0 * chu * sv + f1 * shu * cv);
-        return 2.f * (K - (phi0 - Phipt)) * shu * chu - (s2 + sv2) * dPhidu + 2.f * Lt * chu / (s2 * shu);
-    }
-    FJ_HD float vturn_w(float w) const
-    {
-        float sw, cw;
-        sincosf(w, &sw, &cw);
-        const float Dv = (swp - sw) * (swp + sw), s2 = cw * cw, sw2 = sw * sw;
-        const float dc2 = -(1.f + shu2) * shu2 * Dv / ((shu2 + sw2) * (shu2 + swp * swp));
-        const float dphi = pot_dphi_f(P, Delta * sinhu * cw, Delta * coshu * sw, rpt, c2pt, -D2 * Dv, dc2, Phipt);
-        const float lz = Lt > 0.f ? Lt / (sv2 * s2) : 0.f;
-        return Dv * (K + lz) + pvterm - (shu2 + s2) * dphi;
-    }
-    // the same function of v itself, for orbits reaching the pole
-    FJ_HD float vturn_v(float v) const
-    {
-        float sn, cs;
-        sincosf(v, &sn, &cs);
-        const float s2 = sn * sn;
-        const float Dv = (sn - svp) * (sn + svp);  // sin^2 v - sin^2 v_pt
-        const float dc2 = -(1.f + shu2) * shu2 * Dv / ((shu2 + cs * cs) * (shu2 + swp * swp));
-        const float dphi = pot_dphi_f(P, Delta * sinhu * sn, Delta * coshu * cs, rpt, c2pt, -D2 * Dv, dc2, Phipt);
-        const float lz = Lt > 0.f ? Lt / (sv2 * s2) : 0.f;
-        return Dv * (K + lz) + pvterm - (shu2 + s2) * dphi;
-    }
 };
 
-struct UturnTf { const FudgeF *o; FJ_HD float operator()(float t) const { return o->uturn_t(t); } };
-struct VturnWf { const FudgeF *o; FJ_HD float operator()(float w) const { return o->vturn_w(w); } };
-struct VturnVf { const FudgeF *o; FJ_HD float operator()(float v) const { return o->vturn_v(v); } };
-// Ju integrand (uvOrb.cpp:226-239): u = ubar - Deltau cos(psi)
-struct JuIntFf {
-    const FudgeF *o;
-    FJ_HD float operator()(float psi) const
-    {
+// What fudge_eval evaluates at x: the u-equation U(t), the v-equation V(w) or
+// V(v), and the momentum integrands of Ju (uvOrb.cpp:226-239, u = ubar -
+// Deltau cos psi) and Jv (uvOrb.cpp:247-257, v = pi/2 - (pi/2 - vturn) cos psi).
+enum : int { kEvU = 0, kEvVw = 1, kEvVv = 2, kEvJu = 3, kEvJv = 4 };
+
+// The one evaluator of every FP32 turning-point search and momentum
+// integral: the position on the coordinate line and the exact geometry
+// differences, a single pot_dphi_f, then U or V as A + B dPhi.  Kept out of
+// line, so Brent, the bracket walks and QAGS each exist once in the binary
+// and the divergent warps' working set fits the instruction cache.
+FJ_HDNI float fudge_eval(const FudgeF &o, int mode, float x)
+{
+    float fac = 1.f;
+    int m = mode;
+    if (mode >= kEvJu) {
         float sn, cs;
-        sincosf(psi, &sn, &cs);
-        return sqrtf(fmaxf(0.f, o->uturn_t(o->tb - o->Dt * cs))) * sn;
+        sincosf(x, &sn, &cs);
+        fac = sn;
+        if (mode == kEvJu) { x = o.tb - o.Dt * cs; m = kEvU; }
+        else {
+            const float w = o.wt * cs;
+            if (w <= .5f * kPIHf) { x = w; m = kEvVw; }
+            else { x = kPIHf - w; m = kEvVv; }
+        }
     }
-};
-// Jv integrand (uvOrb.cpp:247-257): v = pi/2 - (pi/2 - vturn) cos(psi)
-struct JvIntFf {
+    float R, z, dr2, dc2, A, Bc;
+    if (m == kEvU) {
+        float s, c, Ds, KE;
+        if (fabsf(x) < .5f) {  // offsets: no cancellation for |t| < 1/2
+            const float st = sinhf(x), h = sinhf(.5f * x), cm1 = 2.f * h * h;
+            const float ds = o.sinhu * cm1 + o.coshu * st;  // sinh(u_pt + t) - sinh(u_pt)
+            s = o.sinhu + ds;
+            c = o.coshu + o.coshu * cm1 + o.sinhu * st;
+            Ds = ds * (s + o.sinhu);
+            KE = Ds * o.K + o.EC;
+        } else {  // far from the point the direct form has no cancellation
+            const float u = (float)o.u_pt + x;
+            s = sinhf(u);
+            c = coshf(u);
+            Ds = s * s - o.shu2;
+            KE = s * s * o.K + o.C0;
+        }
+        const float s2 = s * s, cv2 = o.swp * o.swp;
+        R = o.Delta * s * o.sinv;
+        z = o.Delta * c * o.cosv;
+        dr2 = o.D2 * Ds;
+        dc2 = -cv2 * o.sv2 * Ds / ((s2 + cv2) * (o.shu2 + cv2));
+        A = KE + (o.Lt > 0.f ? o.Lt * Ds / (s2 * o.shu2) : 0.f);
+        Bc = -(s2 + o.sv2);
+    } else {
+        float sn, cs, Dv;
+        sincosf(x, &sn, &cs);
+        if (m == kEvVw) {  // x = w: sin v = cos w, cos v = sin w
+            Dv = (o.swp - sn) * (o.swp + sn);  // cos^2 v_pt - sin^2 w
+            const float t_ = sn; sn = cs; cs = t_;
+        } else {
+            Dv = (sn - o.svp) * (sn + o.svp);  // sin^2 v - sin^2 v_pt
+        }
+        const float s2 = sn * sn;
+        R = o.Delta * o.sinhu * sn;
+        z = o.Delta * o.coshu * cs;
+        dr2 = -o.D2 * Dv;
+        dc2 = -(1.f + o.shu2) * o.shu2 * Dv / ((o.shu2 + cs * cs) * (o.shu2 + o.swp * o.swp));
+        A = Dv * (o.K + (o.Lt > 0.f ? o.Lt / (o.sv2 * s2) : 0.f)) + o.pvterm;
+        Bc = -(o.shu2 + s2);
+    }
+    const float dphi = pot_dphi_f(o.P, R, z, o.rpt, o.c2pt, dr2, dc2, o.Phipt);
+    const float val = A + Bc * dphi;
+    return mode >= kEvJu ? sqrtf(fmaxf(0.f, val)) * fac : val;
+}
+
+// dU/du for the bracket's slope tests (uvOrb.cpp:54-61); E - Phi = K - (Phi - Phi_pt)
+FJ_HDNI float fudge_du(const FudgeF &o, float u)
+{
+    const float shu = sinhf(u), chu = coshf(u), s2 = shu * shu;
+    const float sv = sqrtf(o.sv2), cv = o.cosv < 0.f ? -o.swp : o.swp;
+    float phi0, f0, f1;
+    pot_grad_f(o.P, o.Delta * shu * o.sinv, o.Delta * chu * o.cosv, phi0, f0, f1);
+    const float dPhidu = o.Delta * (f0 * chu * sv + f1 * shu * cv);
+    return 2.f * (o.K - (phi0 - o.Phipt)) * shu * chu - (s2 + o.sv2) * dPhidu + 2.f * o.Lt * chu / (s2 * shu);
+}
+
+// fudge_eval as a functor of x for Brent and QAGS (one type, one instance each)
+struct FudgeFn {
     const FudgeF *o;
-    FJ_HD float operator()(float psi) const
-    {
-        float sn, cs;
-        sincosf(psi, &sn, &cs);
-        const float w = o->wt * cs;
-        const float V = w <= .5f * kPIHf ? o->vturn_w(w) : o->vturn_v(kPIHf - w);
-        return sqrtf(fmaxf(0.f, V)) * sn;
-    }
+    int mode;
+    FJ_HD float operator()(float x) const { return fudge_eval(*o, mode, x); }
 };
 
 // uvOrb::GetTurnu (uvOrb.cpp:131-201): the bracket walk in FP64 positions
@@ -695,13 +703,13 @@ struct JvIntFf {
 // redoes the u solve in FP64.
 FJ_HDNI bool get_turn_u_f(FudgeF &o, double utry, float &tin, float &tout, unsigned &fail)
 {
-    UturnTf U{&o};
+    const FudgeFn U{&o, kEvU};
     const double u0 = o.u_pt;
     double u1 = utry, u2 = utry, uin = utry, uout = utry, eps = .1;
-    float ut = U((float)(utry - u0)), dut = o.duturnfn((float)utry);
+    float ut = U((float)(utry - u0)), dut = fudge_du(o, (float)utry);
     int it = 0;
 #define FJ_STEP_U(x) { ut = U((float)((x) - u0)); if (++it > kLoopCap || !isfinite(ut)) return false; }
-#define FJ_STEP_UD(x) { ut = U((float)((x) - u0)); dut = o.duturnfn((float)(x)); \
+#define FJ_STEP_UD(x) { ut = U((float)((x) - u0)); dut = fudge_du(o, (float)(x)); \
                         if (++it > kLoopCap || !isfinite(ut)) return false; }
     if (!isfinite(ut)) return false;
     if (ut < 0) {
@@ -752,8 +760,8 @@ FJ_HDNI bool get_turn_v_f(FudgeF &o, float &wturn, unsigned &fail)
 {
     const float q = .5f * kPIHf;  // vtry = pi/4
     int it = 0;
-    if (o.vturn_w(q) < 0) {
-        VturnWf V{&o};
+    if (fudge_eval(o, kEvVw, q) < 0) {
+        const FudgeFn V{&o, kEvVw};
         float wbot = q;
         while (V(wbot) < 0) {
             wbot *= .5f;
@@ -762,7 +770,7 @@ FJ_HDNI bool get_turn_v_f(FudgeF &o, float &wturn, unsigned &fail)
         }
         fail |= brent_root_f(V, q, wbot, wturn);
     } else {
-        VturnVf V{&o};
+        const FudgeFn V{&o, kEvVv};
         float vtop = q;
         while (V(vtop) > 0) {
             vtop *= .5f;
@@ -895,7 +903,7 @@ FJ_HDNI double mixed_node_df(const PotView &P, const PotViewF &PF, const GK21f &
         else {
             o.tb = .5f * (tin + tout);
             o.Dt = .5f * (tout - tin);
-            JuIntFf fju{&o};
+            const FudgeFn fju{&o, kEvJu};
             Jr = (double)(rtwo * o.Delta * o.Dt * qags_f(fju, K, 0.f, kPIf, 1e-5f, 1e-3f, fail) / kPIf);
         }
         float wt;
@@ -909,7 +917,7 @@ FJ_HDNI double mixed_node_df(const PotView &P, const PotViewF &PF, const GK21f &
         if (wt < 1e-12f) Jz = 0;
         else {
             o.wt = wt;
-            JvIntFf fjv{&o};
+            const FudgeFn fjv{&o, kEvJv};
             Jz = (double)(2.f * rtwo * o.Delta * wt * qags_f(fjv, K, 0.f, kPIHf, 1e-5f, 1e-3f, fail) / kPIf);
         }
     }

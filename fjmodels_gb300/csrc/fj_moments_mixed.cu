@@ -13,26 +13,27 @@
 
 namespace fj {
 
-// Work layout: a block takes one contiguous range of at most kMixedMaxNodes
+// Work layout: a block takes one contiguous range of at most a.mixed_chunk
 // nodes of one point (mixed_blocks_per_point blocks per point), compacts the
 // bound ones (H < 0; about 40% of the cube) into a shared-memory list in node
 // order, and its threads take the list round-robin.  So no lane idles on an
 // unbound node, each thread's nodes are summed in a fixed order, and the
 // per-block sums are added in a fixed order by k_moments_finalize.
-constexpr int kMixedBlock = 128;
-constexpr int kMixedMaxNodes = 8192;
-
-int mixed_blocks_per_point(long long nq3) { return (int)((nq3 + kMixedMaxNodes - 1) / kMixedMaxNodes); }
+// The kernel is built in kMixedVariants register budgets (launch bounds of
+// 3, 4, 6 and 8 resident blocks per SM: 168, 128, 80 and 64 registers);
+// which one, and the chunk size, is a per-context setting (fj_autotune_mixed).
+int mixed_blocks_per_point(long long nq3, int chunk) { return (int)((nq3 + chunk - 1) / chunk); }
 
 size_t moment_mixed_smem_bytes(const MomentArgs &a)
 {
     const size_t nt = (size_t)a.P.nr * a.P.npoly;
     return (a.P.nr + 3 * nt + 2 * a.ngrid + 2 * a.nq + 6 * (kMixedBlock / 32) + 4) * sizeof(double) +
            (2 * a.P.nr + 2 * nt + 4 * kQuadIntervals) * sizeof(float) + sizeof(GK21f) + 16 +
-           (kMixedBlock / 32) * sizeof(int) + kMixedMaxNodes * sizeof(unsigned short);
+           (kMixedBlock / 32) * sizeof(int) + (size_t)a.mixed_chunk * sizeof(unsigned short);
 }
 
-__global__ void __launch_bounds__(kMixedBlock) k_moments_mixed(MomentArgs a)
+template <int MINB>
+__global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs a)
 {
     extern __shared__ double sm[];
     const int nr = a.P.nr, npoly = a.P.npoly, nt = nr * npoly;
@@ -155,24 +156,49 @@ __global__ void __launch_bounds__(kMixedBlock) k_moments_mixed(MomentArgs a)
     if (lane == 0 && ne) atomicAdd(&a.counters[3], (unsigned long long)ne);
 }
 
-cudaError_t launch_moments_mixed(const MomentArgs &a, cudaStream_t s)
+namespace {
+template <int MINB>
+cudaError_t launch_variant(const MomentArgs &a, size_t smem, cudaStream_t s)
 {
-    const size_t smem = moment_mixed_smem_bytes(a);
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_moments_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(k_moments_mixed<MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     const long long nblocks = (long long)a.npts * a.blocks_per_point;
-    k_moments_mixed<<<(unsigned)nblocks, kMixedBlock, smem, s>>>(a);
-    cudaError_t e = cudaGetLastError();
+    k_moments_mixed<MINB><<<(unsigned)nblocks, kMixedBlock, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <int MINB>
+size_t local_bytes()
+{
+    cudaFuncAttributes at;
+    return cudaFuncGetAttributes(&at, k_moments_mixed<MINB>) == cudaSuccess ? at.localSizeBytes : 0;
+}
+}  // namespace
+
+cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, cudaStream_t s)
+{
+    if (a.mixed_chunk < kMixedBlock || a.mixed_chunk > kMixedMaxNodes) return cudaErrorInvalidValue;
+    const size_t smem = moment_mixed_smem_bytes(a);
+    cudaError_t e;
+    switch (variant) {
+    case 0: e = launch_variant<3>(a, smem, s); break;
+    case 1: e = launch_variant<4>(a, smem, s); break;
+    case 2: e = launch_variant<6>(a, smem, s); break;
+    case 3: e = launch_variant<8>(a, smem, s); break;
+    default: return cudaErrorInvalidValue;
+    }
     if (e != cudaSuccess) return e;
     return launch_moments_finalize(a, s);
 }
 
 size_t moments_mixed_local_bytes()
 {
-    cudaFuncAttributes at;
-    return cudaFuncGetAttributes(&at, k_moments_mixed) == cudaSuccess ? at.localSizeBytes : 0;
+    size_t m = local_bytes<3>();
+    const size_t v[3] = {local_bytes<4>(), local_bytes<6>(), local_bytes<8>()};
+    for (size_t x : v) m = x > m ? x : m;
+    return m;
 }
 
 }  // namespace fj

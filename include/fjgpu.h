@@ -131,6 +131,20 @@ int fj_moments_points(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table
                       const fj_df_params *df, const fj_quad_rule *rule, const double *Rz, int npts,
                       double *out6, fj_moment_stats *stats);
 
+/* Configuration of the mixed-precision phase-space kernel (no reference
+   counterpart: the reference has one CPU loop).  variant 0..3 = register
+   budget of the build (launch bounds of 3, 4, 6, 8 resident blocks per SM),
+   nodes_per_block = velocity nodes of one point per block (128..8192).
+   fj_autotune_mixed times every variant x {2048, 4096, 8192} with
+   fj_moments_points on the given device sample points (out6 device
+   [6][npts] scratch), keeps the fastest in the context and returns its
+   kernel time; results are the same in every configuration up to the
+   summation order of the per-thread sums. */
+int fj_set_mixed_config(fj_ctx *ctx, int variant, int nodes_per_block);
+int fj_get_mixed_config(fj_ctx *ctx, int *variant, int *nodes_per_block);
+int fj_autotune_mixed(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
+                      const fj_quad_rule *rule, const double *Rz, int npts, double *out6, double *best_ms);
+
 /* rho[0][0] extrapolation (pot/potLeg.cpp:68) and the 6-field Legendre
    projection get_Ylm (include/UtilsLeg.h:200-253).  grids6 device
    [6][nr*ngauss] (read only), coef6 device [6][nr*npoly] = rhl, vrotl, sigRl,

@@ -150,3 +150,32 @@ def test_mixed_rejects_unsupported(ctx):
         ctx.moments_points(pot, delta, F.DFParams("Hernquist"), F.Rule(jquad=8, precision=A.FJ_PREC_MIXED), M, out)
     with pytest.raises(F.FJError, match="precision"):
         ctx.moments_points(pot, delta, F.DFParams("Hernquist"), F.Rule(precision=7), M, out)
+
+
+def test_mixed_configurations_agree(ctx):
+    """Every register budget and node range of the mixed kernel gives the same moments up to
+    the summation order (relative 1e-12), the autotuner keeps one of them, and out-of-range
+    settings are argument errors."""
+    (ar, phil, Pr, Pr2, E, D), M, df = _nfw_80(None)
+    pot = ctx.potential(dev(ar), dev(phil), dev(Pr), dev(Pr2))
+    delta = ctx.delta(dev(E), dev(D))
+    rule = F.Rule(*F.tanh_sinh_rule(22), precision=A.FJ_PREC_MIXED)
+    Mt = dev(M[::3])
+    saved = ctx.mixed_config()
+    outs = []
+    try:
+        for v in range(4):
+            for c in (128, 2048, 8192):
+                ctx.set_mixed_config(v, c)
+                out = torch.zeros((6, Mt.shape[0]), dtype=torch.float64, device="cuda")
+                ctx.moments_points(pot, delta, df, rule, Mt, out)
+                outs.append(host(out))
+        for o in outs[1:]:
+            assert rel(o[[0, 2, 3, 4]], outs[0][[0, 2, 3, 4]]) < 1e-12
+        v, c, ms = ctx.autotune_mixed(pot, delta, df, rule, Mt)
+        assert 0 <= v < 4 and c in (2048, 4096, 8192) and ms > 0
+        for bad in ((4, 2048), (0, 64), (0, 8193)):
+            with pytest.raises(F.FJError, match="set_mixed_config"):
+                ctx.set_mixed_config(*bad)
+    finally:
+        ctx.set_mixed_config(*saved)

@@ -32,7 +32,10 @@ def rel_shells(a, ref):
     ref = np.asarray(ref)
     a = np.asarray(a).reshape(ref.shape)
     scale = np.abs(ref[:, :1]) + 1e-10 * np.abs(ref[0, 0])
-    return float(np.max(np.abs(a - ref) / scale))
+    r = np.abs(a - ref) / scale
+    i = np.unravel_index(np.argmax(r), r.shape)
+    print(f"rel_shells max {r[i]:.3e} at shell {i[0]} coefficient {i[1]}: {a[i]!r} vs {ref[i]!r}")
+    return float(r[i])
 
 
 def dev(a):
