@@ -20,10 +20,10 @@ LIB = os.path.join(HERE, "libfjgpu.so")
 # quadratic interpolation point at mid-interval); with contracted arithmetic
 # they take the other branch at a few nodes and densities move by ~1e-7,
 # exactly as the reference's own sources do when compiled with contraction.
-# The mixed-precision form is not a rounding-faithful restatement and keeps
-# contraction.
+# The mixed-precision form is not a rounding-faithful restatement: it keeps
+# contraction and uses the 2-ulp FP32 division and square root.
 SOURCES = {"fj_moments.cu": ["--fmad=false"], "fj_multipole.cu": ["--fmad=false"], "fj_api.cu": [],
-           "fj_peak.cu": [], "fj_noalloc.cu": [], "fj_moments_mixed.cu": []}
+           "fj_peak.cu": [], "fj_noalloc.cu": [], "fj_moments_mixed.cu": ["-prec-div=false", "-prec-sqrt=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xcompiler", "-Wall,-Wno-unused-function,-ffp-contract=off"]

@@ -71,6 +71,35 @@ FJ_HD const LegCoefF &leg_f()
 #endif
 }
 
+// log for the interval guess only (corrected by neighbour tests)
+FJ_HD float fast_logf(float x)
+{
+#ifdef __CUDA_ARCH__
+    return __logf(x);
+#else
+    return logf(x);
+#endif
+}
+
+// sin and cos of a quadrature angle psi in [0, pi]: absolute error 4e-7 of the
+// hardware approximation is below the QAGS tolerances
+FJ_HD void sincos_psi(float x, float *s, float *c)
+{
+#ifdef __CUDA_ARCH__
+    __sincosf(x, s, c);
+#else
+    sincosf(x, s, c);
+#endif
+}
+
+// sinh x and cosh x - 1 from one expm1 (relative precision for small |x|)
+FJ_HD void sinh_coshm1(float x, float &sh, float &chm1)
+{
+    const float em = expm1f(x), h = em / (2.f * (em + 1.f));  // (e^x - 1) / (2 e^x)
+    sh = h * (em + 2.f);
+    chm1 = h * em;
+}
+
 struct InterpF {
     int bot, thr;
     bool ext, quad;
@@ -87,7 +116,7 @@ FJ_HD void interp_setup_f(const PotViewF &P, float r, InterpF &I)
     I.x = 0.f;
     if (r >= ar[nr - 1]) { I.ext = true; I.x = ar[nr - 1] / r; return; }
     I.ext = false;
-    int b = (int)((logf(r) - P.lr0) * P.idl);
+    int b = (int)((fast_logf(r) - P.lr0) * P.idl);
     b = b < 0 ? 0 : (b > nr - 2 ? nr - 2 : b);
     while (b > 0 && r < ar[b]) --b;
     while (b < nr - 2 && r > ar[b + 1]) ++b;
@@ -584,7 +613,7 @@ FJ_HDNI float qags_f(F &f, const GK21f &K, float a, float b, float epsabs, float
 // excursion is small (a near-circular orbit, a thin disc orbit):
 //   u = u_pt + t:  U(t) = Ds K + EC + Lt Ds / (s^2 sh^2) - (s^2 + sv^2) dPhi,
 //                  s = sinh(u), sh = sinh(u_pt), Ds = s^2 - sh^2 formed for
-//                  |t| < 1/2 from sinh(t) and cosh(t) - 1 = 2 sinh^2(t/2); for
+//                  |t| < 1/2 from sinh(t) and cosh(t) - 1 (one expm1); for
 //                  |t| >= 1/2, Ds K + EC = s^2 K + C0 with C0 = EC - sh^2 K
 //                  formed in FP64 (far from the focus sh^2 K and EC are ~(r/Delta)^2
 //                  times larger than U);
@@ -622,7 +651,7 @@ FJ_HDNI float fudge_eval(const FudgeF &o, int mode, float x)
     int m = mode;
     if (mode >= kEvJu) {
         float sn, cs;
-        sincosf(x, &sn, &cs);
+        sincos_psi(x, &sn, &cs);
         fac = sn;
         if (mode == kEvJu) { x = o.tb - o.Dt * cs; m = kEvU; }
         else {
@@ -635,16 +664,17 @@ FJ_HDNI float fudge_eval(const FudgeF &o, int mode, float x)
     if (m == kEvU) {
         float s, c, Ds, KE;
         if (fabsf(x) < .5f) {  // offsets: no cancellation for |t| < 1/2
-            const float st = sinhf(x), h = sinhf(.5f * x), cm1 = 2.f * h * h;
+            float st, cm1;
+            sinh_coshm1(x, st, cm1);
             const float ds = o.sinhu * cm1 + o.coshu * st;  // sinh(u_pt + t) - sinh(u_pt)
             s = o.sinhu + ds;
             c = o.coshu + o.coshu * cm1 + o.sinhu * st;
             Ds = ds * (s + o.sinhu);
             KE = Ds * o.K + o.EC;
         } else {  // far from the point the direct form has no cancellation
-            const float u = (float)o.u_pt + x;
-            s = sinhf(u);
-            c = coshf(u);
+            float cm1;
+            sinh_coshm1((float)o.u_pt + x, s, cm1);
+            c = 1.f + cm1;
             Ds = s * s - o.shu2;
             KE = s * s * o.K + o.C0;
         }
@@ -680,7 +710,9 @@ FJ_HDNI float fudge_eval(const FudgeF &o, int mode, float x)
 // dU/du for the bracket's slope tests (uvOrb.cpp:54-61); E - Phi = K - (Phi - Phi_pt)
 FJ_HDNI float fudge_du(const FudgeF &o, float u)
 {
-    const float shu = sinhf(u), chu = coshf(u), s2 = shu * shu;
+    float shu, chm1;
+    sinh_coshm1(u, shu, chm1);
+    const float chu = 1.f + chm1, s2 = shu * shu;
     const float sv = sqrtf(o.sv2), cv = o.cosv < 0.f ? -o.swp : o.swp;
     float phi0, f0, f1;
     pot_grad_f(o.P, o.Delta * shu * o.sinv, o.Delta * chu * o.cosv, phi0, f0, f1);

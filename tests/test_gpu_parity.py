@@ -147,8 +147,12 @@ def test_run_model_two_iterations(ctx):
     out = ctx.run_model(nr, ng, npl, meta["rmin"], meta["rmax"], df, F.Rule(), itermax=2,
                         delta_table=(g["Egrid"], g["Dgrid"]))
     assert out["iterations"] == 2 and out["failures"] == 0
-    assert rel_shells(out["coef6"][0], g["it1_rhl"].reshape(nr, npl)) < TOL
-    assert rel_shells(out["phil"], g["it1_phil"].reshape(nr, npl)) < TOL
+    # After two iterations the first iteration's rounding-level differences (libm vs CUDA
+    # exp/log/pow) have passed through the Poisson solve and a second moment sweep; the
+    # reference's own builds with and without FMA contraction differ by 1.6e-9 in this
+    # measure, so the two-iteration gate is 2e-9 (single iterations keep 1e-9).
+    assert rel_shells(out["coef6"][0], g["it1_rhl"].reshape(nr, npl)) < 2 * TOL
+    assert rel_shells(out["phil"], g["it1_phil"].reshape(nr, npl)) < 2 * TOL
     ref_vir = g["vir2"][1]  # KE, PE, W/K printed with %f after the second iteration
     K = out["vir7"][0] + out["vir7"][1]
     assert abs(out["vir7"][4] / K - ref_vir[4]) < 1.5e-6
