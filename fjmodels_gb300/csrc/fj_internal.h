@@ -42,7 +42,7 @@ cudaError_t launch_moments_finalize(const MomentArgs &a, cudaStream_t s);
 // integrals); counters[3] gets the nodes whose turning points ran in FP64
 constexpr int kMixedBlock = 128;     // threads per block of the mixed kernel
 constexpr int kMixedMaxNodes = 8192; // largest node range of one block (shared-memory list)
-constexpr int kMixedVariants = 4;    // register budgets the mixed kernel is built in
+constexpr int kMixedVariants = 8;    // builds of the mixed kernel (2 forms x 4 register budgets)
 size_t moment_mixed_smem_bytes(const MomentArgs &a);
 int mixed_blocks_per_point(long long nq3, int chunk);
 cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, cudaStream_t s);

@@ -9,7 +9,7 @@
 #include <cstdint>
 
 #include "fj_internal.h"
-#include "fj_mixed.cuh"
+#include "fj_mixed_wave.cuh"
 
 namespace fj {
 
@@ -19,9 +19,12 @@ namespace fj {
 // order, and its threads take the list round-robin.  So no lane idles on an
 // unbound node, each thread's nodes are summed in a fixed order, and the
 // per-block sums are added in a fixed order by k_moments_finalize.
-// The kernel is built in kMixedVariants register budgets (launch bounds of
-// 3, 4, 6 and 8 resident blocks per SM: 168, 128, 80 and 64 registers);
-// which one, and the chunk size, is a per-context setting (fj_autotune_mixed).
+// The kernel is built in two forms -- each thread running its nodes' solves
+// as nested loops (mixed_node_df), or the wavefront form (MixedLane: every
+// lane's next potential difference evaluated at one call site per step) --
+// and each in four register budgets (launch bounds of 3, 4, 6 and 8 resident
+// blocks per SM: 168, 128, 80 and 64 registers): kMixedVariants builds.
+// Which one, and the chunk size, is a per-context setting (fj_autotune_mixed).
 int mixed_blocks_per_point(long long nq3, int chunk) { return (int)((nq3 + chunk - 1) / chunk); }
 
 size_t moment_mixed_smem_bytes(const MomentArgs &a)
@@ -32,7 +35,7 @@ size_t moment_mixed_smem_bytes(const MomentArgs &a)
            (kMixedBlock / 32) * sizeof(int) + (size_t)a.mixed_chunk * sizeof(unsigned short);
 }
 
-template <int MINB>
+template <int MINB, bool WAVE>
 __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs a)
 {
     extern __shared__ double sm[];
@@ -108,6 +111,50 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
 
     double m[6] = {0, 0, 0, 0, 0, 0};
     unsigned failed = 0, esc = 0;
+    if (WAVE) {
+        // wavefront form: each step every active lane evaluates its pending request at
+        // the one call site below; a lane that completes a node takes its next one
+        MixedLane L;
+        int q = threadIdx.x;
+        double V0 = 0, V1 = 0, V2 = 0, wj = 0;
+        bool active = false;
+        auto accumulate = [&]() {
+            failed += L.fail ? 1u : 0u;
+            esc += L.esc;
+            const double DF = (L.fail & (kFailBracket | kFailRoot)) ? 0. : L.df(a.df);
+            const double jd = wj * (jacob * DF);
+            m[0] += jd;
+            m[1] += jd * V1;
+            m[2] += jd * V0 * V0;
+            m[3] += jd * V1 * V1;
+            m[4] += jd * V2 * V2;
+            m[5] += jd * V0 * V2;
+        };
+        auto next = [&]() {  // the lane's next node with a pending request, or none
+            while (q < nbound) {
+                const int node = n0 + s_list[q];
+                q += kMixedBlock;
+                const int i = node / nq2, j = (node / nq) % nq, k = node % nq;
+                V0 = 1e-6 + Ve * s_xq[i]; V1 = 1e-6 + Ve * s_xq[j]; V2 = 1e-6 + Ve * s_xq[k];
+                wj = s_wq[i] * s_wq[j] * s_wq[k];
+                const double H = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h;
+                if (L.begin(PF, deltafn(s_Eg, s_Dg, a.ngrid, H), R, z, Phi_h, V0, V1, V2)) return true;
+                accumulate();  // E >= 0 after rounding: Jr = Jz = 1e31
+            }
+            return false;
+        };
+        active = next();
+        while (__any_sync(0xffffffffu, active)) {
+            if (active) {
+                const float val = fudge_eval(L.o, L.mode, L.x);
+                const float dval = L.want_du ? fudge_du(L.o, L.xdu) : 0.f;
+                if (L.feed(P, *sK, val, dval)) {
+                    accumulate();
+                    active = next();
+                }
+            }
+        }
+    } else
     for (int q = threadIdx.x; q < nbound; q += kMixedBlock) {
         const int node = n0 + s_list[q];
         const int i = node / nq2, j = (node / nq) % nq, k = node % nq;
@@ -157,23 +204,24 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
 }
 
 namespace {
-template <int MINB>
+template <int MINB, bool WAVE>
 cudaError_t launch_variant(const MomentArgs &a, size_t smem, cudaStream_t s)
 {
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_moments_mixed<MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = cudaFuncSetAttribute(k_moments_mixed<MINB, WAVE>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     const long long nblocks = (long long)a.npts * a.blocks_per_point;
-    k_moments_mixed<MINB><<<(unsigned)nblocks, kMixedBlock, smem, s>>>(a);
+    k_moments_mixed<MINB, WAVE><<<(unsigned)nblocks, kMixedBlock, smem, s>>>(a);
     return cudaGetLastError();
 }
 
-template <int MINB>
+template <int MINB, bool WAVE>
 size_t local_bytes()
 {
     cudaFuncAttributes at;
-    return cudaFuncGetAttributes(&at, k_moments_mixed<MINB>) == cudaSuccess ? at.localSizeBytes : 0;
+    return cudaFuncGetAttributes(&at, k_moments_mixed<MINB, WAVE>) == cudaSuccess ? at.localSizeBytes : 0;
 }
 }  // namespace
 
@@ -183,10 +231,14 @@ cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, cudaStream_t 
     const size_t smem = moment_mixed_smem_bytes(a);
     cudaError_t e;
     switch (variant) {
-    case 0: e = launch_variant<3>(a, smem, s); break;
-    case 1: e = launch_variant<4>(a, smem, s); break;
-    case 2: e = launch_variant<6>(a, smem, s); break;
-    case 3: e = launch_variant<8>(a, smem, s); break;
+    case 0: e = launch_variant<3, false>(a, smem, s); break;
+    case 1: e = launch_variant<4, false>(a, smem, s); break;
+    case 2: e = launch_variant<6, false>(a, smem, s); break;
+    case 3: e = launch_variant<8, false>(a, smem, s); break;
+    case 4: e = launch_variant<3, true>(a, smem, s); break;
+    case 5: e = launch_variant<4, true>(a, smem, s); break;
+    case 6: e = launch_variant<6, true>(a, smem, s); break;
+    case 7: e = launch_variant<8, true>(a, smem, s); break;
     default: return cudaErrorInvalidValue;
     }
     if (e != cudaSuccess) return e;
@@ -195,8 +247,10 @@ cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, cudaStream_t 
 
 size_t moments_mixed_local_bytes()
 {
-    size_t m = local_bytes<3>();
-    const size_t v[3] = {local_bytes<4>(), local_bytes<6>(), local_bytes<8>()};
+    const size_t v[kMixedVariants] = {local_bytes<3, false>(), local_bytes<4, false>(), local_bytes<6, false>(),
+                                      local_bytes<8, false>(), local_bytes<3, true>(), local_bytes<4, true>(),
+                                      local_bytes<6, true>(), local_bytes<8, true>()};
+    size_t m = 0;
     for (size_t x : v) m = x > m ? x : m;
     return m;
 }

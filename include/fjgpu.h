@@ -132,8 +132,11 @@ int fj_moments_points(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table
                       double *out6, fj_moment_stats *stats);
 
 /* Configuration of the mixed-precision phase-space kernel (no reference
-   counterpart: the reference has one CPU loop).  variant 0..3 = register
-   budget of the build (launch bounds of 3, 4, 6, 8 resident blocks per SM),
+   counterpart: the reference has one CPU loop).  variant 0..7: 0..3 run each
+   node's solve as nested loops, 4..7 in the wavefront form (all lanes of a
+   warp evaluate their next potential difference together); within each, the
+   register budget of the build (launch bounds of 3, 4, 6, 8 resident blocks
+   per SM),
    nodes_per_block = velocity nodes of one point per block (128..8192).
    fj_autotune_mixed times every variant x {2048, 4096, 8192} with
    fj_moments_points on the given device sample points (out6 device
