@@ -10,6 +10,7 @@ DP = C.POINTER(C.c_double)
 FJ_OK = 0
 FJ_DF_DPL, FJ_DF_QUASIISO = 0, 1
 FJ_PREC_FP64, FJ_PREC_MIXED = 0, 1
+FJ_TWOCOMP_SUMMED, FJ_TWOCOMP_REFERENCE = 0, 1
 FJ_JQUAD_QAGS = 0
 FJ_GUESS = {"Hernquist": 0, "Isochrone": 1, "NFW": 2}
 
@@ -42,14 +43,16 @@ class fj_model_config(C.Structure):
                 ("rmin", C.c_double), ("rmax", C.c_double), ("guess", C.c_int),
                 ("mass", C.c_double), ("r0", C.c_double), ("q", C.c_double),
                 ("df", fj_df_params), ("rule", fj_quad_rule), ("itermax", C.c_int), ("tol", C.c_double),
-                ("Egrid_in", DP), ("Dgrid_in", DP)]
+                ("Egrid_in", DP), ("Dgrid_in", DP), ("ncomp", C.c_int), ("guess2", C.c_int),
+                ("mass2", C.c_double), ("r0_2", C.c_double), ("q2", C.c_double), ("df2", fj_df_params),
+                ("twocomp_order", C.c_int)]
 
 
 class fj_model_result(C.Structure):
     _fields_ = [(n, DP) for n in ("ar", "coef6", "phil", "Pr", "Pr2", "Egrid", "Dgrid", "grids6")] + [
         ("vir7", C.c_double * 7), ("iterations", C.c_int), ("last_change", C.c_double),
         ("bound", C.c_longlong), ("failures", C.c_longlong), ("wall_ms", C.c_double), ("kernel_ms", C.c_double),
-        ("setup_ms", C.c_double)]
+        ("setup_ms", C.c_double), ("coef6_2", DP), ("vir7_2", C.c_double * 7)]
 
 
 P = C.POINTER
@@ -69,7 +72,7 @@ SIGNATURES = {
     "fj_set_mixed_config": ([CTX, C.c_int, C.c_int], C.c_int),
     "fj_get_mixed_config": ([CTX, P(C.c_int), P(C.c_int)], C.c_int),
     "fj_autotune_mixed": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule), C.c_void_p,
-                           C.c_int, C.c_void_p, DP], C.c_int),
+                           C.c_int, C.c_void_p, DP, DP], C.c_int),
     "fj_legendre_project": ([CTX, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "fj_poisson": ([CTX, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "fj_poisson_noalloc": ([C.c_int, C.c_int] + [C.c_void_p] * 6, C.c_int),

@@ -186,9 +186,10 @@ class Context:
         self._on_torch_stream()
         out = torch.zeros((6, Rz.shape[0]), dtype=torch.float64, device=Rz.device)
         ms = np.zeros(1)
+        self.autotune_table = np.zeros((8, 3))
         self._check(self.lib.fj_autotune_mixed(self.h, C.byref(pot.c), C.byref(delta.c), C.byref(df.c),
-                                               C.byref(rule.c), _ptr(Rz), Rz.shape[0], _ptr(out), _dp(ms)),
-                    "fj_autotune_mixed")
+                                               C.byref(rule.c), _ptr(Rz), Rz.shape[0], _ptr(out), _dp(ms),
+                                               _dp(self.autotune_table)), "fj_autotune_mixed")
         return (*self.mixed_config(), float(ms[0]))
 
     def legendre_project(self, nr, ngauss, npoly, ar, grids6, coef6):
@@ -234,20 +235,30 @@ class Context:
 
     # ---------------------------------------------------------------- whole model
     def run_model(self, nr, ngauss, npoly, rmin, rmax, df, rule, itermax, tol=0.0, ngrid=30, q=1.0,
-                  keep_grids=False, delta_table=None):
-        """One-component self-consistent model (fJmodels.cpp:86-144) with host buffers.
+                  keep_grids=False, delta_table=None, df2=None, q2=1.0, twocomp_order=A.FJ_TWOCOMP_SUMMED):
+        """Self-consistent model (oneComp, fJmodels.cpp:86-144; with df2, the two-component
+        loop of fJmodels.cpp:38-84 in `twocomp_order`) with host buffers.
         delta_table = (Egrid, Dgrid) uses a given focal-distance table instead of tabulating one."""
         self.use_own_stream()
         din = [None, None] if delta_table is None else [_f64(delta_table[0]), _f64(delta_table[1])]
         cfg = A.fj_model_config(nr, ngauss, npoly, ngrid, rmin, rmax, A.FJ_GUESS.get(df.model, 0), df.mass, df.r0,
                                 q, df.c, rule.c, itermax, tol, *[_dp(d) if d is not None else None for d in din])
+        if df2 is not None:
+            cfg.ncomp, cfg.guess2, cfg.mass2, cfg.r0_2, cfg.q2 = 2, A.FJ_GUESS.get(df2.model, 0), df2.mass, df2.r0, q2
+            cfg.df2 = df2.c
+            cfg.twocomp_order = twocomp_order
         out = {"ar": np.zeros(nr), "coef6": np.zeros((6, nr, npoly)), "phil": np.zeros((nr, npoly)),
                "Pr": np.zeros((nr, npoly)), "Pr2": np.zeros((nr, npoly)), "Egrid": np.zeros(ngrid),
                "Dgrid": np.zeros(ngrid)}
         grids = np.zeros((6, nr, ngauss)) if keep_grids else None
         res = A.fj_model_result(*[_dp(out[k]) for k in ("ar", "coef6", "phil", "Pr", "Pr2", "Egrid", "Dgrid")],
                                 _dp(grids) if keep_grids else None)
+        if df2 is not None:
+            out["coef6_2"] = np.zeros((6, nr, npoly))
+            res.coef6_2 = _dp(out["coef6_2"])
         self._check(self.lib.fj_run_model(self.h, C.byref(cfg), C.byref(res)), "fj_run_model")
+        if df2 is not None:
+            out["vir7_2"] = np.array(res.vir7_2[:])
         out.update(vir7=np.array(res.vir7[:]), iterations=res.iterations, last_change=res.last_change,
                    bound=res.bound, failures=res.failures, wall_ms=res.wall_ms, kernel_ms=res.kernel_ms,
                    setup_ms=res.setup_ms)

@@ -364,7 +364,8 @@ int fj_get_mixed_config(fj_ctx *ctx, int *variant, int *nodes_per_block)
 }
 
 int fj_autotune_mixed(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
-                      const fj_quad_rule *rule, const double *Rz, int npts, double *out6, double *best_ms)
+                      const fj_quad_rule *rule, const double *Rz, int npts, double *out6, double *best_ms,
+                      double *all_ms)
 {
     if (!ctx || !rule || rule->precision != FJ_PREC_MIXED || !Rz || npts < 1 || !out6)
         return fail(ctx, FJ_ERR_ARG, "autotune_mixed: needs a mixed-precision rule and sample points");
@@ -379,6 +380,7 @@ int fj_autotune_mixed(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table
             fj_moment_stats st;
             int rc = run_moments(ctx, pot, delta, df, rule, 0, Rz, npts, out6, &st);
             if (rc) { ctx->mixed_variant = v0; ctx->mixed_chunk = c0; return rc; }
+            if (all_ms) all_ms[v * 3 + (c == 2048 ? 0 : c == 4096 ? 1 : 2)] = st.kernel_ms;
             if (best < 0 || st.kernel_ms < best) { best = st.kernel_ms; bv = v; bc = c; }
         }
     ctx->mixed_variant = bv;
@@ -812,24 +814,41 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
     const int nr = cfg->nr, ng = cfg->ngauss, npl = cfg->npoly, ngrid = cfg->ngrid, nt = nr * npl;
     if (nr < 11 || ng < 1 || npl < 1 || npl > kMaxPoly || ngrid < 2 || cfg->itermax < 1)
         return fail(ctx, FJ_ERR_ARG, "run_model: bad sizes");
+    if (cfg->ncomp < 0 || cfg->ncomp > 2 ||
+        (cfg->ncomp == 2 && cfg->twocomp_order != FJ_TWOCOMP_SUMMED && cfg->twocomp_order != FJ_TWOCOMP_REFERENCE))
+        return fail(ctx, FJ_ERR_ARG, "run_model: ncomp must be 1 or 2 with a known two-component order");
+    const bool two = cfg->ncomp == 2;
+    const bool ref_order = two && cfg->twocomp_order == FJ_TWOCOMP_REFERENCE;
     auto t0 = std::chrono::steady_clock::now();
     int rc;
     if ((rc = fj_log_grid(cfg->rmin, cfg->rmax, nr, res->ar))) return fail(ctx, rc, "run_model: grid");
-    std::vector<double> rhl(nt);
+    std::vector<double> rhl(2 * (size_t)nt);
     if ((rc = fj_guess_rhl(nr, ng, npl, res->ar, cfg->guess, cfg->mass, cfg->r0, cfg->q, rhl.data())))
         return fail(ctx, rc, "run_model: guess");
-    // device layout: ar | rhl | pot A (3 tables) | pot B (3 tables) | Eg | Dg | grids6 | coef6
-    const size_t nd = nr + nt + 6 * (size_t)nt + 2 * ngrid + 6 * (size_t)nr * ng + 6 * (size_t)nt;
+    if (two && (rc = fj_guess_rhl(nr, ng, npl, res->ar, cfg->guess2, cfg->mass2, cfg->r0_2, cfg->q2, rhl.data() + nt)))
+        return fail(ctx, rc, "run_model: guess of component 2");
+    // device layout: ar | rhl (2) | pot A, B (total, 3 tables each) | pot C, D (components) | Eg | Dg |
+    // grids6 (2) | coef6 (2)
+    const size_t nd = nr + 2 * (size_t)nt + 12 * (size_t)nt + 2 * ngrid + 12 * (size_t)nr * ng + 12 * (size_t)nt;
     double *dbuf = nullptr;
     FJ_CUDA(cudaMalloc(&dbuf, nd * sizeof(double)));
     struct Free { double *p; ~Free() { cudaFree(p); } } guard{dbuf};
-    double *d_ar = dbuf, *d_rhl = d_ar + nr, *potA = d_rhl + nt, *potB = potA + 3 * nt, *d_Eg = potB + 3 * nt,
-           *d_Dg = d_Eg + ngrid, *d_grids = d_Dg + ngrid, *d_coef = d_grids + 6 * (size_t)nr * ng;
+    double *d_ar = dbuf, *d_rhl = d_ar + nr, *potA = d_rhl + 2 * nt, *potB = potA + 3 * nt, *potC = potB + 3 * nt,
+           *potD = potC + 3 * nt, *d_Eg = potD + 3 * nt, *d_Dg = d_Eg + ngrid, *d_grids = d_Dg + ngrid,
+           *d_grids2 = d_grids + 6 * (size_t)nr * ng, *d_coef = d_grids2 + 6 * (size_t)nr * ng,
+           *d_coef2 = d_coef + 6 * (size_t)nt;
     cudaStream_t s = ctx->stream;
     FJ_CUDA(cudaMemcpyAsync(d_ar, res->ar, nr * sizeof(double), cudaMemcpyHostToDevice, s));
-    FJ_CUDA(cudaMemcpyAsync(d_rhl, rhl.data(), nt * sizeof(double), cudaMemcpyHostToDevice, s));
-    if ((rc = fj_poisson(ctx, nr, npl, d_ar, d_rhl, potA, potA + nt, potA + 2 * nt))) return rc;
-    // focal-distance table from the guess potential (fJmodels.cpp:127)
+    FJ_CUDA(cudaMemcpyAsync(d_rhl, rhl.data(), 2 * nt * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (!two) {
+        if ((rc = fj_poisson(ctx, nr, npl, d_ar, d_rhl, potA, potA + nt, potA + 2 * nt))) return rc;
+    } else {  // each component's guess potential, total = their sum (fJmodels.cpp:49-59)
+        if ((rc = fj_poisson(ctx, nr, npl, d_ar, d_rhl, potC, potC + nt, potC + 2 * nt))) return rc;
+        if ((rc = fj_poisson(ctx, nr, npl, d_ar, d_rhl + nt, potD, potD + nt, potD + 2 * nt))) return rc;
+        FJ_CUDA(launch_sum3(nt, potC, potC + nt, potC + 2 * nt, potD, potD + nt, potD + 2 * nt, potA, potA + nt,
+                            potA + 2 * nt, s));
+    }
+    // focal-distance table from the guess potential (fJmodels.cpp:63, 127)
     std::vector<double> hp(3 * nt);
     FJ_CUDA(cudaMemcpyAsync(hp.data(), potA, 3 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
     FJ_CUDA(cudaStreamSynchronize(s));
@@ -849,16 +868,45 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
     res->last_change = -1;
     FJ_CUDA(cudaStreamSynchronize(s));
     res->setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    int k = 0;
-    for (k = 0; k < cfg->itermax; k++) {
-        fj_potential pot{nr, npl, d_ar, cur, cur + nt, cur + 2 * nt};
-        fj_moment_stats st;
-        if ((rc = fj_compute_new_phi(ctx, &pot, &dt, &cfg->df, &cfg->rule, ng, d_grids, d_coef, nxt, nxt + nt,
-                                     nxt + 2 * nt, &st)))
-            return rc;
+    auto tally = [&](const fj_moment_stats &st) {
         res->bound += st.bound;
         res->failures += st.failures;
         res->kernel_ms += st.kernel_ms;
+    };
+    int k = 0;
+    for (k = 0; k < cfg->itermax; k++) {
+        fj_moment_stats st;
+        const fj_potential pot{nr, npl, d_ar, cur, cur + nt, cur + 2 * nt};
+        if (!two) {
+            if ((rc = fj_compute_new_phi(ctx, &pot, &dt, &cfg->df, &cfg->rule, ng, d_grids, d_coef, nxt, nxt + nt,
+                                         nxt + 2 * nt, &st)))
+                return rc;
+            tally(st);
+        } else if (!ref_order) {
+            // both components in the current total potential, one solve of the summed density
+            if ((rc = fj_moments(ctx, &pot, &dt, &cfg->df, &cfg->rule, ng, d_grids, &st))) return rc;
+            tally(st);
+            if ((rc = fj_legendre_project(ctx, nr, ng, npl, d_ar, d_grids, d_coef))) return rc;
+            if ((rc = fj_moments(ctx, &pot, &dt, &cfg->df2, &cfg->rule, ng, d_grids2, &st))) return rc;
+            tally(st);
+            if ((rc = fj_legendre_project(ctx, nr, ng, npl, d_ar, d_grids2, d_coef2))) return rc;
+            FJ_CUDA(launch_add(nt, d_coef, d_coef2, d_rhl, s));
+            if ((rc = fj_poisson(ctx, nr, npl, d_ar, d_rhl, nxt, nxt + nt, nxt + 2 * nt))) return rc;
+        } else {
+            // component 1 in the total potential; its own new potential replaces the total
+            // (Potential.cpp:182-188); component 2 in that; total = sum (updatePhil)
+            if ((rc = fj_compute_new_phi(ctx, &pot, &dt, &cfg->df, &cfg->rule, ng, d_grids, d_coef, potC, potC + nt,
+                                         potC + 2 * nt, &st)))
+                return rc;
+            tally(st);
+            const fj_potential pot1{nr, npl, d_ar, potC, potC + nt, potC + 2 * nt};
+            if ((rc = fj_compute_new_phi(ctx, &pot1, &dt, &cfg->df2, &cfg->rule, ng, d_grids2, d_coef2, potD, potD + nt,
+                                         potD + 2 * nt, &st)))
+                return rc;
+            tally(st);
+            FJ_CUDA(launch_sum3(nt, potC, potC + nt, potC + 2 * nt, potD, potD + nt, potD + 2 * nt, nxt, nxt + nt,
+                                nxt + 2 * nt, s));
+        }
         FJ_CUDA(cudaMemcpyAsync(neu.data(), nxt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
         FJ_CUDA(cudaStreamSynchronize(s));
         double maxd = 0;
@@ -871,9 +919,12 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
         if (cfg->tol > 0 && maxd < cfg->tol) { k++; break; }
     }
     res->iterations = k;
-    fj_potential pot{nr, npl, d_ar, cur, cur + nt, cur + 2 * nt};
+    const fj_potential pot{nr, npl, d_ar, cur, cur + nt, cur + 2 * nt};
     if ((rc = fj_vir2(ctx, &pot, ng, d_coef, res->vir7))) return rc;
+    if (two && (rc = fj_vir2(ctx, &pot, ng, d_coef2, res->vir7_2))) return rc;
     FJ_CUDA(cudaMemcpyAsync(res->coef6, d_coef, 6 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (two && res->coef6_2)
+        FJ_CUDA(cudaMemcpyAsync(res->coef6_2, d_coef2, 6 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
     FJ_CUDA(cudaMemcpyAsync(res->phil, cur, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
     FJ_CUDA(cudaMemcpyAsync(res->Pr, cur + nt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
     FJ_CUDA(cudaMemcpyAsync(res->Pr2, cur + 2 * nt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));

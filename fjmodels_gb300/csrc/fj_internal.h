@@ -61,6 +61,8 @@ cudaError_t launch_poisson(int nr, int npoly, const double *ar, const double *rh
                            double *Pr, double *Pr2, void *ws, unsigned long long *counters, cudaStream_t s);
 cudaError_t launch_sum3(int n, const double *a0, const double *a1, const double *a2, const double *b0,
                         const double *b1, const double *b2, double *o0, double *o1, double *o2, cudaStream_t s);
+// o = a + b elementwise (summed component densities)
+cudaError_t launch_add(int n, const double *a, const double *b, double *o, cudaStream_t s);
 // vir2: ci, wi = ngauss polar nodes/weights on (0,1); out7 device
 cudaError_t launch_vir2(PotView P, int ngauss, const double *ci, const double *wi, const double *coef6,
                         double *out7, cudaStream_t s);

@@ -233,41 +233,56 @@ FJ_HDNI void pot_grad_f(const PotViewF &P, float R, float z, float &phi, float &
 // recurrence of the even Legendre polynomials,
 //   d_k = C_k ((x - B_k) d_k-1 + (x - y) P_k-1(y) - A_k d_k-2),  x = c^2, y = c2pt,
 // so it keeps its relative precision however close the position is to the
-// point; otherwise it is the difference of two evaluations (Phipt = the FP32
-// potential at the point).
+// point; otherwise it is the direct interpolation (or the r >= ar[nr-1]
+// extrapolation) minus Phipt, the FP32 potential at the point.  All three
+// run in the same loop over the multipoles, each l's term being
+//   vb a_l + (vt - vb) b_l + (v_thr - vb - f3 (vt - vb)) g_l
+// with per-position coefficients, so the lanes of a warp do not split
+// between them.
 FJ_HDNI float pot_dphi_f(const PotViewF &P, float R, float z, float rpt, float c2pt, float dr2, float dc2,
                          float Phipt)
 {
     const float r = sqrtf(R * R + z * z);
     const float *ar = P.ar;
-    const float a0 = ar[0];
-    if (r >= ar[P.nr - 1] || rpt >= ar[P.nr - 1]) return pot_phi_f(P, R, z) - Phipt;
-    const float re = fmaxf(r, a0), rpe = fmaxf(rpt, a0);
-    InterpF I;
-    interp_setup_f(P, re, I);
-    const int b = I.bot;
-    const float ab = ar[b], at = ar[b + 1];
-    if (rpe < ab || rpe > at) return pot_phi_f(P, R, z) - Phipt;
-    const float f1p = (rpe - ab) * P.ih[b];
-    float f2p = 0.f;
-    if (I.quad) {
-        const int thr_p = (f1p < 0.5f && b > 0) ? b - 1 : b + 2;
-        if (thr_p != I.thr && rpe != ab && rpe != at) return pot_phi_f(P, R, z) - Phipt;
-        f2p = (rpe - at) * (rpe - ab) * I.q;
+    const int nr = P.nr, np_ = P.npoly;
+    const float a0 = ar[0], rmax = ar[nr - 1];
+    int mode;  // 0: difference, 1: direct, 2: extrapolated
+    int b = nr - 2, thr = 0;
+    bool quad = false;
+    float f1 = 0.f, f2 = 0.f, f3 = 0.f, f1p = 0.f, f2p = 0.f, df1 = 0.f, df2 = 0.f, xe = 0.f;
+    if (r >= rmax) {
+        mode = 2;
+        xe = rmax / r;
+    } else {
+        const float re = fmaxf(r, a0), rpe = fmaxf(rpt, a0);
+        InterpF I;
+        interp_setup_f(P, re, I);
+        b = I.bot; thr = I.thr; quad = I.quad; f1 = I.f1; f2 = I.f2; f3 = I.f3;
+        const float ab = ar[b], at = ar[b + 1];
+        mode = 1;
+        if (rpt < rmax && rpe >= ab && rpe <= at) {
+            const float fp = (rpe - ab) * P.ih[b];
+            const int thr_p = (fp < 0.5f && b > 0) ? b - 1 : b + 2;
+            if (!quad || thr_p == thr || rpe == ab || rpe == at) {
+                mode = 0;
+                f1p = fp;
+                f2p = quad ? (rpe - at) * (rpe - ab) * I.q : 0.f;
+                const float dr = (r >= a0 && rpt >= a0) ? dr2 / (r + rpt) : re - rpe;
+                df1 = dr * P.ih[b];
+                df2 = quad ? I.q * dr * (re + rpe - ab - at) : 0.f;
+            }
+        }
     }
-    const float dr = (r >= a0 && rpt >= a0) ? dr2 / (r + rpt) : re - rpe;
-    const float df1 = dr * P.ih[b];
-    const float df2 = I.quad ? I.q * dr * (re + rpe - ab - at) : 0.f;
-    const int np_ = P.npoly;
     const float *T = P.phil;
     const LegCoefF &L = leg_f();
-    const float y = c2pt, x = c2pt + dc2;
-    float px1 = 1.f, px2 = 0.f, py1 = 1.f, py2 = 0.f, d1 = 0.f, d2 = 0.f, sum = 0.f;
+    const float y = c2pt, x = mode == 0 ? c2pt + dc2 : (z * z) / (r * r);
+    const float xe2 = xe * xe;
+    float xp = xe;
+    float px1 = 1.f, px2 = 0.f, py1 = 1.f, py2 = 0.f, d1 = 0.f, d2 = 0.f;
+    float sum = mode == 2 ? P.out0 * xe - P.shift : 0.f;  // extrapolated monopole, unshifted table value
     for (int k = 0; k < np_; k++) {
         const float vb = T[b * np_ + k], d = T[(b + 1) * np_ + k] - vb;
-        const float e = I.quad ? T[I.thr * np_ + k] - vb - I.f3 * d : 0.f;
-        const float ph_p = vb + f1p * d + f2p * e;  // phi_k at the point
-        const float dph = df1 * d + df2 * e;         // phi_k(r) - phi_k(point)
+        const float e = quad ? T[thr * np_ + k] - vb - f3 * d : 0.f;
         float px, py, dk;
         if (k == 0) { px = 1.f; py = 1.f; dk = 0.f; }
         else if (k == 1) { px = 1.5f * x - .5f; py = 1.5f * y - .5f; dk = 1.5f * dc2; }
@@ -276,10 +291,18 @@ FJ_HDNI float pot_dphi_f(const PotViewF &P, float R, float z, float rpt, float c
             py = ((y - L.B[k]) * py1 - L.A[k] * py2) * L.C[k];
             dk = ((x - L.B[k]) * d1 + dc2 * py1 - L.A[k] * d2) * L.C[k];
         }
-        sum += dph * px + ph_p * dk;
+        float ca, cb, cg;
+        if (mode == 0) { ca = dk; cb = df1 * px + f1p * dk; cg = df2 * px + f2p * dk; }
+        else if (mode == 1) { ca = px; cb = f1 * px; cg = f2 * px; }
+        else {  // phi_l = phil[nr-1][l] (rmax/r)^(2l+1)
+            const float t = k == 0 ? 0.f : xp * px;
+            ca = t; cb = t; cg = 0.f;
+        }
+        xp *= xe2;
+        sum += vb * ca + d * cb + e * cg;
         px2 = px1; px1 = px; py2 = py1; py1 = py; d2 = d1; d1 = dk;
     }
-    return sum;
+    return mode == 0 ? sum : sum - Phipt;
 }
 
 // Brent root (wrp_GSLroots rule, include/Utils.h:134-167) in FP32; the

@@ -129,6 +129,18 @@ cudaError_t launch_sum3(int n, const double *a0, const double *a1, const double 
     return cudaGetLastError();
 }
 
+__global__ void k_add(int n, const double *a, const double *b, double *o)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) o[i] = a[i] + b[i];
+}
+
+cudaError_t launch_add(int n, const double *a, const double *b, double *o, cudaStream_t s)
+{
+    k_add<<<(n + 255) / 256, 256, 0, s>>>(n, a, b, o);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ vir2
 constexpr int kVirBlock = 256;
 

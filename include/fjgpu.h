@@ -141,12 +141,15 @@ int fj_moments_points(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table
    fj_autotune_mixed times every variant x {2048, 4096, 8192} with
    fj_moments_points on the given device sample points (out6 device
    [6][npts] scratch), keeps the fastest in the context and returns its
-   kernel time; results are the same in every configuration up to the
-   summation order of the per-thread sums. */
+   kernel time (all_ms, if not NULL: host [8][3] times of every variant x
+   {2048, 4096, 8192}); results are the same in every configuration up to
+   the summation order of the per-thread sums (and, between the two forms,
+   the compiler's contraction of the same FP32 expressions). */
 int fj_set_mixed_config(fj_ctx *ctx, int variant, int nodes_per_block);
 int fj_get_mixed_config(fj_ctx *ctx, int *variant, int *nodes_per_block);
 int fj_autotune_mixed(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
-                      const fj_quad_rule *rule, const double *Rz, int npts, double *out6, double *best_ms);
+                      const fj_quad_rule *rule, const double *Rz, int npts, double *out6, double *best_ms,
+                      double *all_ms);
 
 /* rho[0][0] extrapolation (pot/potLeg.cpp:68) and the 6-field Legendre
    projection get_Ylm (include/UtilsLeg.h:200-253).  grids6 device
@@ -247,7 +250,22 @@ typedef struct fj_model_config {
     double tol;                  /* stop when max|dphil/phil_0| < tol (UtilsLeg.h:266-278); <= 0: run itermax */
     const double *Egrid_in;      /* optional host focal-distance table [ngrid] to use instead of */
     const double *Dgrid_in;      /* tabulating it from the guess potential; NULL: tabulate       */
+    /* second component (fJmodels.cpp:38-84); ncomp 0 or 1 = one component */
+    int ncomp;
+    int guess2;                  /* FJ_GUESS_* of component 2 */
+    double mass2, r0_2, q2;
+    fj_df_params df2;
+    int twocomp_order;           /* FJ_TWOCOMP_* */
 } fj_model_config;
+
+/* Two-component iteration order.  SUMMED: both components' moments in the
+   current total potential, one Poisson solve of the summed density
+   multipoles.  REFERENCE: the reference's order (fJmodels.cpp:66-80 with
+   Potential.cpp:182-188): component 1 in the total potential, whose own new
+   potential then replaces the total, component 2 in that, total = sum of the
+   two components' potentials (updatePhil, potLeg.cpp:21-29). */
+#define FJ_TWOCOMP_SUMMED 0
+#define FJ_TWOCOMP_REFERENCE 1
 
 typedef struct fj_model_result {
     /* host arrays the caller allocated: ar [nr], coef6 [6][nr*npoly],
@@ -259,6 +277,9 @@ typedef struct fj_model_result {
     long long bound, failures;
     double wall_ms, kernel_ms;
     double setup_ms;             /* wall time before the first iteration (grid, guess, Poisson, Delta table) */
+    double *coef6_2;             /* two components: component 2's coefficients [6][nr*npoly] (may be NULL);
+                                    coef6, vir7 and grids6 are component 1's */
+    double vir7_2[7];            /* two components: vir2 sums of component 2 in the total potential */
 } fj_model_result;
 
 int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_result *res);
