@@ -38,6 +38,11 @@ class fj_moment_stats(C.Structure):
                 ("kernel_ms", C.c_double), ("escalated", C.c_longlong)]
 
 
+class fj_batch_item(C.Structure):
+    _fields_ = [("pot", fj_potential), ("delta", fj_delta_table), ("df", fj_df_params), ("ngauss", C.c_int),
+                ("grids6", C.c_void_p)]
+
+
 class fj_model_config(C.Structure):
     _fields_ = [("nr", C.c_int), ("ngauss", C.c_int), ("npoly", C.c_int), ("ngrid", C.c_int),
                 ("rmin", C.c_double), ("rmax", C.c_double), ("guess", C.c_int),
@@ -69,6 +74,8 @@ SIGNATURES = {
                     C.c_void_p, P(fj_moment_stats)], C.c_int),
     "fj_moments_points": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule),
                            C.c_void_p, C.c_int, C.c_void_p, P(fj_moment_stats)], C.c_int),
+    "fj_moments_batch": ([CTX, C.c_int, P(fj_batch_item), P(fj_quad_rule), P(fj_moment_stats)], C.c_int),
+    "fj_run_model_batch": ([CTX, C.c_int, P(fj_model_config), P(fj_model_result), C.c_int], C.c_int),
     "fj_set_mixed_config": ([CTX, C.c_int, C.c_int], C.c_int),
     "fj_get_mixed_config": ([CTX, P(C.c_int), P(C.c_int)], C.c_int),
     "fj_autotune_mixed": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule), C.c_void_p,

@@ -171,6 +171,46 @@ class Context:
                     "fj_moments_points")
         return st
 
+    def moments_batch(self, items, rule):
+        """Many models' moment grids in one launch; items = [(pot, delta, df, ngauss, grids6)]
+        with pot/delta from potential()/delta() and grids6 device [6][nr*ngauss]."""
+        self._on_torch_stream()
+        arr = (A.fj_batch_item * len(items))()
+        for i, (pot, delta, df, ng, grids) in enumerate(items):
+            arr[i] = A.fj_batch_item(pot.c, delta.c, df.c, ng, _ptr(grids))
+        st = A.fj_moment_stats()
+        self._check(self.lib.fj_moments_batch(self.h, len(items), arr, C.byref(rule.c), C.byref(st)),
+                    "fj_moments_batch")
+        return st
+
+    def run_model_batch(self, models, rule, itermax, tol=0.0, ngrid=30, use_graph=True):
+        """Several one-component models iterated together (fj_run_model_batch).  models = list of
+        dicts with nr, ngauss, npoly, rmin, rmax, df (DFParams) and optional q, delta_table."""
+        self.use_own_stream()
+        n = len(models)
+        cfgs = (A.fj_model_config * n)()
+        ress = (A.fj_model_result * n)()
+        keep, outs = [], []
+        for i, m in enumerate(models):
+            nr, ng, npl, df = m["nr"], m["ngauss"], m["npoly"], m["df"]
+            dt = m.get("delta_table")
+            din = [None, None] if dt is None else [_f64(dt[0]), _f64(dt[1])]
+            keep.append(din)
+            cfgs[i] = A.fj_model_config(nr, ng, npl, ngrid, m["rmin"], m["rmax"], A.FJ_GUESS.get(df.model, 0), df.mass,
+                                        df.r0, m.get("q", 1.0), df.c, rule.c, itermax, tol,
+                                        *[_dp(d) if d is not None else None for d in din])
+            out = {"ar": np.zeros(nr), "coef6": np.zeros((6, nr, npl)), "phil": np.zeros((nr, npl)),
+                   "Pr": np.zeros((nr, npl)), "Pr2": np.zeros((nr, npl)), "Egrid": np.zeros(ngrid),
+                   "Dgrid": np.zeros(ngrid)}
+            outs.append(out)
+            ress[i] = A.fj_model_result(*[_dp(out[k]) for k in ("ar", "coef6", "phil", "Pr", "Pr2", "Egrid",
+                                                                  "Dgrid")], None)
+        self._check(self.lib.fj_run_model_batch(self.h, n, cfgs, ress, 1 if use_graph else 0), "fj_run_model_batch")
+        for out, r in zip(outs, ress):
+            out.update(vir7=np.array(r.vir7[:]), iterations=r.iterations, last_change=r.last_change, bound=r.bound,
+                       failures=r.failures, wall_ms=r.wall_ms, kernel_ms=r.kernel_ms, setup_ms=r.setup_ms)
+        return outs
+
     def set_mixed_config(self, variant, nodes_per_block):
         self._check(self.lib.fj_set_mixed_config(self.h, variant, nodes_per_block), "fj_set_mixed_config")
 

@@ -38,6 +38,8 @@ struct fj_ctx {
     std::vector<double> rule_host;                     // last uploaded velocity rule
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int mixed_variant = 0, mixed_chunk = kMixedMaxNodes;  // mixed kernel configuration (fj_autotune_mixed)
+    DevBuf batch;                                      // batched launch: MomentArgs[n] | block_start | point_start
+    std::vector<char> batch_host;                      // what `batch` holds (re-uploaded only when it changes)
 };
 
 namespace {
@@ -199,9 +201,11 @@ int check_pot(fj_ctx *ctx, const fj_potential *p)
 
 PotView view(const fj_potential *p) { return PotView{p->nr, p->npoly, p->ar, p->phil, p->Pr, p->Pr2}; }
 
-int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
-                const fj_quad_rule *rule, int ngauss, const double *Rz, int npts, double *out6,
-                fj_moment_stats *stats)
+// Validates one phase-space call and fills its launch arguments (without the
+// scratch pointers).  mixed = the rule asks for the mixed-precision form.
+int build_args(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
+               const fj_quad_rule *rule, int ngauss, const double *Rz, int npts, double *out6, MomentArgs &a,
+               bool &mixed)
 {
     int rc = check_pot(ctx, pot);
     if (rc) return rc;
@@ -210,10 +214,9 @@ int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delt
         return fail(ctx, FJ_ERR_ARG, "moments: bad rule, df or sizes");
     if (rule->precision != FJ_PREC_FP64 && rule->precision != FJ_PREC_MIXED)
         return fail(ctx, FJ_ERR_ARG, "moments: unknown precision mode");
-    const bool mixed = rule->precision == FJ_PREC_MIXED;
+    mixed = rule->precision == FJ_PREC_MIXED;
     if (mixed && (df->kind != FJ_DF_DPL || rule->jquad != FJ_JQUAD_QAGS))
         return fail(ctx, FJ_ERR_ARG, "moments: the mixed form takes the double-power-law DF and QAGS momentum integrals");
-    MomentArgs a;
     a.P = view(pot);
     a.Eg = delta->Egrid; a.Dg = delta->Dgrid; a.ngrid = delta->ngrid;
     if ((rc = upload_rule(ctx, rule, &a.xq, &a.wq))) return rc;
@@ -230,28 +233,43 @@ int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delt
     a.mixed_chunk = ctx->mixed_chunk;
     a.blocks_per_point =
         mixed ? mixed_blocks_per_point(nq3, a.mixed_chunk) : (int)((nq3 + kMomentBlock - 1) / kMomentBlock);
+    a.out6 = out6;
+    return FJ_OK;
+}
+
+int read_stats(fj_ctx *ctx, long long nodes, fj_moment_stats *stats)
+{
+    unsigned long long h[4];
+    FJ_CUDA(cudaMemcpyAsync(h, ctx->counters.p, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+    FJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    stats->nodes = nodes;
+    stats->bound = (long long)h[0];
+    stats->failures = (long long)h[1];
+    stats->kernel_ms = ms;
+    stats->escalated = (long long)h[3];
+    return FJ_OK;
+}
+
+int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
+                const fj_quad_rule *rule, int ngauss, const double *Rz, int npts, double *out6,
+                fj_moment_stats *stats)
+{
+    MomentArgs a;
+    bool mixed = false;
+    int rc = build_args(ctx, pot, delta, df, rule, ngauss, Rz, npts, out6, a, mixed);
+    if (rc) return rc;
     if ((rc = ensure(ctx, ctx->partial, (size_t)npts * a.blocks_per_point * 6 * sizeof(double)))) return rc;
     if ((rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long)))) return rc;
     a.partial = (double *)ctx->partial.p;
     a.counters = (unsigned long long *)ctx->counters.p;
-    a.out6 = out6;
     FJ_CUDA(cudaMemsetAsync(a.counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     FJ_CUDA(mixed ? launch_moments_mixed(a, ctx->mixed_variant, ctx->stream) : launch_moments(a, ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
-    if (stats) {
-        unsigned long long h[4];
-        FJ_CUDA(cudaMemcpyAsync(h, a.counters, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
-        FJ_CUDA(cudaStreamSynchronize(ctx->stream));
-        float ms = 0;
-        cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-        stats->nodes = nq3 * npts;
-        stats->bound = (long long)h[0];
-        stats->failures = (long long)h[1];
-        stats->kernel_ms = ms;
-        stats->escalated = (long long)h[3];
-    }
-    return FJ_OK;
+    const long long nq3 = (long long)rule->nq * rule->nq * rule->nq;
+    return stats ? read_stats(ctx, nq3 * npts, stats) : FJ_OK;
 }
 
 }  // namespace
@@ -343,6 +361,64 @@ int fj_moments_points(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table
 {
     if (!ctx || !Rz) return fail(ctx, FJ_ERR_ARG, "moments_points: bad arguments");
     return run_moments(ctx, pot, delta, df, rule, 0, Rz, npts, out6, stats);
+}
+
+int fj_moments_batch(fj_ctx *ctx, int n, const fj_batch_item *items, const fj_quad_rule *rule,
+                     fj_moment_stats *stats)
+{
+    if (!ctx || n < 1 || !items || !rule) return fail(ctx, FJ_ERR_ARG, "moments_batch: bad arguments");
+    std::vector<MomentArgs> args(n);
+    std::vector<int> bs(n + 1, 0), ps(n + 1, 0);
+    size_t smem = 0, partial = 0;
+    bool mixed = false;
+    long long nodes = 0;
+    const long long nq3 = (long long)rule->nq * rule->nq * rule->nq;
+    for (int m = 0; m < n; m++) {
+        const fj_batch_item &it = items[m];
+        if (it.ngauss < 1) return fail(ctx, FJ_ERR_ARG, "moments_batch: ngauss");
+        const int npts = it.pot.nr * it.ngauss;
+        bool mx = false;
+        int rc = build_args(ctx, &it.pot, &it.delta, &it.df, rule, it.ngauss, nullptr, npts, it.grids6, args[m], mx);
+        if (rc) return rc;
+        mixed = mx;
+        const long long nb = (long long)npts * args[m].blocks_per_point;
+        if (bs[m] + nb > 0x7fffffffLL) return fail(ctx, FJ_ERR_ARG, "moments_batch: too many blocks");
+        bs[m + 1] = bs[m] + (int)nb;
+        ps[m + 1] = ps[m] + npts;
+        args[m].partial = reinterpret_cast<double *>(partial);  // offset, made a pointer below
+        partial += (size_t)nb * 6;
+        const size_t sm = mixed ? moment_mixed_smem_bytes(args[m]) : moment_smem_bytes(args[m]);
+        smem = sm > smem ? sm : smem;
+        nodes += nq3 * npts;
+    }
+    int rc;
+    if ((rc = ensure(ctx, ctx->partial, partial * sizeof(double)))) return rc;
+    if ((rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long)))) return rc;
+    for (int m = 0; m < n; m++) {
+        args[m].partial = (double *)ctx->partial.p + reinterpret_cast<size_t>(args[m].partial);
+        args[m].counters = (unsigned long long *)ctx->counters.p;
+    }
+    // descriptor block: MomentArgs[n] | block_start[n+1] | point_start[n+1]
+    const size_t bytes = n * sizeof(MomentArgs) + 2 * (n + 1) * sizeof(int);
+    std::vector<char> host(bytes);
+    memcpy(host.data(), args.data(), n * sizeof(MomentArgs));
+    memcpy(host.data() + n * sizeof(MomentArgs), bs.data(), (n + 1) * sizeof(int));
+    memcpy(host.data() + n * sizeof(MomentArgs) + (n + 1) * sizeof(int), ps.data(), (n + 1) * sizeof(int));
+    if (ctx->batch_host != host) {  // unchanged descriptors are not re-sent (graph capture repeats the call)
+        if ((rc = ensure(ctx, ctx->batch, bytes))) return rc;
+        FJ_CUDA(cudaMemcpyAsync(ctx->batch.p, host.data(), bytes, cudaMemcpyHostToDevice, ctx->stream));
+        FJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        ctx->batch_host.swap(host);
+    }
+    const char *db = (const char *)ctx->batch.p;
+    const MomentBatch b{(const MomentArgs *)db, (const int *)(db + n * sizeof(MomentArgs)),
+                        (const int *)(db + n * sizeof(MomentArgs) + (n + 1) * sizeof(int)), n};
+    FJ_CUDA(cudaMemsetAsync(ctx->counters.p, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    FJ_CUDA(launch_moments_batch(args[0], b, bs[n], smem, mixed, ctx->mixed_variant, ctx->stream));
+    FJ_CUDA(launch_moments_finalize_batch(b, ps[n], ctx->stream));
+    FJ_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    return stats ? read_stats(ctx, nodes, stats) : FJ_OK;
 }
 
 int fj_set_mixed_config(fj_ctx *ctx, int variant, int nodes_per_block)
@@ -932,5 +1008,184 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
         FJ_CUDA(cudaMemcpyAsync(res->grids6, d_grids, 6 * (size_t)nr * ng * sizeof(double), cudaMemcpyDeviceToHost, s));
     FJ_CUDA(cudaStreamSynchronize(s));
     res->wall_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return FJ_OK;
+}
+
+// ------------------------------------------------------------ many models
+extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfgs, fj_model_result *res,
+                                  int use_graph)
+{
+    if (!ctx || n < 1 || !cfgs || !res) return fail(ctx, FJ_ERR_ARG, "run_model_batch: bad arguments");
+    const fj_quad_rule &rule = cfgs[0].rule;
+    int itermax = cfgs[0].itermax;
+    for (int m = 0; m < n; m++) {
+        const fj_model_config &c = cfgs[m];
+        const fj_model_result &r = res[m];
+        if (!r.ar || !r.coef6 || !r.phil || !r.Pr || !r.Pr2 || !r.Egrid || !r.Dgrid)
+            return fail(ctx, FJ_ERR_ARG, "run_model_batch: missing result buffers");
+        if (c.nr < 11 || c.ngauss < 1 || c.npoly < 1 || c.npoly > kMaxPoly || c.ngrid < 2 || c.itermax < 1 ||
+            c.ncomp > 1)
+            return fail(ctx, FJ_ERR_ARG, "run_model_batch: bad sizes (one-component models only)");
+        if (c.rule.nq != rule.nq || c.rule.precision != rule.precision || c.rule.jquad != rule.jquad ||
+            memcmp(c.rule.xq, rule.xq, rule.nq * sizeof(double)) || memcmp(c.rule.wq, rule.wq, rule.nq * sizeof(double)))
+            return fail(ctx, FJ_ERR_ARG, "run_model_batch: all models must share one velocity rule");
+        itermax = c.itermax > itermax ? c.itermax : itermax;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    // per-model device block: ar | rhl | cur (3 tables) | nxt (3) | Eg | Dg | grids6 | coef6
+    std::vector<size_t> off(n + 1, 0), nts(n);
+    for (int m = 0; m < n; m++) {
+        const fj_model_config &c = cfgs[m];
+        const size_t nt = (size_t)c.nr * c.npoly;
+        nts[m] = nt;
+        off[m + 1] = off[m] + c.nr + nt + 6 * nt + 2 * c.ngrid + 6 * (size_t)c.nr * c.ngauss + 6 * nt;
+    }
+    double *dbuf = nullptr, *hmono = nullptr;
+    FJ_CUDA(cudaMalloc(&dbuf, off[n] * sizeof(double)));
+    struct Free {
+        double *p, *h;
+        ~Free() { cudaFree(p); if (h) cudaFreeHost(h); }
+    } guard{dbuf, nullptr};
+    size_t ntsum = 0;
+    for (int m = 0; m < n; m++) ntsum += nts[m];
+    FJ_CUDA(cudaMallocHost(&hmono, ntsum * sizeof(double)));
+    guard.h = hmono;
+    struct Dev { double *ar, *rhl, *cur, *nxt, *Eg, *Dg, *grids, *coef, *mono; };
+    std::vector<Dev> d(n);
+    cudaStream_t s = ctx->stream;
+    int rc;
+    size_t monooff = 0;
+    for (int m = 0; m < n; m++) {
+        const fj_model_config &c = cfgs[m];
+        const size_t nt = nts[m];
+        double *b = dbuf + off[m];
+        d[m] = Dev{b, b + c.nr, b + c.nr + nt, b + c.nr + 4 * nt, b + c.nr + 7 * nt, b + c.nr + 7 * nt + c.ngrid,
+                   b + c.nr + 7 * nt + 2 * c.ngrid, b + c.nr + 7 * nt + 2 * c.ngrid + 6 * (size_t)c.nr * c.ngauss,
+                   hmono + monooff};
+        monooff += nt;
+        if ((rc = fj_log_grid(c.rmin, c.rmax, c.nr, res[m].ar))) return fail(ctx, rc, "run_model_batch: grid");
+        std::vector<double> rhl(nt);
+        if ((rc = fj_guess_rhl(c.nr, c.ngauss, c.npoly, res[m].ar, c.guess, c.mass, c.r0, c.q, rhl.data())))
+            return fail(ctx, rc, "run_model_batch: guess");
+        FJ_CUDA(cudaMemcpyAsync(d[m].ar, res[m].ar, c.nr * sizeof(double), cudaMemcpyHostToDevice, s));
+        FJ_CUDA(cudaMemcpyAsync(d[m].rhl, rhl.data(), nt * sizeof(double), cudaMemcpyHostToDevice, s));
+        FJ_CUDA(cudaStreamSynchronize(s));
+        if ((rc = fj_poisson(ctx, c.nr, c.npoly, d[m].ar, d[m].rhl, d[m].cur, d[m].cur + nt, d[m].cur + 2 * nt)))
+            return rc;
+        std::vector<double> hp(3 * nt);
+        FJ_CUDA(cudaMemcpyAsync(hp.data(), d[m].cur, 3 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+        FJ_CUDA(cudaStreamSynchronize(s));
+        memcpy(d[m].mono, hp.data(), nt * sizeof(double));
+        fj_potential hpot{c.nr, c.npoly, res[m].ar, hp.data(), hp.data() + nt, hp.data() + 2 * nt};
+        if (c.Egrid_in && c.Dgrid_in) {
+            memcpy(res[m].Egrid, c.Egrid_in, c.ngrid * sizeof(double));
+            memcpy(res[m].Dgrid, c.Dgrid_in, c.ngrid * sizeof(double));
+        } else fj_tabulate_delta(&hpot, c.ngrid, res[m].Egrid, res[m].Dgrid);
+        FJ_CUDA(cudaMemcpyAsync(d[m].Eg, res[m].Egrid, c.ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+        FJ_CUDA(cudaMemcpyAsync(d[m].Dg, res[m].Dgrid, c.ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+        res[m].bound = res[m].failures = 0;
+        res[m].kernel_ms = 0;
+        res[m].last_change = -1;
+    }
+    std::vector<fj_batch_item> items(n);
+    for (int m = 0; m < n; m++) {
+        const fj_model_config &c = cfgs[m];
+        const size_t nt = nts[m];
+        items[m] = fj_batch_item{fj_potential{c.nr, c.npoly, d[m].ar, d[m].cur, d[m].cur + nt, d[m].cur + 2 * nt},
+                                 fj_delta_table{c.ngrid, d[m].Eg, d[m].Dg}, c.df, c.ngauss, d[m].grids};
+    }
+    FJ_CUDA(cudaStreamSynchronize(s));
+    const double setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    std::vector<double> old(ntsum);
+    memcpy(old.data(), hmono, ntsum * sizeof(double));
+    // one iteration of every model: batched phase-space launch, then each model's
+    // projection and Poisson solve into nxt, nxt copied to cur (fixed addresses, so
+    // the sequence can be replayed as a graph) and its multipoles to the host
+    auto iteration = [&](fj_moment_stats *st) -> int {
+        int r2 = fj_moments_batch(ctx, n, items.data(), &rule, st);
+        if (r2) return r2;
+        for (int m = 0; m < n; m++) {
+            const fj_model_config &c = cfgs[m];
+            const size_t nt = nts[m];
+            if ((r2 = fj_legendre_project(ctx, c.nr, c.ngauss, c.npoly, d[m].ar, d[m].grids, d[m].coef))) return r2;
+            if ((r2 = fj_poisson(ctx, c.nr, c.npoly, d[m].ar, d[m].coef, d[m].nxt, d[m].nxt + nt, d[m].nxt + 2 * nt)))
+                return r2;
+            FJ_CUDA(cudaMemcpyAsync(d[m].cur, d[m].nxt, 3 * nt * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            FJ_CUDA(cudaMemcpyAsync(d[m].mono, d[m].nxt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
+        return FJ_OK;
+    };
+    auto converged = [&](int k) {
+        bool all = true;
+        size_t o = 0;
+        for (int m = 0; m < n; m++) {
+            const fj_model_config &c = cfgs[m];
+            double maxd = 0;
+            for (int i = 0; i < c.nr; i++)
+                for (int j = 0; j < c.npoly; j++)
+                    maxd = fmax(maxd, fabs((hmono[o + i * c.npoly + j] - old[o + i * c.npoly + j]) /
+                                           hmono[o + i * c.npoly]));
+            res[m].last_change = maxd;
+            res[m].iterations = k + 1;
+            if (!(c.tol > 0 && maxd < c.tol)) all = false;
+            o += nts[m];
+        }
+        memcpy(old.data(), hmono, ntsum * sizeof(double));
+        return all;
+    };
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    struct GraphFree {
+        cudaGraph_t *g; cudaGraphExec_t *e;
+        ~GraphFree() { if (*e) cudaGraphExecDestroy(*e); if (*g) cudaGraphDestroy(*g); }
+    } gguard{&graph, &exec};
+    double kernel_ms = 0;
+    long long bound = 0, failures = 0;
+    for (int k = 0; k < itermax; k++) {
+        if (use_graph && exec) {
+            FJ_CUDA(cudaGraphLaunch(exec, s));
+            FJ_CUDA(cudaStreamSynchronize(s));
+        } else {
+            fj_moment_stats st;
+            if ((rc = iteration(&st))) return rc;
+            FJ_CUDA(cudaStreamSynchronize(s));
+            kernel_ms += st.kernel_ms;
+            bound += st.bound;
+            failures += st.failures;
+            if (use_graph && k + 1 < itermax) {  // capture the sequence once it has run eagerly
+                FJ_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                rc = iteration(nullptr);
+                cudaGraph_t g = nullptr;
+                const cudaError_t ce = cudaStreamEndCapture(s, &g);
+                if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+                if (ce != cudaSuccess) return cuda_fail(ctx, ce, "run_model_batch: graph capture");
+                graph = g;
+                FJ_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+            }
+        }
+        if (converged(k)) break;
+    }
+    for (int m = 0; m < n; m++) {
+        const fj_model_config &c = cfgs[m];
+        const size_t nt = nts[m];
+        const fj_potential pot{c.nr, c.npoly, d[m].ar, d[m].cur, d[m].cur + nt, d[m].cur + 2 * nt};
+        if ((rc = fj_vir2(ctx, &pot, c.ngauss, d[m].coef, res[m].vir7))) return rc;
+        FJ_CUDA(cudaMemcpyAsync(res[m].coef6, d[m].coef, 6 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+        FJ_CUDA(cudaMemcpyAsync(res[m].phil, d[m].cur, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+        FJ_CUDA(cudaMemcpyAsync(res[m].Pr, d[m].cur + nt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+        FJ_CUDA(cudaMemcpyAsync(res[m].Pr2, d[m].cur + 2 * nt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+        if (res[m].grids6)
+            FJ_CUDA(cudaMemcpyAsync(res[m].grids6, d[m].grids, 6 * (size_t)c.nr * c.ngauss * sizeof(double),
+                                    cudaMemcpyDeviceToHost, s));
+    }
+    FJ_CUDA(cudaStreamSynchronize(s));
+    const double wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    for (int m = 0; m < n; m++) {
+        res[m].wall_ms = wall;
+        res[m].setup_ms = setup_ms;
+        res[m].kernel_ms = kernel_ms;
+        res[m].bound = bound;
+        res[m].failures = failures;
+    }
     return FJ_OK;
 }

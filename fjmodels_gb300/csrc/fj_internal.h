@@ -34,8 +34,33 @@ struct MomentArgs {
     double *out6;            // [6][npts]
 };
 
+// Several models' phase-space launches in one grid: model m owns blocks
+// [block_start[m], block_start[m+1]) and grid points [point_start[m],
+// point_start[m+1]) of the batched finalize.  All pointers are device memory;
+// n = 0: a single launch described by the kernel's MomentArgs parameter.
+struct MomentBatch {
+    const MomentArgs *args;
+    const int *block_start, *point_start;
+    int n;
+};
+
+// the model of block (or point) `i` of a batch: largest m with start[m] <= i
+__device__ __forceinline__ int batch_model(const int *start, int n, int i)
+{
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= i) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
 size_t moment_smem_bytes(const MomentArgs &a);
 cudaError_t launch_moments(const MomentArgs &a, cudaStream_t s);
+// batched forms: grid = total blocks, smem = the largest model's
+cudaError_t launch_moments_batch(const MomentArgs &a0, const MomentBatch &b, int nblocks, size_t smem, bool mixed,
+                                 int variant, cudaStream_t s);
+cudaError_t launch_moments_finalize_batch(const MomentBatch &b, int npoints, cudaStream_t s);
 // the per-point sums of the block partials (shared by both forms)
 cudaError_t launch_moments_finalize(const MomentArgs &a, cudaStream_t s);
 // mixed-precision form (FJ_PREC_MIXED, double-power-law DF, QAGS momentum

@@ -25,9 +25,16 @@ size_t moment_smem_bytes(const MomentArgs &a)
     return nd * sizeof(double) + 6 * (kMomentBlock / 32) * sizeof(double);
 }
 
-__global__ void __launch_bounds__(kMomentBlock) k_moments(MomentArgs a)
+__global__ void __launch_bounds__(kMomentBlock) k_moments(MomentArgs a0, MomentBatch batch)
 {
     extern __shared__ double sm[];
+    MomentArgs a = a0;
+    int bid = blockIdx.x;
+    if (batch.n > 0) {
+        const int m = batch_model(batch.block_start, batch.n, bid);
+        a = batch.args[m];
+        bid -= batch.block_start[m];
+    }
     const int nr = a.P.nr, npoly = a.P.npoly, nt = nr * npoly;
     double *s_ar = sm, *s_phil = s_ar + nr, *s_Pr = s_phil + nt, *s_Pr2 = s_Pr + nt;
     double *s_Eg = s_Pr2 + nt, *s_Dg = s_Eg + a.ngrid, *s_xq = s_Dg + a.ngrid, *s_wq = s_xq + a.nq;
@@ -44,7 +51,7 @@ __global__ void __launch_bounds__(kMomentBlock) k_moments(MomentArgs a)
     const PotView P{nr, npoly, s_ar, s_phil, s_Pr, s_Pr2};
     const GLRule gl{a.gl.n, s_glx, s_glw};
     const int B = a.blocks_per_point;
-    const int p = blockIdx.x / B, chunk = blockIdx.x % B;
+    const int p = bid / B, chunk = bid % B;
     const int nq = a.nq, nq3 = nq * nq * nq;
     const int node = chunk * kMomentBlock + threadIdx.x;
 
@@ -108,10 +115,8 @@ __global__ void __launch_bounds__(kMomentBlock) k_moments(MomentArgs a)
 
 // sums the per-block partials of each point and normalises as rhofDF does
 // (integ/Integ.cpp:160-162)
-__global__ void k_moments_finalize(const double *partial, int npts, int B, double *out6)
+__device__ __forceinline__ void finalize_point(const double *partial, int npts, int B, double *out6, int p)
 {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npts) return;
     double s[6] = {0, 0, 0, 0, 0, 0};
     for (int c = 0; c < B; c++)
 #pragma unroll
@@ -124,6 +129,27 @@ __global__ void k_moments_finalize(const double *partial, int npts, int B, doubl
     out6[5 * (size_t)npts + p] = sqrt(fabs(s[5]) / s[0]);
 }
 
+__global__ void k_moments_finalize(const double *partial, int npts, int B, double *out6)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < npts) finalize_point(partial, npts, B, out6, p);
+}
+
+__global__ void k_moments_finalize_batch(MomentBatch batch, int npoints)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= npoints) return;
+    const int m = batch_model(batch.point_start, batch.n, t);
+    const MomentArgs &a = batch.args[m];
+    finalize_point(a.partial, a.npts, a.blocks_per_point, a.out6, t - batch.point_start[m]);
+}
+
+cudaError_t launch_moments_finalize_batch(const MomentBatch &b, int npoints, cudaStream_t s)
+{
+    k_moments_finalize_batch<<<(npoints + 127) / 128, 128, 0, s>>>(b, npoints);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_moments(const MomentArgs &a, cudaStream_t s)
 {
     const size_t smem = moment_smem_bytes(a);
@@ -132,10 +158,21 @@ cudaError_t launch_moments(const MomentArgs &a, cudaStream_t s)
         if (e != cudaSuccess) return e;
     }
     const long long nblocks = (long long)a.npts * a.blocks_per_point;
-    k_moments<<<(unsigned)nblocks, kMomentBlock, smem, s>>>(a);
+    k_moments<<<(unsigned)nblocks, kMomentBlock, smem, s>>>(a, MomentBatch{nullptr, nullptr, nullptr, 0});
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     return launch_moments_finalize(a, s);
+}
+
+cudaError_t launch_moments_plain_batch(const MomentArgs &a0, const MomentBatch &b, int nblocks, size_t smem,
+                                      cudaStream_t s)
+{
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_moments, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_moments<<<(unsigned)nblocks, kMomentBlock, smem, s>>>(a0, b);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_moments_finalize(const MomentArgs &a, cudaStream_t s)

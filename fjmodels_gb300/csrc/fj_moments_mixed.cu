@@ -36,9 +36,16 @@ size_t moment_mixed_smem_bytes(const MomentArgs &a)
 }
 
 template <int MINB, bool WAVE>
-__global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs a)
+__global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs a0, MomentBatch batch)
 {
     extern __shared__ double sm[];
+    MomentArgs a = a0;
+    int bid = blockIdx.x;
+    if (batch.n > 0) {
+        const int m = batch_model(batch.block_start, batch.n, bid);
+        a = batch.args[m];
+        bid -= batch.block_start[m];
+    }
     const int nr = a.P.nr, npoly = a.P.npoly, nt = nr * npoly;
     double *s_ar = sm, *s_phil = s_ar + nr, *s_Pr = s_phil + nt, *s_Pr2 = s_Pr + nt;
     double *s_Eg = s_Pr2 + nt, *s_Dg = s_Eg + a.ngrid, *s_xq = s_Dg + a.ngrid, *s_wq = s_xq + a.nq;
@@ -61,7 +68,7 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
     }
     const PotView P{nr, npoly, s_ar, s_phil, s_Pr, s_Pr2};
     const int B = a.blocks_per_point;
-    const int p = blockIdx.x / B, chunk = blockIdx.x % B;
+    const int p = bid / B, chunk = bid % B;
     __syncthreads();
     if (threadIdx.x == 0) {  // per-point FP64 setup, shared by the block (integ/Integ.cpp:46-62,150-151)
         double R, z;
@@ -205,16 +212,32 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
 
 namespace {
 template <int MINB, bool WAVE>
-cudaError_t launch_variant(const MomentArgs &a, size_t smem, cudaStream_t s)
+cudaError_t launch_variant(const MomentArgs &a, const MomentBatch &b, long long nblocks, size_t smem,
+                           cudaStream_t s)
 {
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_moments_mixed<MINB, WAVE>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    const long long nblocks = (long long)a.npts * a.blocks_per_point;
-    k_moments_mixed<MINB, WAVE><<<(unsigned)nblocks, kMixedBlock, smem, s>>>(a);
+    k_moments_mixed<MINB, WAVE><<<(unsigned)nblocks, kMixedBlock, smem, s>>>(a, b);
     return cudaGetLastError();
+}
+
+cudaError_t launch_mixed_any(const MomentArgs &a, const MomentBatch &b, long long nblocks, size_t smem, int variant,
+                             cudaStream_t s)
+{
+    switch (variant) {
+    case 0: return launch_variant<3, false>(a, b, nblocks, smem, s);
+    case 1: return launch_variant<4, false>(a, b, nblocks, smem, s);
+    case 2: return launch_variant<6, false>(a, b, nblocks, smem, s);
+    case 3: return launch_variant<8, false>(a, b, nblocks, smem, s);
+    case 4: return launch_variant<3, true>(a, b, nblocks, smem, s);
+    case 5: return launch_variant<4, true>(a, b, nblocks, smem, s);
+    case 6: return launch_variant<6, true>(a, b, nblocks, smem, s);
+    case 7: return launch_variant<8, true>(a, b, nblocks, smem, s);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 template <int MINB, bool WAVE>
@@ -229,20 +252,20 @@ cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, cudaStream_t 
 {
     if (a.mixed_chunk < kMixedBlock || a.mixed_chunk > kMixedMaxNodes) return cudaErrorInvalidValue;
     const size_t smem = moment_mixed_smem_bytes(a);
-    cudaError_t e;
-    switch (variant) {
-    case 0: e = launch_variant<3, false>(a, smem, s); break;
-    case 1: e = launch_variant<4, false>(a, smem, s); break;
-    case 2: e = launch_variant<6, false>(a, smem, s); break;
-    case 3: e = launch_variant<8, false>(a, smem, s); break;
-    case 4: e = launch_variant<3, true>(a, smem, s); break;
-    case 5: e = launch_variant<4, true>(a, smem, s); break;
-    case 6: e = launch_variant<6, true>(a, smem, s); break;
-    case 7: e = launch_variant<8, true>(a, smem, s); break;
-    default: return cudaErrorInvalidValue;
-    }
+    const cudaError_t e = launch_mixed_any(a, MomentBatch{nullptr, nullptr, nullptr, 0},
+                                           (long long)a.npts * a.blocks_per_point, smem, variant, s);
     if (e != cudaSuccess) return e;
     return launch_moments_finalize(a, s);
+}
+
+cudaError_t launch_moments_plain_batch(const MomentArgs &a0, const MomentBatch &b, int nblocks, size_t smem,
+                                      cudaStream_t s);
+
+cudaError_t launch_moments_batch(const MomentArgs &a0, const MomentBatch &b, int nblocks, size_t smem, bool mixed,
+                                 int variant, cudaStream_t s)
+{
+    if (!mixed) return launch_moments_plain_batch(a0, b, nblocks, smem, s);
+    return launch_mixed_any(a0, b, nblocks, smem, variant, s);
 }
 
 size_t moments_mixed_local_bytes()

@@ -131,6 +131,22 @@ int fj_moments_points(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table
                       const fj_df_params *df, const fj_quad_rule *rule, const double *Rz, int npts,
                       double *out6, fj_moment_stats *stats);
 
+/* Many models' phase-space integrals in one launch (no reference counterpart:
+   the reference builds one model per process).  Item m is one model's
+   computeRhl grid (pot/potLeg.cpp:35-70): its own device potential, Delta
+   table, DF and polar node count, output grids6 device [6][nr*ngauss]; all
+   items share the velocity rule (and form).  Blocks are assigned to models
+   by a prefix table; the results are those of fj_moments per item. */
+typedef struct fj_batch_item {
+    fj_potential pot;
+    fj_delta_table delta;
+    fj_df_params df;
+    int ngauss;
+    double *grids6;
+} fj_batch_item;
+int fj_moments_batch(fj_ctx *ctx, int n, const fj_batch_item *items, const fj_quad_rule *rule,
+                     fj_moment_stats *stats);
+
 /* Configuration of the mixed-precision phase-space kernel (no reference
    counterpart: the reference has one CPU loop).  variant 0..7: 0..3 run each
    node's solve as nested loops, 4..7 in the wavefront form (all lanes of a
@@ -283,6 +299,16 @@ typedef struct fj_model_result {
 } fj_model_result;
 
 int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_result *res);
+
+/* n one-component models iterated together (no reference counterpart): per
+   iteration one fj_moments_batch launch over every model's grid, then each
+   model's projection and Poisson solve; with use_graph the iteration is
+   captured once as a CUDA graph after running eagerly and replayed.  All
+   models share cfgs[0].rule; each runs max(itermax) iterations or until every
+   model's tol is met.  res[m] as fj_run_model, except wall_ms, setup_ms,
+   kernel_ms (eager iterations only), bound and failures, which are totals of
+   the batch. */
+int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfgs, fj_model_result *res, int use_graph);
 
 #ifdef __cplusplus
 }
