@@ -44,9 +44,10 @@ UNIT = "s/model"
 # phase-space kernel (dadd + dmul + 2*dfma from ncu on the nfw_80x40 workload,
 # profiles/moments_fp64_nfw_80x40.md); the algorithmic work unit of the roofline.
 FP64_FLOPS_PER_EVAL = {"plain": 1.23e5, "gl": None}
-# FP32 operations (fadd + fmul + 2*ffma) per phase-space evaluation of the mixed
-# form, from ncu on the same workload (profiles/moments_mixed_nfw_80x40.md)
-FP32_FLOPS_PER_EVAL = {"mixed": None}
+# FP32 operations (fadd + fmul + 2*ffma) executed by active lanes per phase-space
+# evaluation of the mixed form, from ncu on a 240-point spread of the same workload
+# (profiles/moments_mixed_nfw_80x40.md)
+FP32_FLOPS_PER_EVAL = {"mixed": 4.78e4}
 
 
 def parse():
@@ -195,7 +196,8 @@ def run_ours(args, rank, world):
         ci, _ = F.gauleg(0, 1, ng)
         allp = np.array([[ar[n] * np.sqrt(1 - c * c), ar[n] * c] for n in range(nr) for c in ci])
         v, c, ms = ctx.autotune_mixed(ctx.potential(d_ar, *tabs), delta, df, rule, torch.tensor(allp[::7], **f64))
-        tuned = {"variant": v, "nodes_per_block": c, "sample_kernel_ms": ms, "sample_points": len(allp[::7])}
+        tuned = {"variant": v, "nodes_per_block": c, "sample_kernel_ms": ms, "sample_points": len(allp[::7]),
+                 "table_ms": np.round(ctx.autotune_table, 2).tolist()}
     state = {"cur": tabs, "nxt": nxt}
     kernel_ms, changes = [], []
 
