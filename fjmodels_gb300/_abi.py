@@ -76,6 +76,8 @@ SIGNATURES = {
                            C.c_void_p, C.c_int, C.c_void_p, P(fj_moment_stats)], C.c_int),
     "fj_moments_batch": ([CTX, C.c_int, P(fj_batch_item), P(fj_quad_rule), P(fj_moment_stats)], C.c_int),
     "fj_run_model_batch": ([CTX, C.c_int, P(fj_model_config), P(fj_model_result), C.c_int], C.c_int),
+    "fj_tc_gemm": ([C.c_int] * 3 + [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int,
+                                     C.c_void_p], C.c_int),
     "fj_set_mixed_config": ([CTX, C.c_int, C.c_int], C.c_int),
     "fj_get_mixed_config": ([CTX, P(C.c_int), P(C.c_int)], C.c_int),
     "fj_autotune_mixed": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule), C.c_void_p,

@@ -211,6 +211,16 @@ class Context:
                        failures=r.failures, wall_ms=r.wall_ms, kernel_ms=r.kernel_ms, setup_ms=r.setup_ms)
         return outs
 
+    def tc_gemm(self, a, b, c, ksplit=1):
+        """c = a @ b.T on the tensor cores: a [M][K], b [N][K] bfloat16, c [M][N] float32 (device)."""
+        import torch
+        m, k = a.shape
+        n = b.shape[0]
+        rc = self.lib.fj_tc_gemm(m, n, k, _ptr(a), a.stride(0), _ptr(b), b.stride(0), _ptr(c), c.stride(0), ksplit,
+                                 C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        if rc != A.FJ_OK:
+            raise FJError(f"fj_tc_gemm failed ({rc})")
+
     def set_mixed_config(self, variant, nodes_per_block):
         self._check(self.lib.fj_set_mixed_config(self.h, variant, nodes_per_block), "fj_set_mixed_config")
 

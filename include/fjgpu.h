@@ -147,6 +147,16 @@ typedef struct fj_batch_item {
 int fj_moments_batch(fj_ctx *ctx, int n, const fj_batch_item *items, const fj_quad_rule *rule,
                      fj_moment_stats *stats);
 
+/* BF16 GEMM on the tensor cores (tcgen05, FP32 accumulation in tensor
+   memory), the building block of the action surrogate; no reference
+   counterpart.  C[M][N] = A[M][K] B[N][K]^T with A, B device BF16 (K
+   contiguous, lda/ldb multiples of 8, 16-byte aligned), C device FP32 (row
+   stride ldc), N and K multiples of 16; ksplit > 1 splits K across CTAs and
+   accumulates with atomics.  Synchronises the stream.  FJ_ERR_CUDA if a
+   tensor-core wait timed out. */
+int fj_tc_gemm(int M, int N, int K, const void *A, int lda, const void *B, int ldb, float *C, int ldc, int ksplit,
+               void *stream);
+
 /* Configuration of the mixed-precision phase-space kernel (no reference
    counterpart: the reference has one CPU loop).  variant 0..7: 0..3 run each
    node's solve as nested loops, 4..7 in the wavefront form (all lanes of a
