@@ -78,6 +78,13 @@ SIGNATURES = {
     "fj_run_model_batch": ([CTX, C.c_int, P(fj_model_config), P(fj_model_result), C.c_int], C.c_int),
     "fj_tc_gemm": ([C.c_int] * 3 + [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int,
                                      C.c_void_p], C.c_int),
+    "fj_surrogate_create": ([CTX, C.c_int, C.c_ulonglong, P(C.c_void_p)], C.c_int),
+    "fj_surrogate_destroy": ([C.c_void_p], C.c_int),
+    "fj_surrogate_nparam": ([C.c_void_p], C.c_longlong),
+    "fj_surrogate_params": ([C.c_void_p, DP, DP], C.c_int),
+    "fj_surrogate_gradients": ([C.c_void_p, C.c_void_p, C.c_void_p, DP, DP], C.c_int),
+    "fj_surrogate_train": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_float, DP], C.c_int),
+    "fj_surrogate_predict": ([C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p], C.c_int),
     "fj_set_mixed_config": ([CTX, C.c_int, C.c_int], C.c_int),
     "fj_get_mixed_config": ([CTX, P(C.c_int), P(C.c_int)], C.c_int),
     "fj_autotune_mixed": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule), C.c_void_p,

@@ -422,3 +422,70 @@ def readParam(path="param.txt"):
         else:
             raise FJError("ERROR in parameterfile: second components is missing some parameter to initialize!")
     return p, comps
+
+
+class Surrogate:
+    """The action surrogate (fj_surrogate_*): MLP 16 -> 128 x 4 (GELU) -> 16 on the tensor
+    cores, outputs 0 and 1 = (log Jr, log Jz) of normalised features."""
+
+    LAYERS = [(128, 16), (128, 128), (128, 128), (128, 128), (16, 128)]  # (rows, cols) of W
+
+    def __init__(self, ctx, batch=4096, seed=1):
+        self.ctx, self.lib, self.batch = ctx, ctx.lib, batch
+        h = C.c_void_p()
+        ctx._on_torch_stream()
+        rc = self.lib.fj_surrogate_create(ctx.h, batch, seed, C.byref(h))
+        if rc != A.FJ_OK:
+            raise FJError(f"fj_surrogate_create failed ({rc})")
+        self.h = h
+        self.nparam = self.lib.fj_surrogate_nparam(h)
+
+    def close(self):
+        if self.h:
+            self.lib.fj_surrogate_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _rc(self, rc, what):
+        if rc != A.FJ_OK:
+            raise FJError(f"{what} failed ({rc})")
+
+    def params(self):
+        p = np.zeros(self.nparam)
+        self._rc(self.lib.fj_surrogate_params(self.h, _dp(p), None), "fj_surrogate_params")
+        return p
+
+    def set_params(self, p):
+        p = _f64(p)
+        self._rc(self.lib.fj_surrogate_params(self.h, None, _dp(p)), "fj_surrogate_params")
+
+    def unpack(self, p):
+        """[(W [rows][cols], b [rows])] per layer from a flat parameter vector."""
+        out, o = [], 0
+        for r, c in self.LAYERS:
+            W = p[o:o + r * c].reshape(r, c)
+            o += r * c
+            out.append((W, p[o:o + r]))
+            o += r
+        return out
+
+    def gradients(self, X, T):
+        g, loss = np.zeros(self.nparam), np.zeros(1)
+        self._rc(self.lib.fj_surrogate_gradients(self.h, _ptr(X), _ptr(T), _dp(g), _dp(loss)),
+                 "fj_surrogate_gradients")
+        return g, float(loss[0])
+
+    def train(self, X, T, epochs=1, lr=1e-3):
+        loss = np.zeros(1)
+        self._rc(self.lib.fj_surrogate_train(self.h, _ptr(X), _ptr(T), X.shape[0], epochs, lr, _dp(loss)),
+                 "fj_surrogate_train")
+        return float(loss[0])
+
+    def predict(self, X, Y):
+        self._rc(self.lib.fj_surrogate_predict(self.h, _ptr(X), X.shape[0], _ptr(Y)), "fj_surrogate_predict")
+

@@ -42,6 +42,10 @@ struct fj_ctx {
     std::vector<char> batch_host;                      // what `batch` holds (re-uploaded only when it changes)
 };
 
+namespace fj {
+cudaStream_t context_stream(fj_ctx *ctx) { return ctx->stream; }
+}  // namespace fj
+
 namespace {
 
 int fail(fj_ctx *c, int code, const std::string &msg)

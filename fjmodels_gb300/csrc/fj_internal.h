@@ -1,9 +1,12 @@
 // fj_internal.h -- launch interface between the C-ABI layer and the kernels.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "fj_device.cuh"
+
+struct fj_ctx;
 
 namespace fj {
 
@@ -91,6 +94,13 @@ cudaError_t launch_add(int n, const double *a, const double *b, double *o, cudaS
 // vir2: ci, wi = ngauss polar nodes/weights on (0,1); out7 device
 cudaError_t launch_vir2(PotView P, int ngauss, const double *ci, const double *wi, const double *coef6,
                         double *out7, cudaStream_t s);
+
+// the stream a context orders its work on
+cudaStream_t context_stream(::fj_ctx *ctx);
+// BF16 tensor-core GEMM (fj_mlp.cu): C = A B^T with a fused epilogue
+namespace tc { struct Epilogue; }
+cudaError_t launch_gemm_tc(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K,
+                           int ksplit, const tc::Epilogue &ep, cudaStream_t s);
 
 // largest per-thread local memory (stack) any kernel of the library needs
 size_t moments_local_bytes();

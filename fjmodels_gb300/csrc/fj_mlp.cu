@@ -1,7 +1,10 @@
 // fj_mlp.cu -- tensor-core (tcgen05) GEMM and the action surrogate built on it.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
+#include <vector>
 
 #include "../../include/fjgpu.h"
 #include "fj_internal.h"
@@ -147,6 +150,12 @@ cudaError_t launch_gemm_tc(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 
     const dim3 grid((M + tc::kTileM - 1) / tc::kTileM, (N + tc::kTileN - 1) / tc::kTileN, (K + kslice - 1) / kslice);
     // 23 KB of unused dynamic shared memory hold residency at 4 CTAs per SM,
     // whose 4 x 128 TMEM columns are exactly the SM's 512: no CTA waits in alloc
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kPadSmem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
     k_gemm_tc<<<grid, tc::kThreads, kPadSmem, s>>>(A, lda, B, ldb, M, N, K, kslice, ep);
     return cudaGetLastError();
 }
@@ -172,3 +181,541 @@ extern "C" int fj_tc_gemm(int M, int N, int K, const void *A, int lda, const voi
     if (e != cudaSuccess) return e == cudaErrorInvalidValue ? FJ_ERR_ARG : FJ_ERR_CUDA;
     return h ? FJ_ERR_CUDA : FJ_OK;
 }
+
+// ======================================================================
+// The action surrogate: an MLP 16 -> 128 -> 128 -> 128 -> 128 -> 16 (GELU),
+// inputs padded from 13 features, outputs 0 and 1 used (log Jr, log Jz),
+// trained with Adam on mean-squared error.  Master weights FP32, BF16 copies
+// (and their transposes, for the backward data products) feed the GEMMs.
+// ======================================================================
+namespace fj {
+namespace {
+
+constexpr int kIn = 16, kHid = 128, kOut = 16, kLayers = 5, kUsedOut = 2;
+
+__global__ void k_to_bf16(int n, const float *x, __nv_bfloat16 *y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = __float2bfloat16_rn(x[i]);
+}
+
+// y[c][r] = x[r][c] (bf16, r < R, c < C), 32 x 32 tiles through shared memory
+__global__ void k_transpose_bf16(int R, int C, const __nv_bfloat16 *x, int ldx, __nv_bfloat16 *y, int ldy)
+{
+    __shared__ __nv_bfloat16 t[32][33];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int r = r0 + i, c = c0 + threadIdx.x;
+        if (r < R && c < C) t[i][threadIdx.x] = x[(size_t)r * ldx + c];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        const int c = c0 + i, r = r0 + threadIdx.x;
+        if (r < R && c < C) y[(size_t)c * ldy + r] = t[threadIdx.x][i];
+    }
+}
+
+// f32 -> transposed bf16 copy of a weight matrix W[rows][cols] -> WT[cols][rows]
+__global__ void k_weight_t(int rows, int cols, const float *w, __nv_bfloat16 *wt)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * cols) return;
+    const int r = i / cols, c = i % cols;
+    wt[(size_t)c * rows + r] = __float2bfloat16_rn(w[i]);
+}
+
+// dY = 2 (Y - T) / (B * kUsedOut) on the used outputs (bf16, zero elsewhere); loss sum
+__global__ void k_mse_grad(int B, const float *y, const float *t, __nv_bfloat16 *dy, float *loss)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float l = 0.f;
+    if (i < B * kOut) {
+        const int b = i / kOut, o = i % kOut;
+        float g = 0.f;
+        if (o < kUsedOut) {
+            const float d = y[i] - t[b * kUsedOut + o];
+            g = 2.f * d / (float)(B * kUsedOut);
+            l = d * d;
+        }
+        dy[i] = __float2bfloat16_rn(g);
+    }
+    for (int off = 16; off > 0; off >>= 1) l += __shfl_xor_sync(0xffffffffu, l, off);
+    if ((threadIdx.x & 31) == 0 && l != 0.f) atomicAdd(loss, l / (float)(B * kUsedOut));
+}
+
+// column sums of a [B][N] bf16 matrix into g[N] (f32, accumulated)
+__global__ void k_colsum(int B, int N, const __nv_bfloat16 *x, float *g)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    float s = 0.f;
+    for (int b = blockIdx.y; b < B; b += gridDim.y) s += __bfloat162float(x[(size_t)b * N + c]);
+    atomicAdd(g + c, s);
+}
+
+// Adam (Kingma & Ba 2015) on n parameters; bias-corrected step size alpha_t
+__global__ void k_adam(int n, float *w, const float *g, float *m, float *v, float alpha_t, float b1, float b2,
+                       float eps, const unsigned char *mask)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || (mask && !mask[i])) return;
+    const float gi = g[i];
+    m[i] = b1 * m[i] + (1.f - b1) * gi;
+    v[i] = b2 * v[i] + (1.f - b2) * gi * gi;
+    w[i] -= alpha_t * m[i] / (sqrtf(v[i]) + eps);
+}
+
+}  // namespace
+}  // namespace fj
+
+struct fj_surrogate {
+    fj_ctx *ctx = nullptr;
+    cudaStream_t stream = nullptr;
+    int batch = 0;  // samples per training step
+    int rows[5], cols[5];
+    size_t woff[5], boff[5], nparam = 0;
+    // parameters (f32 masters), gradients, Adam moments, masks of trainable entries
+    float *P = nullptr, *G = nullptr, *Mom = nullptr, *Var = nullptr;
+    unsigned char *mask = nullptr;
+    __nv_bfloat16 *Wb = nullptr, *WbT = nullptr;  // bf16 weights and transposes, at woff
+    // activations of one batch
+    __nv_bfloat16 *X = nullptr, *XT = nullptr, *H = nullptr, *HT = nullptr, *dZ = nullptr, *dZT = nullptr;
+    float *Z = nullptr, *Y = nullptr, *loss = nullptr;
+    int *err = nullptr;
+    __nv_bfloat16 *Xi = nullptr, *Hi = nullptr;  // inference workspace
+    long long step = 0;
+    std::vector<void *> owned;
+};
+
+namespace {
+
+using fj::tc::Epilogue;
+
+constexpr int kInferRows = 1 << 20;  // rows per inference pass (2 x 256 MB of activations)
+
+int sg_alloc(fj_surrogate *s, void **p, size_t bytes)
+{
+    if (cudaMalloc(p, bytes) != cudaSuccess) return FJ_ERR_NOMEM;
+    s->owned.push_back(*p);
+    return cudaMemsetAsync(*p, 0, bytes, s->stream) == cudaSuccess ? FJ_OK : FJ_ERR_CUDA;
+}
+
+#define SG_CUDA(call)                                   \
+    do {                                                \
+        if ((call) != cudaSuccess) return FJ_ERR_CUDA;  \
+    } while (0)
+
+// bf16 copies of the weights and of their transposes
+int sg_refresh(fj_surrogate *s)
+{
+    for (int l = 0; l < fj::kLayers; l++) {
+        const int n = s->rows[l] * s->cols[l];
+        fj::k_to_bf16<<<(n + 255) / 256, 256, 0, s->stream>>>(n, s->P + s->woff[l], s->Wb + s->woff[l]);
+        fj::k_weight_t<<<(n + 255) / 256, 256, 0, s->stream>>>(s->rows[l], s->cols[l], s->P + s->woff[l],
+                                                               s->WbT + s->woff[l]);
+    }
+    return cudaGetLastError() == cudaSuccess ? FJ_OK : FJ_ERR_CUDA;
+}
+
+int sg_gemm(fj_surrogate *s, const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K,
+            int ksplit, Epilogue ep)
+{
+    ep.err = s->err;
+    return fj::launch_gemm_tc(A, lda, B, ldb, M, N, K, ksplit, ep, s->stream) == cudaSuccess ? FJ_OK : FJ_ERR_CUDA;
+}
+
+int sg_transpose(fj_surrogate *s, int R, int C, const __nv_bfloat16 *x, __nv_bfloat16 *y)
+{
+    const dim3 grid((C + 31) / 32, (R + 31) / 32);
+    fj::k_transpose_bf16<<<grid, dim3(32, 8), 0, s->stream>>>(R, C, x, C, y, R);
+    return cudaGetLastError() == cudaSuccess ? FJ_OK : FJ_ERR_CUDA;
+}
+
+// forward pass of n rows of X (bf16 [n][16]) through the layers; keep
+// (training, n = batch): pre-activations to Z[l] and activations to H[l];
+// else the hidden layers ping-pong between the two halves of Hbuf, each of
+// hcap rows.  Output f32 [n][16] in out.
+int sg_forward(fj_surrogate *s, const __nv_bfloat16 *X, int n, float *out, bool keep, __nv_bfloat16 *Hbuf,
+               size_t hcap)
+{
+    const size_t hb = hcap * fj::kHid;
+    const __nv_bfloat16 *in = X;
+    int inw = fj::kIn, rc;
+    for (int l = 0; l < 4; l++) {
+        __nv_bfloat16 *h = Hbuf + (keep ? l : (l & 1)) * hb;
+        Epilogue ep{fj::tc::kEpiBiasGelu, s->P + s->boff[l], nullptr, h, keep ? s->Z + l * hb : nullptr, nullptr,
+                    fj::kHid, nullptr};
+        if ((rc = sg_gemm(s, in, inw, s->Wb + s->woff[l], s->cols[l], n, fj::kHid, inw, 1, ep))) return rc;
+        in = h;
+        inw = fj::kHid;
+    }
+    Epilogue ep{fj::tc::kEpiStoreF32, s->P + s->boff[4], out, nullptr, nullptr, nullptr, fj::kOut, nullptr};
+    return sg_gemm(s, in, fj::kHid, s->Wb + s->woff[4], fj::kHid, n, fj::kOut, fj::kHid, 1, ep);
+}
+
+// gradients of the mean-squared error of one training batch (after sg_forward
+// with keep) into G; T f32 [batch][2]
+int sg_backward(fj_surrogate *s, const float *T)
+{
+    const int B = s->batch, ks = (B + 4095) / 4096;
+    const size_t hb = (size_t)B * fj::kHid;
+    int rc;
+    SG_CUDA(cudaMemsetAsync(s->G, 0, s->nparam * sizeof(float), s->stream));
+    __nv_bfloat16 *dY = s->dZ + hb;  // [B][16], after the two dZ buffers' first
+    fj::k_mse_grad<<<(B * fj::kOut + 255) / 256, 256, 0, s->stream>>>(B, s->Y, T, dY, s->loss);
+    // output layer: gW4 = dY^T H3, gb4 = colsum(dY), dZ3 = (dY W4) * gelu'(Z3)
+    if ((rc = sg_transpose(s, B, fj::kOut, dY, s->dZT))) return rc;
+    if ((rc = sg_transpose(s, B, fj::kHid, s->H + 3 * hb, s->HT))) return rc;
+    Epilogue gw{fj::tc::kEpiAtomicF32, nullptr, s->G + s->woff[4], nullptr, nullptr, nullptr, fj::kHid, nullptr};
+    if ((rc = sg_gemm(s, s->dZT, B, s->HT, B, fj::kOut, fj::kHid, B, ks, gw))) return rc;
+    fj::k_colsum<<<dim3(1, 64), fj::kOut, 0, s->stream>>>(B, fj::kOut, dY, s->G + s->boff[4]);
+    __nv_bfloat16 *dz = s->dZ, *dz2 = s->dZ + (size_t)2 * hb;
+    Epilogue gg{fj::tc::kEpiGeluGrad, nullptr, nullptr, dz, nullptr, s->Z + 3 * hb, fj::kHid, nullptr};
+    if ((rc = sg_gemm(s, dY, fj::kOut, s->WbT + s->woff[4], fj::kOut, B, fj::kHid, fj::kOut, 1, gg))) return rc;
+    for (int l = 3; l >= 0; l--) {
+        // gW_l = dZ_l^T H_{l-1} (X for l = 0), gb_l = colsum(dZ_l)
+        const __nv_bfloat16 *prev = l > 0 ? s->H + (size_t)(l - 1) * hb : s->X;
+        const int pw = l > 0 ? fj::kHid : fj::kIn;
+        if ((rc = sg_transpose(s, B, fj::kHid, dz, s->dZT))) return rc;
+        if ((rc = sg_transpose(s, B, pw, prev, s->HT))) return rc;
+        Epilogue g2{fj::tc::kEpiAtomicF32, nullptr, s->G + s->woff[l], nullptr, nullptr, nullptr, pw, nullptr};
+        if ((rc = sg_gemm(s, s->dZT, B, s->HT, B, fj::kHid, pw, B, ks, g2))) return rc;
+        fj::k_colsum<<<dim3(1, 64), fj::kHid, 0, s->stream>>>(B, fj::kHid, dz, s->G + s->boff[l]);
+        if (l == 0) break;
+        // dZ_{l-1} = (dZ_l W_l) * gelu'(Z_{l-1})
+        Epilogue g3{fj::tc::kEpiGeluGrad, nullptr, nullptr, dz2, nullptr, s->Z + (size_t)(l - 1) * hb, fj::kHid,
+                    nullptr};
+        if ((rc = sg_gemm(s, dz, fj::kHid, s->WbT + s->woff[l], fj::kHid, B, fj::kHid, fj::kHid, 1, g3))) return rc;
+        std::swap(dz, dz2);
+    }
+    return cudaGetLastError() == cudaSuccess ? FJ_OK : FJ_ERR_CUDA;
+}
+
+int sg_check_err(fj_surrogate *s)
+{
+    int h = 0;
+    SG_CUDA(cudaMemcpyAsync(&h, s->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    SG_CUDA(cudaStreamSynchronize(s->stream));
+    return h ? FJ_ERR_CUDA : FJ_OK;
+}
+
+// one training step on rows [r0, r0 + batch) of X f32 [n][16], T f32 [n][2]
+int sg_step(fj_surrogate *s, const float *X, const float *T, float lr)
+{
+    const int B = s->batch;
+    fj::k_to_bf16<<<(B * fj::kIn + 255) / 256, 256, 0, s->stream>>>(B * fj::kIn, X, s->X);
+    int rc;
+    if ((rc = sg_forward(s, s->X, B, s->Y, true, s->H, B))) return rc;
+    if ((rc = sg_backward(s, T))) return rc;
+    s->step++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float alpha = lr * sqrtf(1.f - powf(b2, (float)s->step)) / (1.f - powf(b1, (float)s->step));
+    fj::k_adam<<<(unsigned)((s->nparam + 255) / 256), 256, 0, s->stream>>>((int)s->nparam, s->P, s->G, s->Mom, s->Var,
+                                                                           alpha, b1, b2, 1e-8f, s->mask);
+    return sg_refresh(s);
+}
+
+}  // namespace
+
+extern "C" {
+
+int fj_surrogate_create(fj_ctx *ctx, int batch, unsigned long long seed, fj_surrogate **out)
+{
+    if (!out || batch < 128 || batch % 128) return FJ_ERR_ARG;
+    fj_surrogate *s = new fj_surrogate;
+    s->ctx = ctx;
+    s->stream = ctx ? fj::context_stream(ctx) : nullptr;
+    s->batch = batch;
+    const int rows[5] = {fj::kHid, fj::kHid, fj::kHid, fj::kHid, fj::kOut};
+    const int cols[5] = {fj::kIn, fj::kHid, fj::kHid, fj::kHid, fj::kHid};
+    size_t o = 0;
+    for (int l = 0; l < fj::kLayers; l++) {
+        s->rows[l] = rows[l]; s->cols[l] = cols[l];
+        s->woff[l] = o; o += (size_t)rows[l] * cols[l];
+        s->boff[l] = o; o += rows[l];
+    }
+    s->nparam = o;
+    // seeded initialisation: uniform(-a, a), a = sqrt(6 / (fan_in + fan_out)); zero biases; the
+    // output rows beyond the two used outputs are zero and frozen
+    std::vector<float> p(o, 0.f);
+    std::vector<unsigned char> mask(o, 1);
+    unsigned long long z = seed ? seed : 0x9E3779B97F4A7C15ull;
+    auto uni = [&]() {  // splitmix64
+        z += 0x9E3779B97F4A7C15ull;
+        unsigned long long x = z;
+        x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+        x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+        x ^= x >> 31;
+        return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+    };
+    for (int l = 0; l < fj::kLayers; l++) {
+        const double a = sqrt(6.0 / (rows[l] + cols[l]));
+        for (int r = 0; r < rows[l]; r++)
+            for (int c = 0; c < cols[l]; c++) p[s->woff[l] + (size_t)r * cols[l] + c] = (float)(a * (2 * uni() - 1));
+        if (l == fj::kLayers - 1)
+            for (int r = fj::kUsedOut; r < rows[l]; r++) {
+                for (int c = 0; c < cols[l]; c++) {
+                    p[s->woff[l] + (size_t)r * cols[l] + c] = 0.f;
+                    mask[s->woff[l] + (size_t)r * cols[l] + c] = 0;
+                }
+                mask[s->boff[l] + r] = 0;
+            }
+    }
+    const size_t hb = (size_t)batch * fj::kHid;
+    int rc = FJ_OK;
+    void *q;
+    auto A = [&](void **dst, size_t bytes) { if (!rc) rc = sg_alloc(s, dst, bytes); };
+    A(&q, o * sizeof(float)); s->P = (float *)q;
+    A(&q, o * sizeof(float)); s->G = (float *)q;
+    A(&q, o * sizeof(float)); s->Mom = (float *)q;
+    A(&q, o * sizeof(float)); s->Var = (float *)q;
+    A(&q, o); s->mask = (unsigned char *)q;
+    A(&q, o * sizeof(__nv_bfloat16)); s->Wb = (__nv_bfloat16 *)q;
+    A(&q, o * sizeof(__nv_bfloat16)); s->WbT = (__nv_bfloat16 *)q;
+    A(&q, (size_t)batch * fj::kIn * sizeof(__nv_bfloat16)); s->X = (__nv_bfloat16 *)q;
+    A(&q, 4 * hb * sizeof(__nv_bfloat16)); s->H = (__nv_bfloat16 *)q;
+    A(&q, hb * sizeof(__nv_bfloat16)); s->HT = (__nv_bfloat16 *)q;
+    A(&q, 4 * hb * sizeof(float)); s->Z = (float *)q;
+    A(&q, (3 * hb) * sizeof(__nv_bfloat16)); s->dZ = (__nv_bfloat16 *)q;
+    A(&q, hb * sizeof(__nv_bfloat16)); s->dZT = (__nv_bfloat16 *)q;
+    A(&q, (size_t)batch * fj::kOut * sizeof(float)); s->Y = (float *)q;
+    A(&q, sizeof(float)); s->loss = (float *)q;
+    A(&q, sizeof(int)); s->err = (int *)q;
+    if (!rc && cudaMemcpyAsync(s->P, p.data(), o * sizeof(float), cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
+        rc = FJ_ERR_CUDA;
+    if (!rc && cudaMemcpyAsync(s->mask, mask.data(), o, cudaMemcpyHostToDevice, s->stream) != cudaSuccess)
+        rc = FJ_ERR_CUDA;
+    if (!rc) rc = sg_refresh(s);
+    if (!rc && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = FJ_ERR_CUDA;
+    if (rc) { fj_surrogate_destroy(s); return rc; }
+    *out = s;
+    return FJ_OK;
+}
+
+int fj_surrogate_destroy(fj_surrogate *s)
+{
+    if (!s) return FJ_ERR_ARG;
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (void *p : s->owned) cudaFree(p);
+    delete s;
+    return FJ_OK;
+}
+
+int fj_surrogate_params(fj_surrogate *s, double *host_out, const double *host_in)
+{
+    if (!s) return FJ_ERR_ARG;
+    std::vector<float> p(s->nparam);
+    if (host_in) {
+        for (size_t i = 0; i < s->nparam; i++) p[i] = (float)host_in[i];
+        SG_CUDA(cudaMemcpyAsync(s->P, p.data(), s->nparam * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        int rc = sg_refresh(s);
+        if (rc) return rc;
+    }
+    if (host_out) {
+        SG_CUDA(cudaMemcpyAsync(p.data(), s->P, s->nparam * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+        SG_CUDA(cudaStreamSynchronize(s->stream));
+        for (size_t i = 0; i < s->nparam; i++) host_out[i] = p[i];
+    }
+    SG_CUDA(cudaStreamSynchronize(s->stream));
+    return FJ_OK;
+}
+
+long long fj_surrogate_nparam(const fj_surrogate *s) { return s ? (long long)s->nparam : -1; }
+
+int fj_surrogate_gradients(fj_surrogate *s, const float *X, const float *T, double *grad_out, double *loss)
+{
+    if (!s || !X || !T || !grad_out) return FJ_ERR_ARG;
+    const int B = s->batch;
+    SG_CUDA(cudaMemsetAsync(s->loss, 0, sizeof(float), s->stream));
+    fj::k_to_bf16<<<(B * fj::kIn + 255) / 256, 256, 0, s->stream>>>(B * fj::kIn, X, s->X);
+    int rc;
+    if ((rc = sg_forward(s, s->X, B, s->Y, true, s->H, B))) return rc;
+    if ((rc = sg_backward(s, T))) return rc;
+    if ((rc = sg_check_err(s))) return rc;
+    std::vector<float> g(s->nparam);
+    float l = 0;
+    SG_CUDA(cudaMemcpyAsync(g.data(), s->G, s->nparam * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    SG_CUDA(cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+    SG_CUDA(cudaStreamSynchronize(s->stream));
+    for (size_t i = 0; i < s->nparam; i++) grad_out[i] = g[i];
+    if (loss) *loss = l;
+    return FJ_OK;
+}
+
+int fj_surrogate_train(fj_surrogate *s, const float *X, const float *T, long long n, int epochs, float lr,
+                       double *final_loss)
+{
+    if (!s || !X || !T || n < s->batch || epochs < 1 || !(lr > 0)) return FJ_ERR_ARG;
+    const long long steps = n / s->batch;
+    int rc;
+    for (int e = 0; e < epochs; e++)
+        for (long long k = 0; k < steps; k++) {
+            if (e == epochs - 1 && k == steps - 1) SG_CUDA(cudaMemsetAsync(s->loss, 0, sizeof(float), s->stream));
+            if ((rc = sg_step(s, X + (size_t)k * s->batch * fj::kIn, T + (size_t)k * s->batch * fj::kUsedOut, lr)))
+                return rc;
+        }
+    if ((rc = sg_check_err(s))) return rc;
+    if (final_loss) {
+        float l = 0;
+        SG_CUDA(cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+        SG_CUDA(cudaStreamSynchronize(s->stream));
+        *final_loss = l;
+    }
+    return FJ_OK;
+}
+
+int fj_surrogate_predict(fj_surrogate *s, const float *X, long long n, float *Y)
+{
+    if (!s || !X || !Y || n < 1) return FJ_ERR_ARG;
+    int rc;
+    if (!s->Xi) {  // inference workspace: kInferRows rows per pass
+        void *q;
+        if ((rc = sg_alloc(s, &q, (size_t)kInferRows * fj::kIn * sizeof(__nv_bfloat16)))) return rc;
+        s->Xi = (__nv_bfloat16 *)q;
+        if ((rc = sg_alloc(s, &q, (size_t)2 * kInferRows * fj::kHid * sizeof(__nv_bfloat16)))) return rc;
+        s->Hi = (__nv_bfloat16 *)q;
+    }
+    for (long long r0 = 0; r0 < n; r0 += kInferRows) {
+        const int m = (int)std::min<long long>(kInferRows, n - r0);
+        fj::k_to_bf16<<<(m * fj::kIn + 255) / 256, 256, 0, s->stream>>>(m * fj::kIn, X + (size_t)r0 * fj::kIn, s->Xi);
+        if ((rc = sg_forward(s, s->Xi, m, Y + (size_t)r0 * fj::kOut, false, s->Hi, kInferRows))) return rc;
+    }
+    return sg_check_err(s);
+}
+
+}  // extern "C"
+
+// ======================================================================
+// Surrogate features, targets and the surrogate moment sums.
+//
+// Features of node (i, j, k) of grid point p = (ar[n], cos theta_g) (all
+// exact table values at the grid radius, nothing interpolated):
+//   0: (log r - mu) / sigma over the grid's log-radius range,   1: cos theta,
+//   2, 3, 4: vR / Ve, vz / Ve, vphi / Ve (the node's rule coordinates),
+//   5: Phi_0(r) / Phi_0(ar[0]),   6..12: Phi_l(r) / |Phi_0(r)|, l = 1..7,
+//   13..15: 0.
+// Targets: t = log(J / (r Ve) + 1e-6) for Jr and Jz.  (The escape speed Ve
+// scales the velocities rather than the circular speed, which vanishes at
+// the centre of a cusped model.)
+// ======================================================================
+namespace fj {
+
+constexpr float kSgFloor = 1e-6f;
+
+struct SgGrid {
+    PotView P;
+    const double *ci;  // polar nodes
+    int ngauss, nq;
+    const double *xq;
+    double lmu, lsig;  // log-radius normalisation
+};
+
+__device__ __forceinline__ void sg_point(const SgGrid &g, int p, double &R, double &z, double &Phi_h, double &Ve)
+{
+    const int n = p / g.ngauss, gg = p % g.ngauss;
+    const double c = g.ci[gg], si = sqrt(1 - c * c);
+    R = g.P.ar[n] * si;
+    z = g.P.ar[n] * c;
+    Phi_h = pot_phi(g.P, R, z);
+    const double rmax = g.P.ar[g.P.nr - 1];
+    Ve = sqrt(-2 * (Phi_h - pot_phi(g.P, 10 * rmax, 10 * rmax)));
+}
+
+// features of nodes idx[0..m) (idx = p * nq^3 + node; NULL: rows 0..m-1 are nodes
+// first .. first+m-1), X f32 [m][16]
+__global__ void k_sg_features(SgGrid g, const long long *idx, long long first, long long m, float *X)
+{
+    const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (s >= m) return;
+    const long long id = idx ? idx[s] : first + s;
+    const int nq = g.nq, nq3 = nq * nq * nq;
+    const int p = (int)(id / nq3), node = (int)(id % nq3);
+    const int n = p / g.ngauss, gg = p % g.ngauss, np_ = g.P.npoly;
+    float *x = X + s * 16;
+    x[0] = (float)((log(g.P.ar[n]) - g.lmu) / g.lsig);
+    x[1] = (float)g.ci[gg];
+    x[2] = (float)g.xq[node / (nq * nq)];
+    x[3] = (float)g.xq[node % nq];
+    x[4] = (float)g.xq[(node / nq) % nq];
+    const double p0 = g.P.phil[n * np_];
+    x[5] = (float)(p0 / g.P.phil[0]);
+    for (int l = 1; l < 8; l++) x[5 + l] = l < np_ ? (float)(g.P.phil[n * np_ + l] / fabs(p0)) : 0.f;
+    x[13] = x[14] = x[15] = 0.f;
+}
+
+// training rows from exact actions J [npts * nq^3][2] (unbound: negative):
+// sample s takes node hash(seed, s) (the next bound one after it, within 64)
+__global__ void k_sg_sample(SgGrid g, const float *J, long long total, unsigned long long seed, long long ns,
+                            long long *idx, float *T, int *found)
+{
+    const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (s >= ns) return;
+    unsigned long long h = seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(s + 1);
+    h = (h ^ (h >> 30)) * 0xBF58476D1CE4E5B9ull;
+    h = (h ^ (h >> 27)) * 0x94D049BB133111EBull;
+    h ^= h >> 31;
+    long long id = (long long)(h % (unsigned long long)total);
+    bool ok = false;
+    for (int t = 0; t < 64 && !ok; t++) {
+        const long long q = (id + t) % total;
+        if (J[2 * q] >= 0.f && J[2 * q + 1] >= 0.f) { id = q; ok = true; }
+    }
+    idx[s] = id;
+    if (!ok) { T[2 * s] = T[2 * s + 1] = 0.f; return; }
+    atomicAdd(found, 1);
+    const int nq3 = g.nq * g.nq * g.nq, p = (int)(id / nq3);
+    double R, z, Phi_h, Ve;
+    sg_point(g, p, R, z, Phi_h, Ve);
+    const double sc = g.P.ar[p / g.ngauss] * Ve;
+    T[2 * s] = logf((float)(J[2 * id] / sc) + kSgFloor);
+    T[2 * s + 1] = logf((float)(J[2 * id + 1] / sc) + kSgFloor);
+}
+
+// moment sums of grid point blockIdx.x from the surrogate outputs Y [npts * nq^3][16]
+__global__ void __launch_bounds__(128) k_sg_moments(SgGrid g, const double *wq, DFDev df, const float *Y,
+                                                    long long first, double *partial)
+{
+    __shared__ double s_red[6 * 4];
+    const int p = blockIdx.x, nq = g.nq, nq3 = nq * nq * nq;
+    double R, z, Phi_h, Ve;
+    sg_point(g, p, R, z, Phi_h, Ve);
+    const double sc = g.P.ar[p / g.ngauss] * Ve, jacob = Ve * Ve * Ve;
+    double m[6] = {0, 0, 0, 0, 0, 0};
+    for (int node = threadIdx.x; node < nq3; node += blockDim.x) {
+        const int i = node / (nq * nq), j = (node / nq) % nq, k = node % nq;
+        const double V0 = 1e-6 + Ve * g.xq[i], V1 = 1e-6 + Ve * g.xq[j], V2 = 1e-6 + Ve * g.xq[k];
+        if (!(.5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h < 0)) continue;
+        const float *y = Y + ((long long)p * nq3 + node - first) * 16;
+        const float Jr = fmaxf(0.f, (expf(y[0]) - kSgFloor) * (float)sc);
+        const float Jz = fmaxf(0.f, (expf(y[1]) - kSgFloor) * (float)sc);
+        const float Jphi = (float)(R * V1), J0 = (float)df.J0;
+        const float h = Jr + (float)df.dphi_h * fabsf(Jphi) + (float)df.dz_h * Jz;
+        const float gg = Jr + (float)df.dphi_g * fabsf(Jphi) + (float)df.dz_g * Jz;
+        const float ev = (float)df.norm *
+                         fmaxf(0.f, powf(1.f + J0 / h, (float)df.alpha) / powf(1.f + gg / J0, (float)df.beta)) /
+                         (float)df.tpi3;
+        float f = df.chi == 0. ? ev : ev + (float)df.k * tanhf((float)df.chi * Jphi / J0) * ev;
+        if (isnan(f)) f = 0.f;
+        const double jd = (wq[i] * wq[j] * wq[k]) * (jacob * (double)f);
+        m[0] += jd;
+        m[1] += jd * V1;
+        m[2] += jd * V0 * V0;
+        m[3] += jd * V1 * V1;
+        m[4] += jd * V2 * V2;
+        m[5] += jd * V0 * V2;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int q = 0; q < 6; q++) {
+        double v = m[q];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane == 0) s_red[warp * 6 + q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double s = 0;
+        for (int w = 0; w < 4; w++) s += s_red[w * 6 + threadIdx.x];
+        partial[(size_t)p * 6 + threadIdx.x] = s;
+    }
+}
+
+}  // namespace fj

@@ -157,6 +157,26 @@ int fj_moments_batch(fj_ctx *ctx, int n, const fj_batch_item *items, const fj_qu
 int fj_tc_gemm(int M, int N, int K, const void *A, int lda, const void *B, int ldb, float *C, int ldc, int ksplit,
                void *stream);
 
+/* The action surrogate (no reference counterpart): an MLP 16 -> 128 x 4
+   (GELU) -> 16 mapping normalised phase-space features (13 used, zero padded)
+   to (log Jr, log Jz) (outputs 0 and 1), trained and evaluated with the
+   tensor-core GEMMs: BF16 weights and activations, FP32 accumulation and
+   master weights, Adam.  batch = samples per training step (a multiple of
+   128); work runs on the context's stream.  X device f32 [n][16], T device
+   f32 [n][2] targets, Y device f32 [n][16] outputs.  fj_surrogate_params
+   copies the parameters out (host_out) and/or in (host_in), laid out per
+   layer as W [rows][cols] then b [rows]; fj_surrogate_gradients gives the
+   mean-squared-error gradient of one batch (the first `batch` rows). */
+typedef struct fj_surrogate fj_surrogate;
+int fj_surrogate_create(fj_ctx *ctx, int batch, unsigned long long seed, fj_surrogate **out);
+int fj_surrogate_destroy(fj_surrogate *s);
+long long fj_surrogate_nparam(const fj_surrogate *s);
+int fj_surrogate_params(fj_surrogate *s, double *host_out, const double *host_in);
+int fj_surrogate_gradients(fj_surrogate *s, const float *X, const float *T, double *grad_out, double *loss);
+int fj_surrogate_train(fj_surrogate *s, const float *X, const float *T, long long n, int epochs, float lr,
+                       double *final_loss);
+int fj_surrogate_predict(fj_surrogate *s, const float *X, long long n, float *Y);
+
 /* Configuration of the mixed-precision phase-space kernel (no reference
    counterpart: the reference has one CPU loop).  variant 0..7: 0..3 run each
    node's solve as nested loops, 4..7 in the wavefront form (all lanes of a

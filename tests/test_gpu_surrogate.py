@@ -1,0 +1,100 @@
+"""The action surrogate's tensor-core MLP: forward outputs and mean-squared-error
+gradients against a float32 reference of the same network on the CPU (torch),
+which rounds weights, activations and back-propagated errors to BF16 at the same
+points as the GPU path; then training reduces the loss on a smooth target.
+
+Tolerances: outputs 2e-3 of their scale; each layer's weight and bias gradients
+1e-2 of the layer's largest gradient (BF16 rounding flips near ties and FP32
+summation order)."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import fjmodels_gb300 as F  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+B = 1024
+
+
+def gelu(z):
+    return 0.5 * z * (1 + torch.tanh(0.7978845608028654 * (z + 0.044715 * z ** 3)))
+
+
+def gelu_grad(z):
+    u = 0.7978845608028654 * (z + 0.044715 * z ** 3)
+    t = torch.tanh(u)
+    return 0.5 * (1 + t) + 0.5 * z * (1 - t * t) * 0.7978845608028654 * (1 + 3 * 0.044715 * z * z)
+
+
+def bf(x):
+    return x.bfloat16().float()
+
+
+def reference(layers, X, T):
+    """Forward, loss and gradients in float32 with the GPU's BF16 rounding points."""
+    Wb = [bf(torch.tensor(W, dtype=torch.float32)) for W, _ in layers]
+    bs = [torch.tensor(b, dtype=torch.float32) for _, b in layers]
+    h = bf(X)
+    Hs, Zs = [h], []
+    for l in range(4):
+        z = h @ Wb[l].T + bs[l]
+        Zs.append(z)
+        h = bf(gelu(z))
+        Hs.append(h)
+    y = h @ Wb[4].T + bs[4]
+    d = y[:, :2] - T
+    loss = (d * d).mean()
+    dY = torch.zeros_like(y)
+    dY[:, :2] = 2 * d / d.numel()
+    dY = bf(dY)
+    grads = [None] * 5
+    grads[4] = (dY.T @ Hs[4], dY.sum(0))
+    dz = bf((dY @ Wb[4]) * gelu_grad(Zs[3]))
+    for l in range(3, -1, -1):
+        grads[l] = (dz.T @ Hs[l], dz.sum(0))
+        if l > 0:
+            dz = bf((dz @ Wb[l]) * gelu_grad(Zs[l - 1]))
+    return y, loss.item(), grads
+
+
+def features(n, seed):
+    g = torch.Generator().manual_seed(seed)
+    X = torch.zeros(n, 16)
+    X[:, :13] = torch.randn(n, 13, generator=g)
+    T = torch.stack([torch.sin(X[:, 0]) + 0.5 * X[:, 1] ** 2, torch.cos(X[:, 2]) * X[:, 3]], 1)
+    return X, T
+
+
+def test_forward_and_gradients_vs_cpu(ctx):
+    s = F.Surrogate(ctx, batch=B, seed=7)
+    X, T = features(B, 3)
+    Xd, Td = X.cuda(), T.contiguous().cuda()
+    layers = s.unpack(s.params())
+    y_ref, loss_ref, g_ref = reference(layers, X, T)
+    Y = torch.zeros(B, 16, device="cuda")
+    s.predict(Xd, Y)
+    torch.cuda.synchronize()
+    yc = Y.cpu()
+    assert (yc[:, :2] - y_ref[:, :2]).abs().max().item() <= 2e-3 * y_ref[:, :2].abs().max().item() + 1e-6
+    g, loss = s.gradients(Xd, Td)
+    assert abs(loss - loss_ref) <= 1e-3 * loss_ref
+    for l, ((gW, gb), (W, b)) in enumerate(zip(s.unpack(g), layers)):
+        rW, rb = g_ref[l]
+        scale = max(rW.abs().max().item(), rb.abs().max().item())
+        assert np.abs(gW - rW.numpy()).max() <= 1e-2 * scale, ("W", l)
+        assert np.abs(gb - rb.numpy()).max() <= 1e-2 * scale, ("b", l)
+    s.close()
+
+
+def test_training_reduces_loss(ctx):
+    s = F.Surrogate(ctx, batch=B, seed=11)
+    X, T = features(64 * B, 5)
+    Xd, Td = X.cuda(), T.contiguous().cuda()
+    _, loss0 = s.gradients(Xd, Td)
+    loss = s.train(Xd, Td, epochs=3, lr=2e-3)
+    assert loss < 0.1 * loss0, (loss0, loss)
+    # the frozen padding outputs stay exactly zero
+    p = s.unpack(s.params())
+    assert np.all(p[4][0][2:] == 0) and np.all(p[4][1][2:] == 0)
+    s.close()
