@@ -38,6 +38,7 @@ struct fj_ctx {
     std::vector<double> rule_host;                     // last uploaded velocity rule
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int mixed_variant = 0, mixed_chunk = kMixedMaxNodes;  // mixed kernel configuration (fj_autotune_mixed)
+    float *jout = nullptr;                             // mixed form: actions of every bound node (fj_set_action_output)
     DevBuf batch;                                      // batched launch: MomentArgs[n] | block_start | point_start
     std::vector<char> batch_host;                      // what `batch` holds (re-uploaded only when it changes)
 };
@@ -238,6 +239,7 @@ int build_args(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta
     a.blocks_per_point =
         mixed ? mixed_blocks_per_point(nq3, a.mixed_chunk) : (int)((nq3 + kMomentBlock - 1) / kMomentBlock);
     a.out6 = out6;
+    a.jout = nullptr;
     return FJ_OK;
 }
 
@@ -268,18 +270,40 @@ int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delt
     if ((rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long)))) return rc;
     a.partial = (double *)ctx->partial.p;
     a.counters = (unsigned long long *)ctx->counters.p;
+    const long long nq3 = (long long)rule->nq * rule->nq * rule->nq;
+    if (mixed && ctx->jout) {  // unbound nodes keep the all-ones (NaN) pattern
+        a.jout = ctx->jout;
+        FJ_CUDA(cudaMemsetAsync(a.jout, 0xFF, (size_t)npts * nq3 * 2 * sizeof(float), ctx->stream));
+    }
     FJ_CUDA(cudaMemsetAsync(a.counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     FJ_CUDA(mixed ? launch_moments_mixed(a, ctx->mixed_variant, ctx->stream) : launch_moments(a, ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
-    const long long nq3 = (long long)rule->nq * rule->nq * rule->nq;
     return stats ? read_stats(ctx, nq3 * npts, stats) : FJ_OK;
 }
 
 }  // namespace
 
+namespace fj {
+int context_grid_inputs(fj_ctx *ctx, int ngauss, const fj_quad_rule *rule, const double **ci, const double **xq,
+                        const double **wq)
+{
+    int rc = gauss_nodes(ctx, ngauss, ci);
+    if (rc) return rc;
+    return upload_rule(ctx, rule, xq, wq);
+}
+}  // namespace fj
+
 // =================================================================== ABI
 extern "C" {
+
+int fj_set_action_output(fj_ctx *ctx, float *jout)
+{
+    if (!ctx) return FJ_ERR_ARG;
+    ctx->jout = jout;
+    return FJ_OK;
+}
+
 
 const char *fj_version(void) { return "fjmodels-gb300 0.1 (sm_103a)"; }
 

@@ -7,6 +7,7 @@
 #include "fj_device.cuh"
 
 struct fj_ctx;
+struct fj_quad_rule;
 
 namespace fj {
 
@@ -32,6 +33,7 @@ struct MomentArgs {
     int npts;
     int blocks_per_point;
     int mixed_chunk;         // mixed form: nodes per block (<= kMixedMaxNodes)
+    float *jout;             // mixed form, optional: (Jr, Jz) of every bound node [npts][nq^3][2]
     double *partial;         // [npts][blocks_per_point][6]
     unsigned long long *counters;  // [0] bound nodes, [1] failed nodes, [3] FP64 escalations
     double *out6;            // [6][npts]
@@ -95,8 +97,11 @@ cudaError_t launch_add(int n, const double *a, const double *b, double *o, cudaS
 cudaError_t launch_vir2(PotView P, int ngauss, const double *ci, const double *wi, const double *coef6,
                         double *out7, cudaStream_t s);
 
-// the stream a context orders its work on
+// the stream a context orders its work on; the device copies of a grid's polar
+// nodes and of a velocity rule
 cudaStream_t context_stream(::fj_ctx *ctx);
+int context_grid_inputs(::fj_ctx *ctx, int ngauss, const struct ::fj_quad_rule *rule, const double **ci,
+                        const double **xq, const double **wq);
 // BF16 tensor-core GEMM (fj_mlp.cu): C = A B^T with a fused epilogue
 namespace tc { struct Epilogue; }
 cudaError_t launch_gemm_tc(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb, int M, int N, int K,

@@ -283,6 +283,12 @@ struct fj_surrogate {
     float *Z = nullptr, *Y = nullptr, *loss = nullptr;
     int *err = nullptr;
     __nv_bfloat16 *Xi = nullptr, *Hi = nullptr;  // inference workspace
+    float *Xf = nullptr, *Yf = nullptr;           // f32 features / outputs of one inference pass
+    float *fitX = nullptr, *fitT = nullptr;       // training rows (fj_surrogate_fit), fit_cap rows
+    long long *fitIdx = nullptr;
+    long long fit_cap = 0;
+    double *partial = nullptr;                    // surrogate moment sums [npts][6]
+    long long partial_cap = 0;
     long long step = 0;
     std::vector<void *> owned;
 };
@@ -662,7 +668,7 @@ __global__ void k_sg_sample(SgGrid g, const float *J, long long total, unsigned 
     }
     idx[s] = id;
     if (!ok) { T[2 * s] = T[2 * s + 1] = 0.f; return; }
-    atomicAdd(found, 1);
+    if (found) atomicAdd(found, 1);
     const int nq3 = g.nq * g.nq * g.nq, p = (int)(id / nq3);
     double R, z, Phi_h, Ve;
     sg_point(g, p, R, z, Phi_h, Ve);
@@ -671,12 +677,13 @@ __global__ void k_sg_sample(SgGrid g, const float *J, long long total, unsigned 
     T[2 * s + 1] = logf((float)(J[2 * id + 1] / sc) + kSgFloor);
 }
 
-// moment sums of grid point blockIdx.x from the surrogate outputs Y [npts * nq^3][16]
+// moment sums of grid point p0 + blockIdx.x from the surrogate outputs Y (rows from
+// node `first` of the grid, [.][16])
 __global__ void __launch_bounds__(128) k_sg_moments(SgGrid g, const double *wq, DFDev df, const float *Y,
-                                                    long long first, double *partial)
+                                                    long long first, int p0, double *partial)
 {
     __shared__ double s_red[6 * 4];
-    const int p = blockIdx.x, nq = g.nq, nq3 = nq * nq * nq;
+    const int p = p0 + blockIdx.x, nq = g.nq, nq3 = nq * nq * nq;
     double R, z, Phi_h, Ve;
     sg_point(g, p, R, z, Phi_h, Ve);
     const double sc = g.P.ar[p / g.ngauss] * Ve, jacob = Ve * Ve * Ve;
@@ -719,3 +726,115 @@ __global__ void __launch_bounds__(128) k_sg_moments(SgGrid g, const double *wq, 
 }
 
 }  // namespace fj
+
+namespace {
+
+int sg_grid(fj_surrogate *s, const fj_potential *pot, int ngauss, const fj_quad_rule *rule, fj::SgGrid &g)
+{
+    if (!s->ctx || !pot || !rule || ngauss < 1 || pot->nr < 2 || pot->npoly < 1) return FJ_ERR_ARG;
+    const double *ci, *xq, *wq;
+    int rc = fj::context_grid_inputs(s->ctx, ngauss, rule, &ci, &xq, &wq);
+    if (rc) return rc;
+    std::vector<double> ar2(2);
+    SG_CUDA(cudaMemcpyAsync(ar2.data(), pot->ar, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    SG_CUDA(cudaMemcpyAsync(ar2.data() + 1, pot->ar + pot->nr - 1, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    SG_CUDA(cudaStreamSynchronize(s->stream));
+    g.P = fj::PotView{pot->nr, pot->npoly, pot->ar, pot->phil, pot->Pr, pot->Pr2};
+    g.ci = ci; g.ngauss = ngauss; g.nq = rule->nq; g.xq = xq;
+    g.lmu = .5 * (log(ar2[0]) + log(ar2[1]));
+    g.lsig = .5 * (log(ar2[1]) - log(ar2[0]));
+    return FJ_OK;
+}
+
+int sg_infer_buffers(fj_surrogate *s)
+{
+    int rc;
+    void *q;
+    if (!s->Xf) {
+        if ((rc = sg_alloc(s, &q, (size_t)kInferRows * fj::kIn * sizeof(float)))) return rc;
+        s->Xf = (float *)q;
+        if ((rc = sg_alloc(s, &q, (size_t)kInferRows * fj::kOut * sizeof(float)))) return rc;
+        s->Yf = (float *)q;
+    }
+    return FJ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fj_surrogate_fit(fj_surrogate *s, const fj_potential *pot, int ngauss, const fj_quad_rule *rule, const float *J,
+                     long long nsamples, unsigned long long seed, int epochs, float lr, double *loss)
+{
+    if (!s || !J || nsamples < s->batch || epochs < 1) return FJ_ERR_ARG;
+    fj::SgGrid g;
+    int rc = sg_grid(s, pot, ngauss, rule, g);
+    if (rc) return rc;
+    const long long ns = nsamples / s->batch * s->batch;
+    if (ns > s->fit_cap) {
+        void *q;
+        if ((rc = sg_alloc(s, &q, (size_t)ns * fj::kIn * sizeof(float)))) return rc;
+        s->fitX = (float *)q;
+        if ((rc = sg_alloc(s, &q, (size_t)ns * fj::kUsedOut * sizeof(float)))) return rc;
+        s->fitT = (float *)q;
+        if ((rc = sg_alloc(s, &q, (size_t)ns * sizeof(long long)))) return rc;
+        s->fitIdx = (long long *)q;
+        s->fit_cap = ns;
+    }
+    const long long total = (long long)pot->nr * ngauss * rule->nq * rule->nq * rule->nq;
+    fj::k_sg_sample<<<(unsigned)((ns + 255) / 256), 256, 0, s->stream>>>(g, J, total, seed, ns, s->fitIdx, s->fitT,
+                                                                         nullptr);
+    fj::k_sg_features<<<(unsigned)((ns + 255) / 256), 256, 0, s->stream>>>(g, s->fitIdx, 0, ns, s->fitX);
+    return fj_surrogate_train(s, s->fitX, s->fitT, ns, epochs, lr, loss);
+}
+
+int fj_surrogate_moments(fj_surrogate *s, const fj_potential *pot, const fj_df_params *df, const fj_quad_rule *rule,
+                         int ngauss, double *grids6, double *ms)
+{
+    if (!s || !df || !grids6 || df->kind != FJ_DF_DPL) return FJ_ERR_ARG;
+    fj::SgGrid g;
+    int rc = sg_grid(s, pot, ngauss, rule, g);
+    if (rc) return rc;
+    if ((rc = sg_infer_buffers(s))) return rc;
+    const double *ci, *xq, *wq;
+    if ((rc = fj::context_grid_inputs(s->ctx, ngauss, rule, &ci, &xq, &wq))) return rc;
+    const int npts = pot->nr * ngauss, nq3 = rule->nq * rule->nq * rule->nq;
+    if (npts > s->partial_cap) {
+        void *q;
+        if ((rc = sg_alloc(s, &q, (size_t)npts * 6 * sizeof(double)))) return rc;
+        s->partial = (double *)q;
+        s->partial_cap = npts;
+    }
+    if (nq3 > kInferRows) return FJ_ERR_ARG;
+    const int per = kInferRows / nq3;  // whole grid points per inference pass
+    fj::DFDev d;
+    d.kind = df->kind; d.alpha = df->alpha; d.beta = df->beta; d.J0 = df->J0;
+    d.norm = df->mass / pow(df->J0, 3); d.tpi3 = pow(2 * fj::kPI, 3.);
+    d.dphi_h = df->dphi_h; d.dz_h = df->dz_h; d.dphi_g = df->dphi_g; d.dz_g = df->dz_g; d.chi = df->chi; d.k = df->k;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s->stream);
+    for (int p0 = 0; p0 < npts; p0 += per) {
+        const int np = std::min(per, npts - p0);
+        const long long first = (long long)p0 * nq3, m = (long long)np * nq3;
+        fj::k_sg_features<<<(unsigned)((m + 255) / 256), 256, 0, s->stream>>>(g, nullptr, first, m, s->Xf);
+        fj::k_to_bf16<<<(unsigned)((m * fj::kIn + 255) / 256), 256, 0, s->stream>>>((int)(m * fj::kIn), s->Xf, s->Xi);
+        if ((rc = sg_forward(s, s->Xi, (int)m, s->Yf, false, s->Hi, kInferRows))) return rc;
+        fj::k_sg_moments<<<np, 128, 0, s->stream>>>(g, wq, d, s->Yf, first, p0, s->partial);
+    }
+    cudaEventRecord(e1, s->stream);
+    fj::MomentArgs a{};
+    a.partial = s->partial; a.npts = npts; a.blocks_per_point = 1; a.out6 = grids6;
+    if (fj::launch_moments_finalize(a, s->stream) != cudaSuccess) return FJ_ERR_CUDA;
+    if ((rc = sg_check_err(s))) return rc;
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ms) *ms = t;
+    return FJ_OK;
+}
+
+}  // extern "C"
+

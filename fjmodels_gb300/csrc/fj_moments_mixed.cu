@@ -125,7 +125,13 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
         int q = threadIdx.x;
         double V0 = 0, V1 = 0, V2 = 0, wj = 0;
         bool active = false;
+        int cur_node = 0;
         auto accumulate = [&]() {
+            if (a.jout) {
+                float *jo = a.jout + ((size_t)p * nq3 + cur_node) * 2;
+                jo[0] = (float)L.Jr;
+                jo[1] = (float)L.Jz;
+            }
             failed += L.fail ? 1u : 0u;
             esc += L.esc;
             const double DF = (L.fail & (kFailBracket | kFailRoot)) ? 0. : L.df(a.df);
@@ -140,6 +146,7 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
         auto next = [&]() {  // the lane's next node with a pending request, or none
             while (q < nbound) {
                 const int node = n0 + s_list[q];
+                cur_node = node;
                 q += kMixedBlock;
                 const int i = node / nq2, j = (node / nq) % nq, k = node % nq;
                 V0 = 1e-6 + Ve * s_xq[i]; V1 = 1e-6 + Ve * s_xq[j]; V2 = 1e-6 + Ve * s_xq[k];
@@ -169,7 +176,13 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
         const double H = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h;
         unsigned fail = 0, e = 0;
         const double Delta = deltafn(s_Eg, s_Dg, a.ngrid, H);
-        const double f = mixed_node_df(P, PF, *sK, a.df, Delta, R, z, Phi_h, V0, V1, V2, fail, e);
+        double J[2];
+        const double f = mixed_node_df(P, PF, *sK, a.df, Delta, R, z, Phi_h, V0, V1, V2, fail, e, J);
+        if (a.jout) {
+            float *jo = a.jout + ((size_t)p * nq3 + node) * 2;
+            jo[0] = (float)J[0];
+            jo[1] = (float)J[1];
+        }
         esc += e;
         failed += fail ? 1u : 0u;
         const double DF = (fail & (kFailBracket | kFailRoot)) ? 0. : f;

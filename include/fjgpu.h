@@ -167,6 +167,12 @@ int fj_tc_gemm(int M, int N, int K, const void *A, int lda, const void *B, int l
    copies the parameters out (host_out) and/or in (host_in), laid out per
    layer as W [rows][cols] then b [rows]; fj_surrogate_gradients gives the
    mean-squared-error gradient of one batch (the first `batch` rows). */
+/* Mixed form: also write (Jr, Jz) of every bound velocity node of the grid
+   (device f32 [npts][nq^3][2], point-major as the grid; unbound nodes are
+   left NaN) on subsequent fj_moments / fj_moments_points / fj_compute_new_phi
+   calls of this context; NULL turns it off.  Feeds fj_surrogate_fit. */
+int fj_set_action_output(fj_ctx *ctx, float *jout);
+
 typedef struct fj_surrogate fj_surrogate;
 int fj_surrogate_create(fj_ctx *ctx, int batch, unsigned long long seed, fj_surrogate **out);
 int fj_surrogate_destroy(fj_surrogate *s);
