@@ -43,6 +43,18 @@ class fj_batch_item(C.Structure):
                 ("grids6", C.c_void_p)]
 
 
+class fj_surrogate_schedule(C.Structure):
+    _fields_ = [("exact_first", C.c_int), ("exact_last", C.c_int), ("samples", C.c_longlong),
+                ("epochs_first", C.c_int), ("epochs", C.c_int), ("lr", C.c_float), ("seed", C.c_ulonglong),
+                ("r_exact", C.c_double), ("audit_stride", C.c_int), ("audit_tol", C.c_double)]
+
+
+class fj_surrogate_report(C.Structure):
+    _fields_ = [("surrogate_iterations", C.c_int), ("fallback_iterations", C.c_int), ("fits", C.c_int),
+                ("last_audit_err", C.c_double), ("max_audit_err", C.c_double), ("last_fit_loss", C.c_double),
+                ("surrogate_ms", C.c_double), ("exact_ms", C.c_double), ("fit_ms", C.c_double)]
+
+
 class fj_model_config(C.Structure):
     _fields_ = [("nr", C.c_int), ("ngauss", C.c_int), ("npoly", C.c_int), ("ngrid", C.c_int),
                 ("rmin", C.c_double), ("rmax", C.c_double), ("guess", C.c_int),
@@ -85,6 +97,13 @@ SIGNATURES = {
     "fj_surrogate_gradients": ([C.c_void_p, C.c_void_p, C.c_void_p, DP, DP], C.c_int),
     "fj_surrogate_train": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_longlong, C.c_int, C.c_float, DP], C.c_int),
     "fj_surrogate_predict": ([C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p], C.c_int),
+    "fj_set_action_output": ([CTX, C.c_void_p], C.c_int),
+    "fj_surrogate_fit": ([C.c_void_p, P(fj_potential), C.c_int, P(fj_quad_rule), C.c_void_p, C.c_longlong,
+                          C.c_ulonglong, C.c_int, C.c_float, DP], C.c_int),
+    "fj_surrogate_moments": ([C.c_void_p, P(fj_potential), P(fj_df_params), P(fj_quad_rule), C.c_int, C.c_void_p,
+                              DP], C.c_int),
+    "fj_run_model_surrogate": ([CTX, P(fj_model_config), P(fj_surrogate_schedule), C.c_void_p, P(fj_model_result),
+                                P(fj_surrogate_report)], C.c_int),
     "fj_set_mixed_config": ([CTX, C.c_int, C.c_int], C.c_int),
     "fj_get_mixed_config": ([CTX, P(C.c_int), P(C.c_int)], C.c_int),
     "fj_autotune_mixed": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule), C.c_void_p,

@@ -183,6 +183,35 @@ class Context:
                     "fj_moments_batch")
         return st
 
+    def set_action_output(self, jout):
+        """Mixed form: write every bound node's (Jr, Jz) into jout (device f32 [npts][nq^3][2]); None: off."""
+        self._check(self.lib.fj_set_action_output(self.h, _ptr(jout) if jout is not None else None),
+                    "fj_set_action_output")
+
+    def run_model_surrogate(self, nr, ngauss, npoly, rmin, rmax, df, rule, itermax, surrogate, tol=0.0, ngrid=30,
+                            q=1.0, delta_table=None, exact_first=1, exact_last=3, samples=1 << 20, epochs_first=8,
+                            epochs=2, lr=1e-3, seed=1, r_exact=None, audit_stride=100, audit_tol=1e-2):
+        """The self-consistent loop with the action surrogate in the middle iterations
+        (fj_run_model_surrogate); returns (result dict as run_model, report dict)."""
+        self.use_own_stream()
+        din = [None, None] if delta_table is None else [_f64(delta_table[0]), _f64(delta_table[1])]
+        cfg = A.fj_model_config(nr, ngauss, npoly, ngrid, rmin, rmax, A.FJ_GUESS.get(df.model, 0), df.mass, df.r0,
+                                q, df.c, rule.c, itermax, tol, *[_dp(d) if d is not None else None for d in din])
+        sch = A.fj_surrogate_schedule(exact_first, exact_last, samples, epochs_first, epochs, lr, seed,
+                                      0.05 * df.r0 if r_exact is None else r_exact, audit_stride, audit_tol)
+        out = {"ar": np.zeros(nr), "coef6": np.zeros((6, nr, npoly)), "phil": np.zeros((nr, npoly)),
+               "Pr": np.zeros((nr, npoly)), "Pr2": np.zeros((nr, npoly)), "Egrid": np.zeros(ngrid),
+               "Dgrid": np.zeros(ngrid), "grids6": np.zeros((6, nr, ngauss))}
+        res = A.fj_model_result(*[_dp(out[k]) for k in ("ar", "coef6", "phil", "Pr", "Pr2", "Egrid", "Dgrid",
+                                                        "grids6")])
+        rep = A.fj_surrogate_report()
+        self._check(self.lib.fj_run_model_surrogate(self.h, C.byref(cfg), C.byref(sch), surrogate.h, C.byref(res),
+                                                    C.byref(rep)), "fj_run_model_surrogate")
+        out.update(vir7=np.array(res.vir7[:]), iterations=res.iterations, last_change=res.last_change,
+                   bound=res.bound, failures=res.failures, wall_ms=res.wall_ms, kernel_ms=res.kernel_ms,
+                   setup_ms=res.setup_ms)
+        return out, {f: getattr(rep, f) for f, _ in A.fj_surrogate_report._fields_}
+
     def run_model_batch(self, models, rule, itermax, tol=0.0, ngrid=30, use_graph=True):
         """Several one-component models iterated together (fj_run_model_batch).  models = list of
         dicts with nr, ngauss, npoly, rmin, rmax, df (DFParams) and optional q, delta_table."""
@@ -485,6 +514,18 @@ class Surrogate:
         self._rc(self.lib.fj_surrogate_train(self.h, _ptr(X), _ptr(T), X.shape[0], epochs, lr, _dp(loss)),
                  "fj_surrogate_train")
         return float(loss[0])
+
+    def fit(self, pot, ngauss, rule, jout, samples, seed=1, epochs=1, lr=1e-3):
+        loss = np.zeros(1)
+        self._rc(self.lib.fj_surrogate_fit(self.h, C.byref(pot.c), ngauss, C.byref(rule.c), _ptr(jout), samples,
+                                           seed, epochs, lr, _dp(loss)), "fj_surrogate_fit")
+        return float(loss[0])
+
+    def moments(self, pot, df, rule, ngauss, grids6):
+        ms = np.zeros(1)
+        self._rc(self.lib.fj_surrogate_moments(self.h, C.byref(pot.c), C.byref(df.c), C.byref(rule.c), ngauss,
+                                               _ptr(grids6), _dp(ms)), "fj_surrogate_moments")
+        return float(ms[0])
 
     def predict(self, X, Y):
         self._rc(self.lib.fj_surrogate_predict(self.h, _ptr(X), X.shape[0], _ptr(Y)), "fj_surrogate_predict")

@@ -1217,3 +1217,176 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
     }
     return FJ_OK;
 }
+
+// ------------------------------------------------------------ surrogate loop
+extern "C" int fj_run_model_surrogate(fj_ctx *ctx, const fj_model_config *cfg, const fj_surrogate_schedule *sch,
+                                      fj_surrogate *sg, fj_model_result *res, fj_surrogate_report *rep)
+{
+    if (!ctx || !cfg || !sch || !sg || !res || !res->ar || !res->coef6 || !res->phil || !res->Pr || !res->Pr2 ||
+        !res->Egrid || !res->Dgrid)
+        return fail(ctx, FJ_ERR_ARG, "run_model_surrogate: missing arguments");
+    const int nr = cfg->nr, ng = cfg->ngauss, npl = cfg->npoly, ngrid = cfg->ngrid, nt = nr * npl;
+    if (nr < 11 || ng < 1 || npl < 1 || npl > kMaxPoly || ngrid < 2 || cfg->itermax < 1 || cfg->ncomp > 1 ||
+        cfg->rule.precision != FJ_PREC_MIXED || cfg->df.kind != FJ_DF_DPL || sch->exact_first < 1 ||
+        sch->exact_last < 0 || sch->audit_stride < 1 || sch->samples < 1 || sch->epochs_first < 1 || sch->epochs < 1)
+        return fail(ctx, FJ_ERR_ARG, "run_model_surrogate: needs one DPL component, the mixed rule and a valid schedule");
+    fj_surrogate_report rp{};
+    auto now = [] { return std::chrono::steady_clock::now(); };
+    auto ms_since = [](std::chrono::steady_clock::time_point t) {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t).count();
+    };
+    auto t0 = now();
+    int rc;
+    if ((rc = fj_log_grid(cfg->rmin, cfg->rmax, nr, res->ar))) return fail(ctx, rc, "run_model_surrogate: grid");
+    std::vector<double> rhl(nt);
+    if ((rc = fj_guess_rhl(nr, ng, npl, res->ar, cfg->guess, cfg->mass, cfg->r0, cfg->q, rhl.data())))
+        return fail(ctx, rc, "run_model_surrogate: guess");
+    const int npts = nr * ng;
+    const long long nq3 = (long long)cfg->rule.nq * cfg->rule.nq * cfg->rule.nq;
+    // exact points: r < r_exact, and the audit points (every audit_stride-th of the rest)
+    std::vector<double> ci(ng), wi(ng);
+    gauleg_host(0., 1., ng, ci.data(), wi.data());
+    std::vector<int> ex_idx, audit;
+    std::vector<double> ex_rz;
+    for (int p = 0; p < npts; p++) {
+        const int n = p / ng, g = p % ng;
+        const bool inner = res->ar[n] < sch->r_exact, aud = !inner && p % sch->audit_stride == 0;
+        if (!inner && !aud) continue;
+        if (aud) audit.push_back((int)ex_idx.size());
+        ex_idx.push_back(p);
+        ex_rz.push_back(res->ar[n] * sqrt(1 - ci[g] * ci[g]));
+        ex_rz.push_back(res->ar[n] * ci[g]);
+    }
+    const int ne = (int)ex_idx.size();
+    // device: ar | rhl | pot A, B | Eg | Dg | grids6 | coef6 | exact Rz | exact out6 ; actions (floats) ; exact index
+    const size_t nd = nr + nt + 6 * (size_t)nt + 2 * ngrid + 6 * (size_t)npts + 6 * (size_t)nt + 2 * (size_t)ne +
+                      6 * (size_t)ne;
+    double *dbuf = nullptr;
+    float *jout = nullptr;
+    int *d_idx = nullptr;
+    FJ_CUDA(cudaMalloc(&dbuf, nd * sizeof(double)));
+    struct Free {
+        double *p; float *j; int *i;
+        ~Free() { cudaFree(p); cudaFree(j); cudaFree(i); }
+    } guard{dbuf, nullptr, nullptr};
+    FJ_CUDA(cudaMalloc(&jout, (size_t)npts * nq3 * 2 * sizeof(float)));
+    guard.j = jout;
+    FJ_CUDA(cudaMalloc(&d_idx, (ne > 0 ? ne : 1) * sizeof(int)));
+    guard.i = d_idx;
+    double *d_ar = dbuf, *d_rhl = d_ar + nr, *potA = d_rhl + nt, *potB = potA + 3 * nt, *d_Eg = potB + 3 * nt,
+           *d_Dg = d_Eg + ngrid, *d_grids = d_Dg + ngrid, *d_coef = d_grids + 6 * (size_t)npts,
+           *d_exrz = d_coef + 6 * (size_t)nt, *d_ex6 = d_exrz + 2 * (size_t)ne;
+    cudaStream_t s = ctx->stream;
+    FJ_CUDA(cudaMemcpyAsync(d_ar, res->ar, nr * sizeof(double), cudaMemcpyHostToDevice, s));
+    FJ_CUDA(cudaMemcpyAsync(d_rhl, rhl.data(), nt * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (ne) {
+        FJ_CUDA(cudaMemcpyAsync(d_exrz, ex_rz.data(), 2 * ne * sizeof(double), cudaMemcpyHostToDevice, s));
+        FJ_CUDA(cudaMemcpyAsync(d_idx, ex_idx.data(), ne * sizeof(int), cudaMemcpyHostToDevice, s));
+    }
+    if ((rc = fj_poisson(ctx, nr, npl, d_ar, d_rhl, potA, potA + nt, potA + 2 * nt))) return rc;
+    std::vector<double> hp(3 * nt);
+    FJ_CUDA(cudaMemcpyAsync(hp.data(), potA, 3 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FJ_CUDA(cudaStreamSynchronize(s));
+    fj_potential hpot{nr, npl, res->ar, hp.data(), hp.data() + nt, hp.data() + 2 * nt};
+    if (cfg->Egrid_in && cfg->Dgrid_in) {
+        memcpy(res->Egrid, cfg->Egrid_in, ngrid * sizeof(double));
+        memcpy(res->Dgrid, cfg->Dgrid_in, ngrid * sizeof(double));
+    } else fj_tabulate_delta(&hpot, ngrid, res->Egrid, res->Dgrid);
+    FJ_CUDA(cudaMemcpyAsync(d_Eg, res->Egrid, ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+    FJ_CUDA(cudaMemcpyAsync(d_Dg, res->Dgrid, ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+    const fj_delta_table dt{ngrid, d_Eg, d_Dg};
+    double *cur = potA, *nxt = potB;
+    std::vector<double> old(nt), neu(nt), ex6(6 * (size_t)ne), sg6(6 * (size_t)npts);
+    memcpy(old.data(), hp.data(), nt * sizeof(double));
+    res->bound = res->failures = 0;
+    res->kernel_ms = 0;
+    res->last_change = -1;
+    FJ_CUDA(cudaStreamSynchronize(s));
+    res->setup_ms = ms_since(t0);
+    int k = 0;
+    for (k = 0; k < cfg->itermax; k++) {
+        const fj_potential pot{nr, npl, d_ar, cur, cur + nt, cur + 2 * nt};
+        bool exact = k < sch->exact_first || k >= cfg->itermax - sch->exact_last;
+        if (!exact) {
+            auto ts = now();
+            double sms = 0;
+            if ((rc = fj_surrogate_moments(sg, &pot, &cfg->df, &cfg->rule, ng, d_grids, &sms)))
+                return fail(ctx, rc, "run_model_surrogate: surrogate moments");
+            double err = 0;
+            if (ne) {
+                fj_moment_stats st;
+                if ((rc = run_moments(ctx, &pot, &dt, &cfg->df, &cfg->rule, 0, d_exrz, ne, d_ex6, &st))) return rc;
+                res->bound += st.bound;
+                res->failures += st.failures;
+                FJ_CUDA(cudaMemcpyAsync(ex6.data(), d_ex6, ne * sizeof(double), cudaMemcpyDeviceToHost, s));
+                FJ_CUDA(cudaMemcpyAsync(sg6.data(), d_grids, npts * sizeof(double), cudaMemcpyDeviceToHost, s));
+                FJ_CUDA(cudaStreamSynchronize(s));
+                for (int a : audit)
+                    if (ex6[a] > 0) err = fmax(err, fabs(sg6[ex_idx[a]] - ex6[a]) / ex6[a]);
+                FJ_CUDA(launch_scatter6(ne, d_idx, d_ex6, npts, d_grids, s));
+            }
+            rp.last_audit_err = err;
+            rp.max_audit_err = fmax(rp.max_audit_err, err);
+            if (err > sch->audit_tol) {
+                exact = true;
+                rp.fallback_iterations++;
+            } else {
+                if ((rc = fj_legendre_project(ctx, nr, ng, npl, d_ar, d_grids, d_coef))) return rc;
+                if ((rc = fj_poisson(ctx, nr, npl, d_ar, d_coef, nxt, nxt + nt, nxt + 2 * nt))) return rc;
+                rp.surrogate_iterations++;
+            }
+            FJ_CUDA(cudaStreamSynchronize(s));
+            rp.surrogate_ms += ms_since(ts);
+        }
+        if (exact) {
+            auto ts = now();
+            // fit while a surrogate iteration is still ahead
+            const bool fit = k + 1 < cfg->itermax - sch->exact_last;
+            fj_set_action_output(ctx, fit ? jout : nullptr);
+            fj_moment_stats st;
+            rc = fj_compute_new_phi(ctx, &pot, &dt, &cfg->df, &cfg->rule, ng, d_grids, d_coef, nxt, nxt + nt,
+                                    nxt + 2 * nt, &st);
+            fj_set_action_output(ctx, nullptr);
+            if (rc) return rc;
+            res->bound += st.bound;
+            res->failures += st.failures;
+            res->kernel_ms += st.kernel_ms;
+            FJ_CUDA(cudaStreamSynchronize(s));
+            rp.exact_ms += ms_since(ts);
+            if (fit) {
+                auto tf = now();
+                double loss = 0;
+                if ((rc = fj_surrogate_fit(sg, &pot, ng, &cfg->rule, jout, sch->samples, sch->seed + (unsigned)k,
+                                           rp.fits ? sch->epochs : sch->epochs_first, sch->lr, &loss)))
+                    return fail(ctx, rc, "run_model_surrogate: fit");
+                rp.fits++;
+                rp.last_fit_loss = loss;
+                rp.fit_ms += ms_since(tf);
+            }
+        }
+        FJ_CUDA(cudaMemcpyAsync(neu.data(), nxt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+        FJ_CUDA(cudaStreamSynchronize(s));
+        double maxd = 0;
+        for (int i = 0; i < nr; i++)
+            for (int j = 0; j < npl; j++)
+                maxd = fmax(maxd, fabs((neu[i * npl + j] - old[i * npl + j]) / neu[i * npl]));
+        res->last_change = maxd;
+        old.swap(neu);
+        std::swap(cur, nxt);
+        if (cfg->tol > 0 && maxd < cfg->tol && k >= cfg->itermax - sch->exact_last) { k++; break; }
+    }
+    res->iterations = k;
+    const fj_potential pot{nr, npl, d_ar, cur, cur + nt, cur + 2 * nt};
+    if ((rc = fj_vir2(ctx, &pot, ng, d_coef, res->vir7))) return rc;
+    FJ_CUDA(cudaMemcpyAsync(res->coef6, d_coef, 6 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FJ_CUDA(cudaMemcpyAsync(res->phil, cur, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FJ_CUDA(cudaMemcpyAsync(res->Pr, cur + nt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FJ_CUDA(cudaMemcpyAsync(res->Pr2, cur + 2 * nt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (res->grids6)
+        FJ_CUDA(cudaMemcpyAsync(res->grids6, d_grids, 6 * (size_t)npts * sizeof(double), cudaMemcpyDeviceToHost, s));
+    FJ_CUDA(cudaStreamSynchronize(s));
+    res->wall_ms = ms_since(t0);
+    if (rep) *rep = rp;
+    return FJ_OK;
+}
+

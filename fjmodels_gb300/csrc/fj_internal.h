@@ -66,6 +66,8 @@ cudaError_t launch_moments(const MomentArgs &a, cudaStream_t s);
 cudaError_t launch_moments_batch(const MomentArgs &a0, const MomentBatch &b, int nblocks, size_t smem, bool mixed,
                                  int variant, cudaStream_t s);
 cudaError_t launch_moments_finalize_batch(const MomentBatch &b, int npoints, cudaStream_t s);
+// dst6[q][idx[t]] = src6[q][t] (moments of n points into a grid of npts)
+cudaError_t launch_scatter6(int n, const int *idx, const double *src6, int npts, double *dst6, cudaStream_t s);
 // the per-point sums of the block partials (shared by both forms)
 cudaError_t launch_moments_finalize(const MomentArgs &a, cudaStream_t s);
 // mixed-precision form (FJ_PREC_MIXED, double-power-law DF, QAGS momentum

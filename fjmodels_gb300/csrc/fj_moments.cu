@@ -144,6 +144,19 @@ __global__ void k_moments_finalize_batch(MomentBatch batch, int npoints)
     finalize_point(a.partial, a.npts, a.blocks_per_point, a.out6, t - batch.point_start[m]);
 }
 
+__global__ void k_scatter6(int n, const int *idx, const double *src6, int npts, double *dst6)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    for (int q = 0; q < 6; q++) dst6[(size_t)q * npts + idx[t]] = src6[(size_t)q * n + t];
+}
+
+cudaError_t launch_scatter6(int n, const int *idx, const double *src6, int npts, double *dst6, cudaStream_t s)
+{
+    k_scatter6<<<(n + 127) / 128, 128, 0, s>>>(n, idx, src6, npts, dst6);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_moments_finalize_batch(const MomentBatch &b, int npoints, cudaStream_t s)
 {
     k_moments_finalize_batch<<<(npoints + 127) / 128, 128, 0, s>>>(b, npoints);

@@ -182,6 +182,16 @@ int fj_surrogate_gradients(fj_surrogate *s, const float *X, const float *T, doub
 int fj_surrogate_train(fj_surrogate *s, const float *X, const float *T, long long n, int epochs, float lr,
                        double *final_loss);
 int fj_surrogate_predict(fj_surrogate *s, const float *X, long long n, float *Y);
+/* Fit to the exact actions J of a grid iteration (from fj_set_action_output,
+   in potential pot): `samples` rows drawn with `seed` among bound nodes,
+   features built on the device, `epochs` of Adam at lr. */
+int fj_surrogate_fit(fj_surrogate *s, const fj_potential *pot, int ngauss, const fj_quad_rule *rule, const float *J,
+                     long long samples, unsigned long long seed, int epochs, float lr, double *loss);
+/* computeRhl with the surrogate's actions: features of every velocity node
+   of the grid, the MLP on the tensor cores, the double-power-law DF and the
+   moment sums into grids6 device [6][nr*ngauss]; ms = device time. */
+int fj_surrogate_moments(fj_surrogate *s, const fj_potential *pot, const fj_df_params *df, const fj_quad_rule *rule,
+                         int ngauss, double *grids6, double *ms);
 
 /* Configuration of the mixed-precision phase-space kernel (no reference
    counterpart: the reference has one CPU loop).  variant 0..7: 0..3 run each
@@ -345,6 +355,37 @@ int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_result *res);
    kernel_ms (eager iterations only), bound and failures, which are totals of
    the batch. */
 int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfgs, fj_model_result *res, int use_graph);
+
+/* Surrogate-accelerated self-consistent loop (no reference counterpart).
+   Iterations [0, exact_first) and the last exact_last run the mixed-precision
+   phase-space kernel and fit the surrogate to that iteration's exact actions
+   (samples rows, seeded; epochs_first Adam epochs on the first fit, epochs
+   later); the iterations between use the surrogate's actions, except at grid
+   points with r < r_exact, which keep the exact kernel, and with an audit:
+   every audit_stride-th grid point is also computed exactly and, if the
+   largest relative density difference there exceeds audit_tol, the iteration
+   is redone exactly (a fallback).  cfg as fj_run_model (mixed rule,
+   double-power-law DF, one component). */
+typedef struct fj_surrogate_schedule {
+    int exact_first, exact_last;
+    long long samples;
+    int epochs_first, epochs;
+    float lr;
+    unsigned long long seed;
+    double r_exact;
+    int audit_stride;
+    double audit_tol;
+} fj_surrogate_schedule;
+
+typedef struct fj_surrogate_report {
+    int surrogate_iterations, fallback_iterations, fits;
+    double last_audit_err, max_audit_err, last_fit_loss;
+    double surrogate_ms, exact_ms, fit_ms;  /* wall time in each kind of step */
+} fj_surrogate_report;
+
+int fj_run_model_surrogate(fj_ctx *ctx, const fj_model_config *cfg, const fj_surrogate_schedule *sch,
+                           fj_surrogate *sg, fj_model_result *res, fj_surrogate_report *rep);
+
 
 #ifdef __cplusplus
 }

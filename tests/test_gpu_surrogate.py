@@ -98,3 +98,65 @@ def test_training_reduces_loss(ctx):
     p = s.unpack(s.params())
     assert np.all(p[4][0][2:] == 0) and np.all(p[4][1][2:] == 0)
     s.close()
+
+
+def _nfw_80_tanh():
+    nr, ng, npl = 80, 40, 7
+    ar = F.log_grid(1e-3, 300.0, nr)
+    from oracle import oracle as O
+    phil, Pr, Pr2 = O.compute_phil(ar, F.guess_rhl(ar, ng, npl, "NFW"))
+    E, D, _ = F.tabulate_delta(ar, phil, Pr, Pr2)
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda")  # noqa: E731
+    return (nr, ng, npl), [dev(t) for t in (ar, phil, Pr, Pr2)], (dev(E), dev(D))
+
+
+def test_surrogate_moments_gain(ctx):
+    """Fit to one exact iteration of the 80 x 40 rotating NFW workload (22^3 tanh-sinh
+    nodes), then the surrogate's grid of moments: much faster than the exact mixed
+    kernel, densities within a few per cent (the surrogate serves the early
+    iterations only; the last ones are exact)."""
+    from fjmodels_gb300 import _abi as A
+    (nr, ng, npl), tabs, (E, D) = _nfw_80_tanh()
+    pot, delta = ctx.potential(*tabs), ctx.delta(E, D)
+    df = F.DFParams("NFW", chi=1.0, k=0.5)
+    rule = F.Rule(*F.tanh_sinh_rule(22), precision=A.FJ_PREC_MIXED)
+    npts, nq3 = nr * ng, 22 ** 3
+    jout = torch.empty(npts * nq3 * 2, dtype=torch.float32, device="cuda")
+    g_exact = torch.zeros((6, nr, ng), dtype=torch.float64, device="cuda")
+    ctx.set_action_output(jout)
+    st = ctx.moments(pot, delta, df, rule, ng, g_exact)
+    ctx.set_action_output(None)
+    s = F.Surrogate(ctx, batch=8192, seed=3)
+    loss = s.fit(pot, ng, rule, jout, 1 << 20, seed=5, epochs=8, lr=2e-3)
+    g_sg = torch.zeros_like(g_exact)
+    s.moments(pot, df, rule, ng, g_sg)  # warm-up (workspace allocation)
+    ms = s.moments(pot, df, rule, ng, g_sg)
+    torch.cuda.synchronize()
+    a, b = g_sg[0].cpu().numpy().ravel(), g_exact[0].cpu().numpy().ravel()
+    rel = np.abs(a - b) / b
+    print(f"surrogate: fit loss {loss:.3e}, moments {ms:.1f} ms vs exact {st.kernel_ms:.1f} ms, "
+          f"rho rel err median {np.median(rel):.2e} p90 {np.percentile(rel, 90):.2e} max {rel.max():.2e}")
+    assert loss < 0.05
+    assert ms < st.kernel_ms / 5
+    assert np.median(rel) < 0.05
+    s.close()
+
+
+def test_surrogate_schedule(ctx):
+    """The surrogate-accelerated loop (exact first and last iterations) lands within
+    1e-3 of the exact mixed loop after the same number of iterations, on a smaller NFW
+    model, and reports its iteration kinds."""
+    from fjmodels_gb300 import _abi as A
+    rule = F.Rule(*F.tanh_sinh_rule(16), precision=A.FJ_PREC_MIXED)
+    df = F.DFParams("NFW", chi=1.0, k=0.5)
+    args = (40, 16, 5, 1e-3, 300.0, df, rule)
+    ref = ctx.run_model(*args, itermax=8)
+    s = F.Surrogate(ctx, batch=4096, seed=9)
+    out, rep = ctx.run_model_surrogate(*args, itermax=8, surrogate=s, samples=1 << 18, epochs_first=8, epochs=2,
+                                       lr=2e-3, exact_first=1, exact_last=3, audit_stride=50, audit_tol=0.05)
+    print("schedule report", rep)
+    assert out["iterations"] == 8
+    assert rep["surrogate_iterations"] + rep["fallback_iterations"] == 4 and rep["fits"] >= 1
+    from tests.helpers import rel_rows
+    assert rel_rows(out["phil"], ref["phil"]) < 1e-3
+    s.close()
