@@ -397,6 +397,24 @@ int sg_backward(fj_surrogate *s, const float *T)
     return cudaGetLastError() == cudaSuccess ? FJ_OK : FJ_ERR_CUDA;
 }
 
+// the inference workspace: kInferRows rows per pass (bf16 inputs, two hidden
+// buffers, f32 features and outputs), allocated on first use
+int sg_infer_buffers(fj_surrogate *s)
+{
+    if (s->Xi && s->Hi && s->Xf && s->Yf) return FJ_OK;
+    int rc;
+    void *q;
+    if ((rc = sg_alloc(s, &q, (size_t)kInferRows * fj::kIn * sizeof(__nv_bfloat16)))) return rc;
+    s->Xi = (__nv_bfloat16 *)q;
+    if ((rc = sg_alloc(s, &q, (size_t)2 * kInferRows * fj::kHid * sizeof(__nv_bfloat16)))) return rc;
+    s->Hi = (__nv_bfloat16 *)q;
+    if ((rc = sg_alloc(s, &q, (size_t)kInferRows * fj::kIn * sizeof(float)))) return rc;
+    s->Xf = (float *)q;
+    if ((rc = sg_alloc(s, &q, (size_t)kInferRows * fj::kOut * sizeof(float)))) return rc;
+    s->Yf = (float *)q;
+    return FJ_OK;
+}
+
 int sg_check_err(fj_surrogate *s)
 {
     int h = 0;
@@ -574,13 +592,7 @@ int fj_surrogate_predict(fj_surrogate *s, const float *X, long long n, float *Y)
 {
     if (!s || !X || !Y || n < 1) return FJ_ERR_ARG;
     int rc;
-    if (!s->Xi) {  // inference workspace: kInferRows rows per pass
-        void *q;
-        if ((rc = sg_alloc(s, &q, (size_t)kInferRows * fj::kIn * sizeof(__nv_bfloat16)))) return rc;
-        s->Xi = (__nv_bfloat16 *)q;
-        if ((rc = sg_alloc(s, &q, (size_t)2 * kInferRows * fj::kHid * sizeof(__nv_bfloat16)))) return rc;
-        s->Hi = (__nv_bfloat16 *)q;
-    }
+    if ((rc = sg_infer_buffers(s))) return rc;
     for (long long r0 = 0; r0 < n; r0 += kInferRows) {
         const int m = (int)std::min<long long>(kInferRows, n - r0);
         fj::k_to_bf16<<<(m * fj::kIn + 255) / 256, 256, 0, s->stream>>>(m * fj::kIn, X + (size_t)r0 * fj::kIn, s->Xi);
@@ -746,18 +758,6 @@ int sg_grid(fj_surrogate *s, const fj_potential *pot, int ngauss, const fj_quad_
     return FJ_OK;
 }
 
-int sg_infer_buffers(fj_surrogate *s)
-{
-    int rc;
-    void *q;
-    if (!s->Xf) {
-        if ((rc = sg_alloc(s, &q, (size_t)kInferRows * fj::kIn * sizeof(float)))) return rc;
-        s->Xf = (float *)q;
-        if ((rc = sg_alloc(s, &q, (size_t)kInferRows * fj::kOut * sizeof(float)))) return rc;
-        s->Yf = (float *)q;
-    }
-    return FJ_OK;
-}
 
 }  // namespace
 
