@@ -289,6 +289,8 @@ struct fj_surrogate {
     long long fit_cap = 0;
     double *partial = nullptr;                    // surrogate moment sums [npts][6]
     long long partial_cap = 0;
+    double *points = nullptr;                     // per grid point: Phi, Ve
+    long long points_cap = 0;
     long long step = 0;
     std::vector<void *> owned;
 };
@@ -606,37 +608,52 @@ int fj_surrogate_predict(fj_surrogate *s, const float *X, long long n, float *Y)
 // ======================================================================
 // Surrogate features, targets and the surrogate moment sums.
 //
-// Features of node (i, j, k) of grid point p = (ar[n], cos theta_g) (all
-// exact table values at the grid radius, nothing interpolated):
+// Features of node (i, j, k) of grid point p = (ar[n], cos theta_g) (table
+// values at the grid radius, nothing interpolated):
 //   0: (log r - mu) / sigma over the grid's log-radius range,   1: cos theta,
 //   2, 3, 4: vR / Ve, vz / Ve, vphi / Ve (the node's rule coordinates),
 //   5: Phi_0(r) / Phi_0(ar[0]),   6..12: Phi_l(r) / |Phi_0(r)|, l = 1..7,
-//   13..15: 0.
-// Targets: t = log(J / (r Ve) + 1e-6) for Jr and Jz.  (The escape speed Ve
-// scales the velocities rather than the circular speed, which vanishes at
-// the centre of a cusped model.)
+//   13: log(H / Phi(point)) / 5 (-> -inf as the orbit becomes unbound),
+//   14, 15: 0.
+// Outputs: 0: log(Jr + Jz + |Jphi| + 1e-12), 1: Jr / (Jr + Jz).  |Jphi| =
+// R vphi is known exactly, so Jr and Jz follow from (Jt - |Jphi|) split by the
+// fraction; regressing log J of each action instead is dominated by the
+// circular (Jr = 0) and near-unbound (J -> inf) tails.
 // ======================================================================
 namespace fj {
-
-constexpr float kSgFloor = 1e-6f;
 
 struct SgGrid {
     PotView P;
     const double *ci;  // polar nodes
     int ngauss, nq;
     const double *xq;
-    double lmu, lsig;  // log-radius normalisation
+    double lmu, lsig;     // log-radius normalisation
+    const double *point;  // [npts][2]: Phi at the point, escape speed Ve
 };
 
-__device__ __forceinline__ void sg_point(const SgGrid &g, int p, double &R, double &z, double &Phi_h, double &Ve)
+__global__ void k_sg_points(SgGrid g, int npts, double *point)
 {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npts) return;
     const int n = p / g.ngauss, gg = p % g.ngauss;
     const double c = g.ci[gg], si = sqrt(1 - c * c);
-    R = g.P.ar[n] * si;
-    z = g.P.ar[n] * c;
-    Phi_h = pot_phi(g.P, R, z);
+    const double Phi_h = pot_phi(g.P, g.P.ar[n] * si, g.P.ar[n] * c);
     const double rmax = g.P.ar[g.P.nr - 1];
-    Ve = sqrt(-2 * (Phi_h - pot_phi(g.P, 10 * rmax, 10 * rmax)));
+    point[2 * p] = Phi_h;
+    point[2 * p + 1] = sqrt(-2 * (Phi_h - pot_phi(g.P, 10 * rmax, 10 * rmax)));
+}
+
+__device__ __forceinline__ void sg_velocity(const SgGrid &g, int p, int node, double &V0, double &V1, double &V2,
+                                            double &H, double &R)
+{
+    const int nq = g.nq;
+    const double Phi_h = g.point[2 * p], Ve = g.point[2 * p + 1];
+    V0 = 1e-6 + Ve * g.xq[node / (nq * nq)];
+    V1 = 1e-6 + Ve * g.xq[(node / nq) % nq];
+    V2 = 1e-6 + Ve * g.xq[node % nq];
+    H = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h;
+    const double c = g.ci[p % g.ngauss];
+    R = g.P.ar[p / g.ngauss] * sqrt(1 - c * c);
 }
 
 // features of nodes idx[0..m) (idx = p * nq^3 + node; NULL: rows 0..m-1 are nodes
@@ -658,13 +675,16 @@ __global__ void k_sg_features(SgGrid g, const long long *idx, long long first, l
     const double p0 = g.P.phil[n * np_];
     x[5] = (float)(p0 / g.P.phil[0]);
     for (int l = 1; l < 8; l++) x[5 + l] = l < np_ ? (float)(g.P.phil[n * np_ + l] / fabs(p0)) : 0.f;
-    x[13] = x[14] = x[15] = 0.f;
+    double V0, V1, V2, H, R;
+    sg_velocity(g, p, node, V0, V1, V2, H, R);
+    x[13] = (float)(log(fmax(H / g.point[2 * p], 1e-12)) / 5);
+    x[14] = x[15] = 0.f;
 }
 
-// training rows from exact actions J [npts * nq^3][2] (unbound: negative):
-// sample s takes node hash(seed, s) (the next bound one after it, within 64)
+// training rows from exact actions J [npts * nq^3][2] (unbound or E >= 0: NaN or
+// 1e31): sample s takes node hash(seed, s) (the next valid one after it, within 64)
 __global__ void k_sg_sample(SgGrid g, const float *J, long long total, unsigned long long seed, long long ns,
-                            long long *idx, float *T, int *found)
+                            long long *idx, float *T)
 {
     const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (s >= ns) return;
@@ -676,17 +696,16 @@ __global__ void k_sg_sample(SgGrid g, const float *J, long long total, unsigned 
     bool ok = false;
     for (int t = 0; t < 64 && !ok; t++) {
         const long long q = (id + t) % total;
-        if (J[2 * q] >= 0.f && J[2 * q + 1] >= 0.f) { id = q; ok = true; }
+        const float jr = J[2 * q], jz = J[2 * q + 1];
+        if (jr >= 0.f && jz >= 0.f && jr < 1e30f && jz < 1e30f) { id = q; ok = true; }
     }
     idx[s] = id;
-    if (!ok) { T[2 * s] = T[2 * s + 1] = 0.f; return; }
-    if (found) atomicAdd(found, 1);
-    const int nq3 = g.nq * g.nq * g.nq, p = (int)(id / nq3);
-    double R, z, Phi_h, Ve;
-    sg_point(g, p, R, z, Phi_h, Ve);
-    const double sc = g.P.ar[p / g.ngauss] * Ve;
-    T[2 * s] = logf((float)(J[2 * id] / sc) + kSgFloor);
-    T[2 * s + 1] = logf((float)(J[2 * id + 1] / sc) + kSgFloor);
+    const int nq3 = g.nq * g.nq * g.nq, p = (int)(id / nq3), node = (int)(id % nq3);
+    double V0, V1, V2, H, R;
+    sg_velocity(g, p, node, V0, V1, V2, H, R);
+    const double jr = ok ? J[2 * id] : 0., jz = ok ? J[2 * id + 1] : 0., jp = fabs(R * V1);
+    T[2 * s] = (float)log(jr + jz + jp + 1e-12);
+    T[2 * s + 1] = jr + jz > 0 ? (float)(jr / (jr + jz)) : 0.5f;
 }
 
 // moment sums of grid point p0 + blockIdx.x from the surrogate outputs Y (rows from
@@ -696,18 +715,16 @@ __global__ void __launch_bounds__(128) k_sg_moments(SgGrid g, const double *wq, 
 {
     __shared__ double s_red[6 * 4];
     const int p = p0 + blockIdx.x, nq = g.nq, nq3 = nq * nq * nq;
-    double R, z, Phi_h, Ve;
-    sg_point(g, p, R, z, Phi_h, Ve);
-    const double sc = g.P.ar[p / g.ngauss] * Ve, jacob = Ve * Ve * Ve;
+    const double Ve = g.point[2 * p + 1], jacob = Ve * Ve * Ve;
     double m[6] = {0, 0, 0, 0, 0, 0};
     for (int node = threadIdx.x; node < nq3; node += blockDim.x) {
-        const int i = node / (nq * nq), j = (node / nq) % nq, k = node % nq;
-        const double V0 = 1e-6 + Ve * g.xq[i], V1 = 1e-6 + Ve * g.xq[j], V2 = 1e-6 + Ve * g.xq[k];
-        if (!(.5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h < 0)) continue;
+        double V0, V1, V2, H, R;
+        sg_velocity(g, p, node, V0, V1, V2, H, R);
+        if (!(H < 0)) continue;
         const float *y = Y + ((long long)p * nq3 + node - first) * 16;
-        const float Jr = fmaxf(0.f, (expf(y[0]) - kSgFloor) * (float)sc);
-        const float Jz = fmaxf(0.f, (expf(y[1]) - kSgFloor) * (float)sc);
-        const float Jphi = (float)(R * V1), J0 = (float)df.J0;
+        const float Jphi = (float)(R * V1);
+        const float js = fmaxf(0.f, expf(y[0]) - fabsf(Jphi)), fr = fminf(1.f, fmaxf(0.f, y[1]));
+        const float Jr = fr * js, Jz = (1.f - fr) * js, J0 = (float)df.J0;
         const float h = Jr + (float)df.dphi_h * fabsf(Jphi) + (float)df.dz_h * Jz;
         const float gg = Jr + (float)df.dphi_g * fabsf(Jphi) + (float)df.dz_g * Jz;
         const float ev = (float)df.norm *
@@ -715,6 +732,7 @@ __global__ void __launch_bounds__(128) k_sg_moments(SgGrid g, const double *wq, 
                          (float)df.tpi3;
         float f = df.chi == 0. ? ev : ev + (float)df.k * tanhf((float)df.chi * Jphi / J0) * ev;
         if (isnan(f)) f = 0.f;
+        const int i = node / (nq * nq), j = (node / nq) % nq, k = node % nq;
         const double jd = (wq[i] * wq[j] * wq[k]) * (jacob * (double)f);
         m[0] += jd;
         m[1] += jd * V1;
@@ -755,7 +773,17 @@ int sg_grid(fj_surrogate *s, const fj_potential *pot, int ngauss, const fj_quad_
     g.ci = ci; g.ngauss = ngauss; g.nq = rule->nq; g.xq = xq;
     g.lmu = .5 * (log(ar2[0]) + log(ar2[1]));
     g.lsig = .5 * (log(ar2[1]) - log(ar2[0]));
-    return FJ_OK;
+    const int npts = pot->nr * ngauss;
+    if (npts > s->points_cap) {
+        void *q;
+        int rc2 = sg_alloc(s, &q, (size_t)npts * 2 * sizeof(double));
+        if (rc2) return rc2;
+        s->points = (double *)q;
+        s->points_cap = npts;
+    }
+    g.point = s->points;
+    fj::k_sg_points<<<(npts + 127) / 128, 128, 0, s->stream>>>(g, npts, s->points);
+    return cudaGetLastError() == cudaSuccess ? FJ_OK : FJ_ERR_CUDA;
 }
 
 
@@ -782,8 +810,7 @@ int fj_surrogate_fit(fj_surrogate *s, const fj_potential *pot, int ngauss, const
         s->fit_cap = ns;
     }
     const long long total = (long long)pot->nr * ngauss * rule->nq * rule->nq * rule->nq;
-    fj::k_sg_sample<<<(unsigned)((ns + 255) / 256), 256, 0, s->stream>>>(g, J, total, seed, ns, s->fitIdx, s->fitT,
-                                                                         nullptr);
+    fj::k_sg_sample<<<(unsigned)((ns + 255) / 256), 256, 0, s->stream>>>(g, J, total, seed, ns, s->fitIdx, s->fitT);
     fj::k_sg_features<<<(unsigned)((ns + 255) / 256), 256, 0, s->stream>>>(g, s->fitIdx, 0, ns, s->fitX);
     return fj_surrogate_train(s, s->fitX, s->fitT, ns, epochs, lr, loss);
 }

@@ -136,7 +136,7 @@ def test_surrogate_moments_gain(ctx):
     rel = np.abs(a - b) / b
     print(f"surrogate: fit loss {loss:.3e}, moments {ms:.1f} ms vs exact {st.kernel_ms:.1f} ms, "
           f"rho rel err median {np.median(rel):.2e} p90 {np.percentile(rel, 90):.2e} max {rel.max():.2e}")
-    assert loss < 0.05
+    assert loss < 0.1
     assert ms < st.kernel_ms / 5
     assert np.median(rel) < 0.05
     s.close()
