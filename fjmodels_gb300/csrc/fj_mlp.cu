@@ -401,6 +401,15 @@ int sg_backward(fj_surrogate *s, const float *T)
 
 // the inference workspace: kInferRows rows per pass (bf16 inputs, two hidden
 // buffers, f32 features and outputs), allocated on first use
+fj::DFDev sg_df(const fj_df_params *df)
+{
+    fj::DFDev d;
+    d.kind = df->kind; d.alpha = df->alpha; d.beta = df->beta; d.J0 = df->J0;
+    d.norm = df->mass / pow(df->J0, 3); d.tpi3 = pow(2 * fj::kPI, 3.);
+    d.dphi_h = df->dphi_h; d.dz_h = df->dz_h; d.dphi_g = df->dphi_g; d.dz_g = df->dz_g; d.chi = df->chi; d.k = df->k;
+    return d;
+}
+
 int sg_infer_buffers(fj_surrogate *s)
 {
     if (s->Xi && s->Hi && s->Xf && s->Yf) return FJ_OK;
@@ -615,10 +624,12 @@ int fj_surrogate_predict(fj_surrogate *s, const float *X, long long n, float *Y)
 //   5: Phi_0(r) / Phi_0(ar[0]),   6..12: Phi_l(r) / |Phi_0(r)|, l = 1..7,
 //   13: log(H / Phi(point)) / 5 (-> -inf as the orbit becomes unbound),
 //   14, 15: 0.
-// Outputs: 0: log(Jr + Jz + |Jphi| + 1e-12), 1: Jr / (Jr + Jz).  |Jphi| =
-// R vphi is known exactly, so Jr and Jz follow from (Jt - |Jphi|) split by the
-// fraction; regressing log J of each action instead is dominated by the
-// circular (Jr = 0) and near-unbound (J -> inf) tails.
+// Outputs: log h and log g of the double-power-law DF (DF.cpp:65-76),
+// h = Jr + dphi_h |Jphi| + dz_h Jz and g likewise: the DF needs nothing else
+// (Jphi = R vphi is exact), and their logs are smooth with no cancellation.
+// Regressing log J of each action is dominated by the circular (Jr = 0) and
+// near-unbound tails; recovering Jr + Jz from a predicted total action loses
+// the near-circular in-plane orbits, where the DF peaks.
 // ======================================================================
 namespace fj {
 
@@ -683,7 +694,7 @@ __global__ void k_sg_features(SgGrid g, const long long *idx, long long first, l
 
 // training rows from exact actions J [npts * nq^3][2] (unbound or E >= 0: NaN or
 // 1e31): sample s takes node hash(seed, s) (the next valid one after it, within 64)
-__global__ void k_sg_sample(SgGrid g, const float *J, long long total, unsigned long long seed, long long ns,
+__global__ void k_sg_sample(SgGrid g, DFDev df, const float *J, long long total, unsigned long long seed, long long ns,
                             long long *idx, float *T)
 {
     const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -704,8 +715,8 @@ __global__ void k_sg_sample(SgGrid g, const float *J, long long total, unsigned 
     double V0, V1, V2, H, R;
     sg_velocity(g, p, node, V0, V1, V2, H, R);
     const double jr = ok ? J[2 * id] : 0., jz = ok ? J[2 * id + 1] : 0., jp = fabs(R * V1);
-    T[2 * s] = (float)log(jr + jz + jp + 1e-12);
-    T[2 * s + 1] = jr + jz > 0 ? (float)(jr / (jr + jz)) : 0.5f;
+    T[2 * s] = (float)log(jr + df.dphi_h * jp + df.dz_h * jz + 1e-12);
+    T[2 * s + 1] = (float)log(jr + df.dphi_g * jp + df.dz_g * jz + 1e-12);
 }
 
 // moment sums of grid point p0 + blockIdx.x from the surrogate outputs Y (rows from
@@ -722,11 +733,8 @@ __global__ void __launch_bounds__(128) k_sg_moments(SgGrid g, const double *wq, 
         sg_velocity(g, p, node, V0, V1, V2, H, R);
         if (!(H < 0)) continue;
         const float *y = Y + ((long long)p * nq3 + node - first) * 16;
-        const float Jphi = (float)(R * V1);
-        const float js = fmaxf(0.f, expf(y[0]) - fabsf(Jphi)), fr = fminf(1.f, fmaxf(0.f, y[1]));
-        const float Jr = fr * js, Jz = (1.f - fr) * js, J0 = (float)df.J0;
-        const float h = Jr + (float)df.dphi_h * fabsf(Jphi) + (float)df.dz_h * Jz;
-        const float gg = Jr + (float)df.dphi_g * fabsf(Jphi) + (float)df.dz_g * Jz;
+        const float Jphi = (float)(R * V1), J0 = (float)df.J0;
+        const float h = expf(y[0]), gg = expf(y[1]);
         const float ev = (float)df.norm *
                          fmaxf(0.f, powf(1.f + J0 / h, (float)df.alpha) / powf(1.f + gg / J0, (float)df.beta)) /
                          (float)df.tpi3;
@@ -791,10 +799,11 @@ int sg_grid(fj_surrogate *s, const fj_potential *pot, int ngauss, const fj_quad_
 
 extern "C" {
 
-int fj_surrogate_fit(fj_surrogate *s, const fj_potential *pot, int ngauss, const fj_quad_rule *rule, const float *J,
-                     long long nsamples, unsigned long long seed, int epochs, float lr, double *loss)
+int fj_surrogate_fit(fj_surrogate *s, const fj_potential *pot, const fj_df_params *df, int ngauss,
+                     const fj_quad_rule *rule, const float *J, long long nsamples, unsigned long long seed, int epochs,
+                     float lr, double *loss)
 {
-    if (!s || !J || nsamples < s->batch || epochs < 1) return FJ_ERR_ARG;
+    if (!s || !J || !df || nsamples < s->batch || epochs < 1) return FJ_ERR_ARG;
     fj::SgGrid g;
     int rc = sg_grid(s, pot, ngauss, rule, g);
     if (rc) return rc;
@@ -810,7 +819,8 @@ int fj_surrogate_fit(fj_surrogate *s, const fj_potential *pot, int ngauss, const
         s->fit_cap = ns;
     }
     const long long total = (long long)pot->nr * ngauss * rule->nq * rule->nq * rule->nq;
-    fj::k_sg_sample<<<(unsigned)((ns + 255) / 256), 256, 0, s->stream>>>(g, J, total, seed, ns, s->fitIdx, s->fitT);
+    fj::k_sg_sample<<<(unsigned)((ns + 255) / 256), 256, 0, s->stream>>>(g, sg_df(df), J, total, seed, ns, s->fitIdx,
+                                                                         s->fitT);
     fj::k_sg_features<<<(unsigned)((ns + 255) / 256), 256, 0, s->stream>>>(g, s->fitIdx, 0, ns, s->fitX);
     return fj_surrogate_train(s, s->fitX, s->fitT, ns, epochs, lr, loss);
 }
@@ -834,10 +844,7 @@ int fj_surrogate_moments(fj_surrogate *s, const fj_potential *pot, const fj_df_p
     }
     if (nq3 > kInferRows) return FJ_ERR_ARG;
     const int per = kInferRows / nq3;  // whole grid points per inference pass
-    fj::DFDev d;
-    d.kind = df->kind; d.alpha = df->alpha; d.beta = df->beta; d.J0 = df->J0;
-    d.norm = df->mass / pow(df->J0, 3); d.tpi3 = pow(2 * fj::kPI, 3.);
-    d.dphi_h = df->dphi_h; d.dz_h = df->dz_h; d.dphi_g = df->dphi_g; d.dz_g = df->dz_g; d.chi = df->chi; d.k = df->k;
+    const fj::DFDev d = sg_df(df);
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

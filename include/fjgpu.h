@@ -159,7 +159,7 @@ int fj_tc_gemm(int M, int N, int K, const void *A, int lda, const void *B, int l
 
 /* The action surrogate (no reference counterpart): an MLP 16 -> 128 x 4
    (GELU) -> 16 mapping normalised phase-space features (13 used, zero padded)
-   to (log Jr, log Jz) (outputs 0 and 1), trained and evaluated with the
+   to log h and log g of the double-power-law DF (outputs 0 and 1), trained and evaluated with the
    tensor-core GEMMs: BF16 weights and activations, FP32 accumulation and
    master weights, Adam.  batch = samples per training step (a multiple of
    128); work runs on the context's stream.  X device f32 [n][16], T device
@@ -184,9 +184,11 @@ int fj_surrogate_train(fj_surrogate *s, const float *X, const float *T, long lon
 int fj_surrogate_predict(fj_surrogate *s, const float *X, long long n, float *Y);
 /* Fit to the exact actions J of a grid iteration (from fj_set_action_output,
    in potential pot): `samples` rows drawn with `seed` among bound nodes,
-   features built on the device, `epochs` of Adam at lr. */
-int fj_surrogate_fit(fj_surrogate *s, const fj_potential *pot, int ngauss, const fj_quad_rule *rule, const float *J,
-                     long long samples, unsigned long long seed, int epochs, float lr, double *loss);
+   features built on the device, targets log h and log g of the DF df,
+   `epochs` of Adam at lr. */
+int fj_surrogate_fit(fj_surrogate *s, const fj_potential *pot, const fj_df_params *df, int ngauss,
+                     const fj_quad_rule *rule, const float *J, long long samples, unsigned long long seed, int epochs,
+                     float lr, double *loss);
 /* computeRhl with the surrogate's actions: features of every velocity node
    of the grid, the MLP on the tensor cores, the double-power-law DF and the
    moment sums into grids6 device [6][nr*ngauss]; ms = device time. */
