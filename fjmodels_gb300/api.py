@@ -521,10 +521,10 @@ class Surrogate:
                                            _ptr(jout), samples, seed, epochs, lr, _dp(loss)), "fj_surrogate_fit")
         return float(loss[0])
 
-    def moments(self, pot, df, rule, ngauss, grids6):
+    def moments(self, pot, df, rule, ngauss, grids6, fused=True):
         ms = np.zeros(1)
         self._rc(self.lib.fj_surrogate_moments(self.h, C.byref(pot.c), C.byref(df.c), C.byref(rule.c), ngauss,
-                                               _ptr(grids6), _dp(ms)), "fj_surrogate_moments")
+                                               _ptr(grids6), _dp(ms), 1 if fused else 0), "fj_surrogate_moments")
         return float(ms[0])
 
     def predict(self, X, Y):

@@ -1310,7 +1310,7 @@ extern "C" int fj_run_model_surrogate(fj_ctx *ctx, const fj_model_config *cfg, c
         if (!exact) {
             auto ts = now();
             double sms = 0;
-            if ((rc = fj_surrogate_moments(sg, &pot, &cfg->df, &cfg->rule, ng, d_grids, &sms)))
+            if ((rc = fj_surrogate_moments(sg, &pot, &cfg->df, &cfg->rule, ng, d_grids, &sms, 1)))
                 return fail(ctx, rc, "run_model_surrogate: surrogate moments");
             double err = 0;
             if (ne) {

@@ -765,6 +765,263 @@ __global__ void __launch_bounds__(128) k_sg_moments(SgGrid g, const double *wq, 
 
 }  // namespace fj
 
+// ======================================================================
+// Fused surrogate moments: features, the MLP on the tensor cores and the DF
+// moment sums of one grid point's bound nodes in one kernel.  One CTA per
+// (grid point, node range); two groups of four warps each own a 128-node
+// tile in flight (own activation buffer, 128 TMEM columns, mbarrier) and
+// share the five layers' BF16 weights, resident in shared memory in the
+// canonical K-major layout.  Per tile: each thread writes its node's 16
+// features into the operand buffer; one thread issues the layer's
+// tcgen05.mma chain; after the commit the group reads the accumulators back
+// (tcgen05.ld), applies bias and GELU and writes the BF16 activations into
+// the same buffer as the next layer's operand; the output layer's log h and
+// log g go straight into the DF and the FP64 moment sums.
+// ======================================================================
+namespace fj {
+
+struct SgWeights {
+    const __nv_bfloat16 *W[5];  // [rows][cols] row-major
+    const float *b[5];
+};
+
+constexpr int kFusedThreads = 256;     // two groups of 128
+constexpr int kFusedMaxNodes = 12288;  // node range of one CTA (bound-node list in shared memory)
+
+// canonical no-swizzle K-major offset (bytes) of element (row, k) of a [rows][K]
+// bf16 operand: K steps of 16 are rows*32 bytes apart
+__device__ __forceinline__ uint32_t kmaj_off(int row, int k, int rows)
+{
+    return (uint32_t)((k >> 4) * rows * 32 + (row >> 3) * 256 + ((k >> 3) & 1) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// shared memory: W0 4 KB | W1..W3 96 KB | W4 4 KB | biases 2112 B | 2 x act 32 KB | list | misc
+constexpr int kSmW0 = 0, kSmW1 = 4096, kSmW4 = kSmW1 + 3 * 32768, kSmBias = kSmW4 + 4096;
+constexpr int kSmAct = kSmBias + 4 * 128 * 4 + 16 * 4 + 192;  // 1024-aligned below
+constexpr int kSmActAligned = (kSmAct + 1023) / 1024 * 1024;
+constexpr int kSmList = kSmActAligned + 2 * 32768;
+constexpr size_t fused_smem_bytes() { return (size_t)kSmList + kFusedMaxNodes * 2 + 256; }
+
+__global__ void __launch_bounds__(kFusedThreads, 1) k_sg_fused(SgGrid g, SgWeights wts, const double *wq, DFDev df,
+                                                               int blocks_per_point, double *partial, int *err)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    __shared__ __align__(8) unsigned long long bars[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_wc[8];
+    __shared__ double s_red[8 * 6];
+    unsigned short *s_list = (unsigned short *)(sm + kSmList);
+    float *s_bias = (float *)(sm + kSmBias);
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, grp = tid >> 7, gt = tid & 127;
+    const int B = blocks_per_point, p = blockIdx.x / B, chunk = blockIdx.x % B;
+    const int nq = g.nq, nq3 = nq * nq * nq;
+    const int n0 = (int)((long long)chunk * nq3 / B), n1 = (int)((long long)(chunk + 1) * nq3 / B);
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         tc::smem_addr(&tmem_slot)),
+                     "r"(256)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid < 2) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(tc::smem_addr(&bars[tid])), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // weights -> canonical layout (16-byte pieces), biases
+    {
+        const int rows[5] = {128, 128, 128, 128, 16}, cols[5] = {16, 128, 128, 128, 128};
+        const int base[5] = {kSmW0, kSmW1, kSmW1 + 32768, kSmW1 + 65536, kSmW4};
+        for (int l = 0; l < 5; l++) {
+            const int pieces = rows[l] * cols[l] / 8;
+            for (int q = tid; q < pieces; q += kFusedThreads) {
+                const int r = q / (cols[l] / 8), k = (q % (cols[l] / 8)) * 8;
+                *reinterpret_cast<uint4 *>(sm + base[l] + kmaj_off(r, k, rows[l])) =
+                    *reinterpret_cast<const uint4 *>(wts.W[l] + (size_t)r * cols[l] + k);
+            }
+        }
+        for (int q = tid; q < 4 * 128 + 16; q += kFusedThreads) s_bias[q] = wts.b[q >> 7 < 4 ? q >> 7 : 4][q < 512 ? q & 127 : q - 512];
+    }
+    // bound nodes of [n0, n1) in node order
+    const double Phi_h = g.point[2 * p], Ve = g.point[2 * p + 1];
+    int nbound = 0;
+    for (int base = n0; base < n1; base += kFusedThreads) {
+        const int node = base + tid;
+        bool b = false;
+        if (node < n1) {
+            double V0, V1, V2, H, R;
+            sg_velocity(g, p, node, V0, V1, V2, H, R);
+            b = H < 0;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, b);
+        if (lane == 0) s_wc[warp] = __popc(bal);
+        __syncthreads();
+        int off = nbound, tot = 0;
+        for (int w = 0; w < 8; w++) {
+            if (w < warp) off += s_wc[w];
+            tot += s_wc[w];
+        }
+        if (b) s_list[off + __popc(bal & ((1u << lane) - 1u))] = (unsigned short)(node - n0);
+        __syncthreads();
+        nbound += tot;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot + (uint32_t)(grp * 128);
+    const uint32_t bar = tc::smem_addr(&bars[grp]);
+    unsigned char *act = sm + kSmActAligned + grp * 32768;
+    const uint32_t act_a = tc::smem_addr(act), w_a = tc::smem_addr(sm);
+    const int n = p / g.ngauss, np_ = g.P.npoly;
+    const double c = g.ci[p % g.ngauss], R = g.P.ar[n] * sqrt(1 - c * c), jacob = Ve * Ve * Ve;
+    // per-point features
+    float fx[14];
+    fx[0] = (float)((log(g.P.ar[n]) - g.lmu) / g.lsig);
+    fx[1] = (float)c;
+    const double p0v = g.P.phil[n * np_];
+    fx[5] = (float)(p0v / g.P.phil[0]);
+    for (int l = 1; l < 8; l++) fx[5 + l] = l < np_ ? (float)(g.P.phil[n * np_ + l] / fabs(p0v)) : 0.f;
+    double m[6] = {0, 0, 0, 0, 0, 0};
+    uint32_t phase = 0;
+    const float J0 = (float)df.J0;
+    auto group_sync = [&]() { asm volatile("bar.sync %0, 128;" ::"r"(1 + grp) : "memory"); };
+    // true in every thread of the group when v is true in any of them (also a group barrier)
+    auto group_any = [&](bool v) {
+        uint32_t r;
+        asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, %2, 128, p;\n"
+                     " selp.u32 %0, 1, 0, q;\n}\n"
+                     : "=r"(r)
+                     : "r"((uint32_t)v), "r"(1 + grp)
+                     : "memory");
+        return r != 0;
+    };
+    // one layer's MMAs; false (in the whole group) if the completion wait gave up
+    auto mma_chain = [&](int k_steps, uint32_t b_base, int n_cols) {
+        if (gt == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t idesc = tc::idesc_bf16(128, n_cols);
+            for (int ks = 0; ks < k_steps; ks++) {
+                const uint64_t ad = tc::smem_desc(act_a + ks * 4096, 128, 256);
+                const uint64_t bd = tc::smem_desc(w_a + b_base + ks * (n_cols * 32), 128, 256);
+                const uint32_t acc = ks ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                         : "memory");
+        }
+        const bool ok = tc::mbar_wait(bar, phase);
+        phase ^= 1u;
+        const bool bad = group_any(!ok);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        return !bad;
+    };
+    const int ntiles = (nbound + 127) / 128;
+    bool aborted = false;
+    for (int t = grp; t < ntiles && !aborted; t += 2) {
+        const int q = t * 128 + gt;
+        const bool valid = q < nbound;
+        const int node = valid ? n0 + s_list[q] : n0;
+        double V0, V1, V2, H, Rr;
+        sg_velocity(g, p, node, V0, V1, V2, H, Rr);
+        // features of this thread's node, row gt of the K = 16 operand
+        {
+            float x[16];
+            for (int i = 0; i < 14; i++) x[i] = fx[i];
+            x[2] = (float)g.xq[node / (nq * nq)];
+            x[3] = (float)g.xq[node % nq];
+            x[4] = (float)g.xq[(node / nq) % nq];
+            x[13] = valid ? (float)(log(fmax(H / Phi_h, 1e-12)) / 5) : 0.f;
+            x[14] = x[15] = 0.f;
+            for (int h8 = 0; h8 < 2; h8++) {
+                __align__(16) __nv_bfloat16 v[8];
+                for (int e = 0; e < 8; e++) v[e] = __float2bfloat16_rn(x[h8 * 8 + e]);
+                *reinterpret_cast<uint4 *>(act + kmaj_off(gt, h8 * 8, 128)) = *reinterpret_cast<const uint4 *>(v);
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        group_sync();
+        // hidden layers: acc -> bias + GELU -> bf16 operand of the next layer
+        for (int l = 0; l < 4 && !aborted; l++) {
+            if (!mma_chain(l == 0 ? 1 : 8, l == 0 ? kSmW0 : kSmW1 + (l - 1) * 32768, 128)) { aborted = true; break; }
+            for (int c0 = 0; c0 < 128; c0 += 16) {
+                uint32_t r[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                      "=r"(r[15])
+                    : "r"(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)c0));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                __align__(16) __nv_bfloat16 v[16];
+                for (int e = 0; e < 16; e++) v[e] = __float2bfloat16_rn(tc::gelu(__uint_as_float(r[e]) + s_bias[l * 128 + c0 + e]));
+                *reinterpret_cast<uint4 *>(act + kmaj_off(gt, c0, 128)) = *reinterpret_cast<const uint4 *>(v);
+                *reinterpret_cast<uint4 *>(act + kmaj_off(gt, c0 + 8, 128)) = *reinterpret_cast<const uint4 *>(v + 8);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            group_sync();
+        }
+        if (aborted) break;
+        // output layer (N = 16): columns 0, 1 = log h, log g
+        if (!mma_chain(8, kSmW4, 16)) { aborted = true; break; }
+        uint32_t r[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(tmem + ((uint32_t)((warp & 3) * 32) << 16)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        group_sync();  // the operand buffer and TMEM are free for the group's next tile
+        if (valid) {
+            const float h = expf(__uint_as_float(r[0]) + s_bias[512]), gg = expf(__uint_as_float(r[1]) + s_bias[513]);
+            const float Jphi = (float)(R * V1);
+            const float ev = (float)df.norm *
+                             fmaxf(0.f, powf(1.f + J0 / h, (float)df.alpha) / powf(1.f + gg / J0, (float)df.beta)) /
+                             (float)df.tpi3;
+            float f = df.chi == 0. ? ev : ev + (float)df.k * tanhf((float)df.chi * Jphi / J0) * ev;
+            if (isnan(f)) f = 0.f;
+            const int i = node / (nq * nq), j = (node / nq) % nq, k = node % nq;
+            const double jd = (wq[i] * wq[j] * wq[k]) * (jacob * (double)f);
+            m[0] += jd;
+            m[1] += jd * V1;
+            m[2] += jd * V0 * V0;
+            m[3] += jd * V1 * V1;
+            m[4] += jd * V2 * V2;
+            m[5] += jd * V0 * V2;
+        }
+    }
+    for (int qq = 0; qq < 6; qq++) {
+        double v = m[qq];
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+        if (lane == 0) s_red[warp * 6 + qq] = v;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (tid < 6) {
+        double sacc = 0;
+        for (int w = 0; w < 8; w++) sacc += s_red[w * 6 + tid];
+        partial[((size_t)p * B + chunk) * 6 + tid] = sacc;
+    }
+    if (aborted) {  // let the group's outstanding commit land before TMEM is freed
+        tc::mbar_wait(bar, phase ^ 1u);
+        if (gt == 0 && err) atomicExch(err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_slot), "r"(256) : "memory");
+}
+
+}  // namespace fj
+
 namespace {
 
 int sg_grid(fj_surrogate *s, const fj_potential *pot, int ngauss, const fj_quad_rule *rule, fj::SgGrid &g)
@@ -826,25 +1083,56 @@ int fj_surrogate_fit(fj_surrogate *s, const fj_potential *pot, const fj_df_param
 }
 
 int fj_surrogate_moments(fj_surrogate *s, const fj_potential *pot, const fj_df_params *df, const fj_quad_rule *rule,
-                         int ngauss, double *grids6, double *ms)
+                         int ngauss, double *grids6, double *ms, int fused)
 {
     if (!s || !df || !grids6 || df->kind != FJ_DF_DPL) return FJ_ERR_ARG;
     fj::SgGrid g;
     int rc = sg_grid(s, pot, ngauss, rule, g);
     if (rc) return rc;
-    if ((rc = sg_infer_buffers(s))) return rc;
     const double *ci, *xq, *wq;
     if ((rc = fj::context_grid_inputs(s->ctx, ngauss, rule, &ci, &xq, &wq))) return rc;
     const int npts = pot->nr * ngauss, nq3 = rule->nq * rule->nq * rule->nq;
-    if (npts > s->partial_cap) {
+    const int B = fused ? (nq3 + fj::kFusedMaxNodes - 1) / fj::kFusedMaxNodes : 1;
+    if ((long long)npts * B > s->partial_cap) {
         void *q;
-        if ((rc = sg_alloc(s, &q, (size_t)npts * 6 * sizeof(double)))) return rc;
+        if ((rc = sg_alloc(s, &q, (size_t)npts * B * 6 * sizeof(double)))) return rc;
         s->partial = (double *)q;
-        s->partial_cap = npts;
+        s->partial_cap = (long long)npts * B;
     }
+    const fj::DFDev dd = sg_df(df);
+    if (fused) {  // features, MLP and moment sums in one kernel
+        static bool attr = false;
+        const size_t smem = fj::fused_smem_bytes();
+        if (!attr) {
+            if (cudaFuncSetAttribute(fj::k_sg_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess)
+                return FJ_ERR_CUDA;
+            attr = true;
+        }
+        fj::SgWeights w;
+        for (int l = 0; l < fj::kLayers; l++) { w.W[l] = s->Wb + s->woff[l]; w.b[l] = s->P + s->boff[l]; }
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, s->stream);
+        fj::k_sg_fused<<<npts * B, fj::kFusedThreads, smem, s->stream>>>(g, w, wq, dd, B, s->partial, s->err);
+        cudaEventRecord(e1, s->stream);
+        if (cudaGetLastError() != cudaSuccess) return FJ_ERR_CUDA;
+        fj::MomentArgs a{};
+        a.partial = s->partial; a.npts = npts; a.blocks_per_point = B; a.out6 = grids6;
+        if (fj::launch_moments_finalize(a, s->stream) != cudaSuccess) return FJ_ERR_CUDA;
+        if ((rc = sg_check_err(s))) return rc;
+        float t = 0;
+        cudaEventElapsedTime(&t, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (ms) *ms = t;
+        return FJ_OK;
+    }
+    if ((rc = sg_infer_buffers(s))) return rc;
     if (nq3 > kInferRows) return FJ_ERR_ARG;
     const int per = kInferRows / nq3;  // whole grid points per inference pass
-    const fj::DFDev d = sg_df(df);
+    const fj::DFDev &d = dd;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -871,4 +1159,5 @@ int fj_surrogate_moments(fj_surrogate *s, const fj_potential *pot, const fj_df_p
 }
 
 }  // extern "C"
+
 

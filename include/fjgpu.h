@@ -189,11 +189,14 @@ int fj_surrogate_predict(fj_surrogate *s, const float *X, long long n, float *Y)
 int fj_surrogate_fit(fj_surrogate *s, const fj_potential *pot, const fj_df_params *df, int ngauss,
                      const fj_quad_rule *rule, const float *J, long long samples, unsigned long long seed, int epochs,
                      float lr, double *loss);
-/* computeRhl with the surrogate's actions: features of every velocity node
-   of the grid, the MLP on the tensor cores, the double-power-law DF and the
-   moment sums into grids6 device [6][nr*ngauss]; ms = device time. */
+/* computeRhl with the surrogate's actions: the features of every bound
+   velocity node of the grid, the MLP on the tensor cores, the double-power-law
+   DF and the moment sums into grids6 device [6][nr*ngauss]; ms = device time.
+   fused = 1: one kernel per grid point (weights resident in shared memory,
+   accumulators in tensor memory, nothing but the sums leaves the chip);
+   fused = 0: features, GEMMs and sums as separate passes through memory. */
 int fj_surrogate_moments(fj_surrogate *s, const fj_potential *pot, const fj_df_params *df, const fj_quad_rule *rule,
-                         int ngauss, double *grids6, double *ms);
+                         int ngauss, double *grids6, double *ms, int fused);
 
 /* Configuration of the mixed-precision phase-space kernel (no reference
    counterpart: the reference has one CPU loop).  variant 0..7: 0..3 run each
