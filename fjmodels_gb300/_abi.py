@@ -99,7 +99,7 @@ SIGNATURES = {
     "fj_surrogate_predict": ([C.c_void_p, C.c_void_p, C.c_longlong, C.c_void_p], C.c_int),
     "fj_set_action_output": ([CTX, C.c_void_p], C.c_int),
     "fj_surrogate_fit": ([C.c_void_p, P(fj_potential), P(fj_df_params), C.c_int, P(fj_quad_rule), C.c_void_p,
-                          C.c_longlong, C.c_ulonglong, C.c_int, C.c_float, DP], C.c_int),
+                          C.c_void_p, C.c_longlong, C.c_ulonglong, C.c_int, C.c_float, DP], C.c_int),
     "fj_surrogate_moments": ([C.c_void_p, P(fj_potential), P(fj_df_params), P(fj_quad_rule), C.c_int, C.c_void_p,
                               DP, C.c_int], C.c_int),
     "fj_run_model_surrogate": ([CTX, P(fj_model_config), P(fj_surrogate_schedule), C.c_void_p, P(fj_model_result),

@@ -515,10 +515,11 @@ class Surrogate:
                  "fj_surrogate_train")
         return float(loss[0])
 
-    def fit(self, pot, df, ngauss, rule, jout, samples, seed=1, epochs=1, lr=1e-3):
+    def fit(self, pot, df, ngauss, rule, jout, samples, seed=1, epochs=1, lr=1e-3, rho=None):
         loss = np.zeros(1)
         self._rc(self.lib.fj_surrogate_fit(self.h, C.byref(pot.c), C.byref(df.c), ngauss, C.byref(rule.c),
-                                           _ptr(jout), samples, seed, epochs, lr, _dp(loss)), "fj_surrogate_fit")
+                                           _ptr(jout), _ptr(rho) if rho is not None else None, samples, seed, epochs,
+                                           lr, _dp(loss)), "fj_surrogate_fit")
         return float(loss[0])
 
     def moments(self, pot, df, rule, ngauss, grids6, fused=True):

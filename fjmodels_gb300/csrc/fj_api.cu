@@ -1356,7 +1356,8 @@ extern "C" int fj_run_model_surrogate(fj_ctx *ctx, const fj_model_config *cfg, c
             if (fit) {
                 auto tf = now();
                 double loss = 0;
-                if ((rc = fj_surrogate_fit(sg, &pot, &cfg->df, ng, &cfg->rule, jout, sch->samples, sch->seed + (unsigned)k,
+                if ((rc = fj_surrogate_fit(sg, &pot, &cfg->df, ng, &cfg->rule, jout, d_grids, sch->samples,
+                                           sch->seed + (unsigned)k,
                                            rp.fits ? sch->epochs : sch->epochs_first, sch->lr, &loss)))
                     return fail(ctx, rc, "run_model_surrogate: fit");
                 rp.fits++;

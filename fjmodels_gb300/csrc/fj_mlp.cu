@@ -224,8 +224,9 @@ __global__ void k_weight_t(int rows, int cols, const float *w, __nv_bfloat16 *wt
     wt[(size_t)c * rows + r] = __float2bfloat16_rn(w[i]);
 }
 
-// dY = 2 (Y - T) / (B * kUsedOut) on the used outputs (bf16, zero elsewhere); loss sum
-__global__ void k_mse_grad(int B, const float *y, const float *t, __nv_bfloat16 *dy, float *loss)
+// dY = 2 w (Y - T) / (B * kUsedOut) on the used outputs (bf16, zero elsewhere),
+// w = per-row weight (1 if wt is null); loss = the weighted mean of squares
+__global__ void k_mse_grad(int B, const float *y, const float *t, const float *wt, __nv_bfloat16 *dy, float *loss)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float l = 0.f;
@@ -233,9 +234,10 @@ __global__ void k_mse_grad(int B, const float *y, const float *t, __nv_bfloat16 
         const int b = i / kOut, o = i % kOut;
         float g = 0.f;
         if (o < kUsedOut) {
+            const float w = wt ? wt[b] : 1.f;
             const float d = y[i] - t[b * kUsedOut + o];
-            g = 2.f * d / (float)(B * kUsedOut);
-            l = d * d;
+            g = 2.f * w * d / (float)(B * kUsedOut);
+            l = w * d * d;
         }
         dy[i] = __float2bfloat16_rn(g);
     }
@@ -284,7 +286,7 @@ struct fj_surrogate {
     int *err = nullptr;
     __nv_bfloat16 *Xi = nullptr, *Hi = nullptr;  // inference workspace
     float *Xf = nullptr, *Yf = nullptr;           // f32 features / outputs of one inference pass
-    float *fitX = nullptr, *fitT = nullptr;       // training rows (fj_surrogate_fit), fit_cap rows
+    float *fitX = nullptr, *fitT = nullptr, *fitW = nullptr;  // training rows (fj_surrogate_fit), fit_cap rows
     long long *fitIdx = nullptr;
     long long fit_cap = 0;
     double *partial = nullptr;                    // surrogate moment sums [npts][6]
@@ -363,14 +365,14 @@ int sg_forward(fj_surrogate *s, const __nv_bfloat16 *X, int n, float *out, bool 
 
 // gradients of the mean-squared error of one training batch (after sg_forward
 // with keep) into G; T f32 [batch][2]
-int sg_backward(fj_surrogate *s, const float *T)
+int sg_backward(fj_surrogate *s, const float *T, const float *Wt)
 {
     const int B = s->batch, ks = (B + 4095) / 4096;
     const size_t hb = (size_t)B * fj::kHid;
     int rc;
     SG_CUDA(cudaMemsetAsync(s->G, 0, s->nparam * sizeof(float), s->stream));
     __nv_bfloat16 *dY = s->dZ + hb;  // [B][16], after the two dZ buffers' first
-    fj::k_mse_grad<<<(B * fj::kOut + 255) / 256, 256, 0, s->stream>>>(B, s->Y, T, dY, s->loss);
+    fj::k_mse_grad<<<(B * fj::kOut + 255) / 256, 256, 0, s->stream>>>(B, s->Y, T, Wt, dY, s->loss);
     // output layer: gW4 = dY^T H3, gb4 = colsum(dY), dZ3 = (dY W4) * gelu'(Z3)
     if ((rc = sg_transpose(s, B, fj::kOut, dY, s->dZT))) return rc;
     if ((rc = sg_transpose(s, B, fj::kHid, s->H + 3 * hb, s->HT))) return rc;
@@ -435,13 +437,13 @@ int sg_check_err(fj_surrogate *s)
 }
 
 // one training step on rows [r0, r0 + batch) of X f32 [n][16], T f32 [n][2]
-int sg_step(fj_surrogate *s, const float *X, const float *T, float lr)
+int sg_step(fj_surrogate *s, const float *X, const float *T, const float *Wt, float lr)
 {
     const int B = s->batch;
     fj::k_to_bf16<<<(B * fj::kIn + 255) / 256, 256, 0, s->stream>>>(B * fj::kIn, X, s->X);
     int rc;
     if ((rc = sg_forward(s, s->X, B, s->Y, true, s->H, B))) return rc;
-    if ((rc = sg_backward(s, T))) return rc;
+    if ((rc = sg_backward(s, T, Wt))) return rc;
     s->step++;
     const float b1 = 0.9f, b2 = 0.999f;
     const float alpha = lr * sqrtf(1.f - powf(b2, (float)s->step)) / (1.f - powf(b1, (float)s->step));
@@ -565,7 +567,7 @@ int fj_surrogate_gradients(fj_surrogate *s, const float *X, const float *T, doub
     fj::k_to_bf16<<<(B * fj::kIn + 255) / 256, 256, 0, s->stream>>>(B * fj::kIn, X, s->X);
     int rc;
     if ((rc = sg_forward(s, s->X, B, s->Y, true, s->H, B))) return rc;
-    if ((rc = sg_backward(s, T))) return rc;
+    if ((rc = sg_backward(s, T, nullptr))) return rc;
     if ((rc = sg_check_err(s))) return rc;
     std::vector<float> g(s->nparam);
     float l = 0;
@@ -577,8 +579,19 @@ int fj_surrogate_gradients(fj_surrogate *s, const float *X, const float *T, doub
     return FJ_OK;
 }
 
+static int sg_train(fj_surrogate *s, const float *X, const float *T, const float *Wt, long long n, int epochs,
+                    float lr, double *final_loss);
+
 int fj_surrogate_train(fj_surrogate *s, const float *X, const float *T, long long n, int epochs, float lr,
                        double *final_loss)
+{
+    return sg_train(s, X, T, nullptr, n, epochs, lr, final_loss);
+}
+
+}  // extern "C"
+
+static int sg_train(fj_surrogate *s, const float *X, const float *T, const float *Wt, long long n, int epochs,
+                    float lr, double *final_loss)
 {
     if (!s || !X || !T || n < s->batch || epochs < 1 || !(lr > 0)) return FJ_ERR_ARG;
     const long long steps = n / s->batch;
@@ -586,7 +599,8 @@ int fj_surrogate_train(fj_surrogate *s, const float *X, const float *T, long lon
     for (int e = 0; e < epochs; e++)
         for (long long k = 0; k < steps; k++) {
             if (e == epochs - 1 && k == steps - 1) SG_CUDA(cudaMemsetAsync(s->loss, 0, sizeof(float), s->stream));
-            if ((rc = sg_step(s, X + (size_t)k * s->batch * fj::kIn, T + (size_t)k * s->batch * fj::kUsedOut, lr)))
+            if ((rc = sg_step(s, X + (size_t)k * s->batch * fj::kIn, T + (size_t)k * s->batch * fj::kUsedOut,
+                              Wt ? Wt + (size_t)k * s->batch : nullptr, lr)))
                 return rc;
         }
     if ((rc = sg_check_err(s))) return rc;
@@ -598,6 +612,8 @@ int fj_surrogate_train(fj_surrogate *s, const float *X, const float *T, long lon
     }
     return FJ_OK;
 }
+
+extern "C" {
 
 int fj_surrogate_predict(fj_surrogate *s, const float *X, long long n, float *Y)
 {
@@ -694,16 +710,16 @@ __global__ void k_sg_features(SgGrid g, const long long *idx, long long first, l
 
 // training rows from exact actions J [npts * nq^3][2] (unbound or E >= 0: NaN or
 // 1e31): sample s takes node hash(seed, s) (the next valid one after it, within 64)
-__global__ void k_sg_sample(SgGrid g, DFDev df, const float *J, long long total, unsigned long long seed, long long ns,
-                            long long *idx, float *T)
+__global__ void k_sg_sample(SgGrid g, DFDev df, const float *J, const double *rho, const double *wq, long long total,
+                            unsigned long long seed, long long ns, long long *idx, float *T, float *Wt)
 {
     const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (s >= ns) return;
-    unsigned long long h = seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(s + 1);
-    h = (h ^ (h >> 30)) * 0xBF58476D1CE4E5B9ull;
-    h = (h ^ (h >> 27)) * 0x94D049BB133111EBull;
-    h ^= h >> 31;
-    long long id = (long long)(h % (unsigned long long)total);
+    unsigned long long hs = seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(s + 1);
+    hs = (hs ^ (hs >> 30)) * 0xBF58476D1CE4E5B9ull;
+    hs = (hs ^ (hs >> 27)) * 0x94D049BB133111EBull;
+    hs ^= hs >> 31;
+    long long id = (long long)(hs % (unsigned long long)total);
     bool ok = false;
     for (int t = 0; t < 64 && !ok; t++) {
         const long long q = (id + t) % total;
@@ -715,8 +731,20 @@ __global__ void k_sg_sample(SgGrid g, DFDev df, const float *J, long long total,
     double V0, V1, V2, H, R;
     sg_velocity(g, p, node, V0, V1, V2, H, R);
     const double jr = ok ? J[2 * id] : 0., jz = ok ? J[2 * id + 1] : 0., jp = fabs(R * V1);
-    T[2 * s] = (float)log(jr + df.dphi_h * jp + df.dz_h * jz + 1e-12);
-    T[2 * s + 1] = (float)log(jr + df.dphi_g * jp + df.dz_g * jz + 1e-12);
+    const double h = jr + df.dphi_h * jp + df.dz_h * jz, gg = jr + df.dphi_g * jp + df.dz_g * jz;
+    T[2 * s] = (float)log(h + 1e-12);
+    T[2 * s + 1] = (float)log(gg + 1e-12);
+    // weight: a floor plus the node's share of its point's density (x nq^3)
+    float w = ok ? 1.f : 0.f;
+    if (ok && rho && rho[p] > 0) {
+        const double Jphi = R * V1, Ve = g.point[2 * p + 1];
+        double f = df.norm * fmax(0., pow(1. + df.J0 / h, df.alpha) / pow(1. + gg / df.J0, df.beta)) / df.tpi3;
+        if (df.chi != 0.) f += df.k * tanh(df.chi * Jphi / df.J0) * f;
+        const int nq = g.nq;
+        const double share = wq[node / (nq * nq)] * wq[(node / nq) % nq] * wq[node % nq] * Ve * Ve * Ve * f / rho[p];
+        w = (float)fmin(100., 0.2 + (double)nq3 * share);
+    }
+    Wt[s] = w;
 }
 
 // moment sums of grid point p0 + blockIdx.x from the surrogate outputs Y (rows from
@@ -1057,8 +1085,8 @@ int sg_grid(fj_surrogate *s, const fj_potential *pot, int ngauss, const fj_quad_
 extern "C" {
 
 int fj_surrogate_fit(fj_surrogate *s, const fj_potential *pot, const fj_df_params *df, int ngauss,
-                     const fj_quad_rule *rule, const float *J, long long nsamples, unsigned long long seed, int epochs,
-                     float lr, double *loss)
+                     const fj_quad_rule *rule, const float *J, const double *rho, long long nsamples,
+                     unsigned long long seed, int epochs, float lr, double *loss)
 {
     if (!s || !J || !df || nsamples < s->batch || epochs < 1) return FJ_ERR_ARG;
     fj::SgGrid g;
@@ -1073,13 +1101,17 @@ int fj_surrogate_fit(fj_surrogate *s, const fj_potential *pot, const fj_df_param
         s->fitT = (float *)q;
         if ((rc = sg_alloc(s, &q, (size_t)ns * sizeof(long long)))) return rc;
         s->fitIdx = (long long *)q;
+        if ((rc = sg_alloc(s, &q, (size_t)ns * sizeof(float)))) return rc;
+        s->fitW = (float *)q;
         s->fit_cap = ns;
     }
     const long long total = (long long)pot->nr * ngauss * rule->nq * rule->nq * rule->nq;
-    fj::k_sg_sample<<<(unsigned)((ns + 255) / 256), 256, 0, s->stream>>>(g, sg_df(df), J, total, seed, ns, s->fitIdx,
-                                                                         s->fitT);
+    const double *ci, *xq, *wq;
+    if ((rc = fj::context_grid_inputs(s->ctx, ngauss, rule, &ci, &xq, &wq))) return rc;
+    fj::k_sg_sample<<<(unsigned)((ns + 255) / 256), 256, 0, s->stream>>>(g, sg_df(df), J, rho, wq, total, seed, ns,
+                                                                         s->fitIdx, s->fitT, s->fitW);
     fj::k_sg_features<<<(unsigned)((ns + 255) / 256), 256, 0, s->stream>>>(g, s->fitIdx, 0, ns, s->fitX);
-    return fj_surrogate_train(s, s->fitX, s->fitT, ns, epochs, lr, loss);
+    return sg_train(s, s->fitX, s->fitT, s->fitW, ns, epochs, lr, loss);
 }
 
 int fj_surrogate_moments(fj_surrogate *s, const fj_potential *pot, const fj_df_params *df, const fj_quad_rule *rule,

@@ -185,10 +185,12 @@ int fj_surrogate_predict(fj_surrogate *s, const float *X, long long n, float *Y)
 /* Fit to the exact actions J of a grid iteration (from fj_set_action_output,
    in potential pot): `samples` rows drawn with `seed` among bound nodes,
    features built on the device, targets log h and log g of the DF df,
-   `epochs` of Adam at lr. */
+   `epochs` of Adam at lr.  rho (device [nr*ngauss], the same iteration's
+   densities; may be NULL) weights each row by 0.2 + nq^3 x the node's share
+   of its point's density, so the fit concentrates where the density is. */
 int fj_surrogate_fit(fj_surrogate *s, const fj_potential *pot, const fj_df_params *df, int ngauss,
-                     const fj_quad_rule *rule, const float *J, long long samples, unsigned long long seed, int epochs,
-                     float lr, double *loss);
+                     const fj_quad_rule *rule, const float *J, const double *rho, long long samples,
+                     unsigned long long seed, int epochs, float lr, double *loss);
 /* computeRhl with the surrogate's actions: the features of every bound
    velocity node of the grid, the MLP on the tensor cores, the double-power-law
    DF and the moment sums into grids6 device [6][nr*ngauss]; ms = device time.
