@@ -112,9 +112,11 @@ def _nfw_80_tanh():
 
 def test_surrogate_moments_gain(ctx):
     """Fit to one exact iteration of the 80 x 40 rotating NFW workload (22^3 tanh-sinh
-    nodes), then the surrogate's grid of moments: much faster than the exact mixed
-    kernel, densities within a few per cent (the surrogate serves the early
-    iterations only; the last ones are exact)."""
+    nodes), then the surrogate's grid of moments.  The fused tensor-core kernel equals
+    the separate passes and is > 20x faster than the exact mixed kernel; the
+    densities are only within tens of per cent (median 15 % measured), so the
+    schedule's audit keeps the iterations exact -- the accuracy bound here guards
+    against regressions of the fit, not a target."""
     from fjmodels_gb300 import _abi as A
     (nr, ng, npl), tabs, (E, D) = _nfw_80_tanh()
     pot, delta = ctx.potential(*tabs), ctx.delta(E, D)
@@ -144,6 +146,7 @@ def test_surrogate_moments_gain(ctx):
     rel = np.abs(a - b) / b
     print(f"surrogate: fit loss {loss:.3e}, moments {ms:.1f} ms vs exact {st.kernel_ms:.1f} ms, "
           f"rho rel err median {np.median(rel):.2e} p90 {np.percentile(rel, 90):.2e} max {rel.max():.2e}")
+    assert np.median(rel) < 0.3
     s.close()
 
 
