@@ -43,6 +43,8 @@ struct PotViewF {
     int nr, npoly;
     const float *ar, *phil, *Pr, *ih, *qc;
     float out0, shift, lr0, idl;
+    float c2pt;         // cos^2 of the polar angle of the grid point
+    const float *pyl;   // P_2k(c2pt), k < npoly
 };
 
 // even-Legendre recurrence P_2k from P_2k-2, P_2k-4 (include/UtilsLeg.h:43-50)
@@ -237,72 +239,106 @@ FJ_HDNI void pot_grad_f(const PotViewF &P, float R, float z, float &phi, float &
 // extrapolation) minus Phipt, the FP32 potential at the point.  All three
 // run in the same loop over the multipoles, each l's term being
 //   vb a_l + (vt - vb) b_l + (v_thr - vb - f3 (vt - vb)) g_l
-// with per-position coefficients, so the lanes of a warp do not split
-// between them.
-FJ_HDNI float pot_dphi_f(const PotViewF &P, float R, float z, float rpt, float c2pt, float dr2, float dc2,
-                         float Phipt)
+// with per-position coefficients selected without branches, so the lanes of
+// a warp do not split between them.  P_k(y) is the point's table P.pyl.
+struct DState {
+    int mode;  // 0: difference, 1: direct, 2: extrapolated
+    int b, thr;
+    bool quad;
+    float f1, f2, f3, f1p, f2p, df1, df2, x, dc2, xe2, xp1, sum0, phipt;
+};
+
+FJ_HD void dphi_setup(const PotViewF &P, float R, float z, float rpt, float dr2, float dc2, float Phipt, DState &s)
 {
     const float r = sqrtf(R * R + z * z);
     const float *ar = P.ar;
-    const int nr = P.nr, np_ = P.npoly;
+    const int nr = P.nr;
     const float a0 = ar[0], rmax = ar[nr - 1];
-    int mode;  // 0: difference, 1: direct, 2: extrapolated
-    int b = nr - 2, thr = 0;
-    bool quad = false;
-    float f1 = 0.f, f2 = 0.f, f3 = 0.f, f1p = 0.f, f2p = 0.f, df1 = 0.f, df2 = 0.f, xe = 0.f;
-    if (r >= rmax) {
-        mode = 2;
-        xe = rmax / r;
+    s.b = nr - 2; s.thr = 0; s.quad = false;
+    s.f1 = s.f2 = s.f3 = s.f1p = s.f2p = s.df1 = s.df2 = 0.f;
+    s.xe2 = 1.f; s.xp1 = 1.f; s.sum0 = 0.f;
+    s.phipt = Phipt; s.dc2 = dc2;
+    if (r >= rmax) {  // phi_l = phil[nr-1][l] (rmax/r)^(2l+1); the monopole from the unshifted table value
+        s.mode = 2;
+        const float xe = rmax / r;
+        s.xe2 = xe * xe;
+        s.xp1 = xe * s.xe2;
+        s.sum0 = P.out0 * xe - P.shift;
     } else {
         const float re = fmaxf(r, a0), rpe = fmaxf(rpt, a0);
         InterpF I;
         interp_setup_f(P, re, I);
-        b = I.bot; thr = I.thr; quad = I.quad; f1 = I.f1; f2 = I.f2; f3 = I.f3;
-        const float ab = ar[b], at = ar[b + 1];
-        mode = 1;
+        s.b = I.bot; s.thr = I.thr; s.quad = I.quad; s.f1 = I.f1; s.f2 = I.f2; s.f3 = I.f3;
+        const float ab = ar[s.b], at = ar[s.b + 1];
+        s.mode = 1;
         if (rpt < rmax && rpe >= ab && rpe <= at) {
-            const float fp = (rpe - ab) * P.ih[b];
-            const int thr_p = (fp < 0.5f && b > 0) ? b - 1 : b + 2;
-            if (!quad || thr_p == thr || rpe == ab || rpe == at) {
-                mode = 0;
-                f1p = fp;
-                f2p = quad ? (rpe - at) * (rpe - ab) * I.q : 0.f;
+            const float fp = (rpe - ab) * P.ih[s.b];
+            const int thr_p = (fp < 0.5f && s.b > 0) ? s.b - 1 : s.b + 2;
+            if (!s.quad || thr_p == s.thr || rpe == ab || rpe == at) {
+                s.mode = 0;
+                s.f1p = fp;
+                s.f2p = s.quad ? (rpe - at) * (rpe - ab) * I.q : 0.f;
                 const float dr = (r >= a0 && rpt >= a0) ? dr2 / (r + rpt) : re - rpe;
-                df1 = dr * P.ih[b];
-                df2 = quad ? I.q * dr * (re + rpe - ab - at) : 0.f;
+                s.df1 = dr * P.ih[s.b];
+                s.df2 = s.quad ? I.q * dr * (re + rpe - ab - at) : 0.f;
             }
         }
     }
+    s.x = s.mode == 0 ? P.c2pt + dc2 : (z * z) / (r * r);
+}
+
+// the term of multipole k: px = P_k(x), dk = P_k(x) - P_k(y), xp the
+// extrapolation factor (1 in the other modes)
+FJ_HD void dphi_acc(const PotViewF &P, const DState &s, float &sum, int k, float px, float dk, float xp)
+{
+    const int np_ = P.npoly;
     const float *T = P.phil;
-    const LegCoefF &L = leg_f();
-    const float y = c2pt, x = mode == 0 ? c2pt + dc2 : (z * z) / (r * r);
-    const float xe2 = xe * xe;
-    float xp = xe;
-    float px1 = 1.f, px2 = 0.f, py1 = 1.f, py2 = 0.f, d1 = 0.f, d2 = 0.f;
-    float sum = mode == 2 ? P.out0 * xe - P.shift : 0.f;  // extrapolated monopole, unshifted table value
-    for (int k = 0; k < np_; k++) {
-        const float vb = T[b * np_ + k], d = T[(b + 1) * np_ + k] - vb;
-        const float e = quad ? T[thr * np_ + k] - vb - f3 * d : 0.f;
-        float px, py, dk;
-        if (k == 0) { px = 1.f; py = 1.f; dk = 0.f; }
-        else if (k == 1) { px = 1.5f * x - .5f; py = 1.5f * y - .5f; dk = 1.5f * dc2; }
-        else {
-            px = ((x - L.B[k]) * px1 - L.A[k] * px2) * L.C[k];
-            py = ((y - L.B[k]) * py1 - L.A[k] * py2) * L.C[k];
-            dk = ((x - L.B[k]) * d1 + dc2 * py1 - L.A[k] * d2) * L.C[k];
+    const float vb = T[s.b * np_ + k], d = T[(s.b + 1) * np_ + k] - vb;
+    const float e = s.quad ? T[s.thr * np_ + k] - vb - s.f3 * d : 0.f;
+    const float t = xp * px;
+    const bool m0 = s.mode == 0, m1 = s.mode == 1;
+    const float ca = m0 ? dk : t;
+    const float cb = m0 ? s.df1 * px + s.f1p * dk : (m1 ? s.f1 * px : t);
+    const float cg = m0 ? s.df2 * px + s.f2p * dk : s.f2 * px;
+    sum += vb * ca + d * cb + e * cg;
+}
+
+FJ_HD float dphi_end(const DState &s, float sum) { return s.mode == 0 ? sum : sum - s.phipt; }
+
+// one multipole chain: Legendre recurrences of x and of the difference
+struct DChain {
+    float px1, px2, d1, d2, xp, sum;
+    FJ_HD void begin(const PotViewF &P, const DState &s)
+    {
+        sum = s.sum0;
+        dphi_acc(P, s, sum, 0, 1.f, 0.f, s.mode == 2 ? 0.f : 1.f);  // the extrapolated monopole is in sum0
+        px2 = 1.f; d2 = 0.f;
+        if (P.npoly > 1) {
+            px1 = 1.5f * s.x - .5f;
+            d1 = 1.5f * s.dc2;
+            dphi_acc(P, s, sum, 1, px1, d1, s.xp1);
         }
-        float ca, cb, cg;
-        if (mode == 0) { ca = dk; cb = df1 * px + f1p * dk; cg = df2 * px + f2p * dk; }
-        else if (mode == 1) { ca = px; cb = f1 * px; cg = f2 * px; }
-        else {  // phi_l = phil[nr-1][l] (rmax/r)^(2l+1)
-            const float t = k == 0 ? 0.f : xp * px;
-            ca = t; cb = t; cg = 0.f;
-        }
-        xp *= xe2;
-        sum += vb * ca + d * cb + e * cg;
-        px2 = px1; px1 = px; py2 = py1; py1 = py; d2 = d1; d1 = dk;
+        xp = s.xp1 * s.xe2;
     }
-    return mode == 0 ? sum : sum - Phipt;
+    FJ_HD void step(const PotViewF &P, const LegCoefF &L, const DState &s, int k)
+    {
+        const float px = ((s.x - L.B[k]) * px1 - L.A[k] * px2) * L.C[k];
+        const float dk = ((s.x - L.B[k]) * d1 + s.dc2 * P.pyl[k - 1] - L.A[k] * d2) * L.C[k];
+        dphi_acc(P, s, sum, k, px, dk, xp);
+        xp *= s.xe2;
+        px2 = px1; px1 = px; d2 = d1; d1 = dk;
+    }
+};
+
+FJ_HD float pot_dphi_f(const PotViewF &P, float R, float z, float rpt, float dr2, float dc2, float Phipt)
+{
+    DState s;
+    dphi_setup(P, R, z, rpt, dr2, dc2, Phipt, s);
+    DChain c;
+    c.begin(P, s);
+    const LegCoefF &L = leg_f();
+    for (int k = 2; k < P.npoly; k++) c.step(P, L, s, k);
+    return dphi_end(s, c.sum);
 }
 
 // Brent root (wrp_GSLroots rule, include/Utils.h:134-167) in FP32; the
@@ -374,19 +410,49 @@ FJ_HD float rescale_err_f(float err, float resabs, float resasc)
 
 struct GK21f { float xgk[11], wgk[11], wg[5]; };
 
-template <class F>
-FJ_HDNI void gk21_f(F &f, const GK21f &K, float a, float b, float &res, float &abserr, float &resabs, float &resasc)
+// FP32 products and sums that are never contracted into an FMA, so a value
+// computed in different code (one lane's panel or a warp's shared panel) has
+// the same bits
+FJ_HD float mul_rn(float x, float y)
 {
-    float fv1[11], fv2[11];
-    const float center = 0.5f * (a + b), half = 0.5f * (b - a), ahalf = fabsf(half);
-    const float fc = f(center);
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(x, y);
+#else
+    return x * y;
+#endif
+}
+FJ_HD float add_rn(float x, float y)
+{
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(x, y);
+#else
+    return x + y;
+#endif
+}
+
+// The e-th (0..20) abscissa of the 21-point Gauss-Kronrod panel on [a, b], in
+// the evaluation order of gk21_f: the centre, then -/+ the Gauss-point
+// offsets xgk[1], xgk[3], .., xgk[9], then -/+ xgk[0], xgk[2], .., xgk[8]
+FJ_HD float gk21_abscissa(const GK21f &K, float a, float b, int e)
+{
+    const float center = mul_rn(0.5f, add_rn(a, b)), half = mul_rn(0.5f, add_rn(b, -a));
+    if (e == 0) return center;
+    const int jj = e <= 10 ? 2 * ((e - 1) >> 1) + 1 : 2 * ((e - 11) >> 1);
+    const float x = mul_rn(half, K.xgk[jj]);
+    return ((e - 1) & 1) ? add_rn(center, x) : add_rn(center, -x);
+}
+
+// The panel's sums (QUADPACK DQK21) over the 21 values v[e] in that order
+FJ_HD void gk21_sum(const GK21f &K, float a, float b, const float *v, float &res, float &abserr, float &resabs,
+                    float &resasc)
+{
+    const float half = mul_rn(0.5f, add_rn(b, -a)), ahalf = fabsf(half);
+    const float fc = v[0];
     float rg = 0, rk = fc * K.wgk[10], ra = fabsf(rk);
     FJ_UNROLL
     for (int j = 0; j < 5; j++) {
         const int jj = 2 * j + 1;
-        const float x = half * K.xgk[jj];
-        const float f1 = f(center - x), f2 = f(center + x);
-        fv1[jj] = f1; fv2[jj] = f2;
+        const float f1 = v[1 + 2 * j], f2 = v[2 + 2 * j];
         rg += K.wg[j] * (f1 + f2);
         rk += K.wgk[jj] * (f1 + f2);
         ra += K.wgk[jj] * (fabsf(f1) + fabsf(f2));
@@ -394,20 +460,30 @@ FJ_HDNI void gk21_f(F &f, const GK21f &K, float a, float b, float &res, float &a
     FJ_UNROLL
     for (int j = 0; j < 5; j++) {
         const int jj = 2 * j;
-        const float x = half * K.xgk[jj];
-        const float f1 = f(center - x), f2 = f(center + x);
-        fv1[jj] = f1; fv2[jj] = f2;
+        const float f1 = v[11 + 2 * j], f2 = v[12 + 2 * j];
         rk += K.wgk[jj] * (f1 + f2);
         ra += K.wgk[jj] * (fabsf(f1) + fabsf(f2));
     }
     const float mean = 0.5f * rk;
     float rasc = K.wgk[10] * fabsf(fc - mean);
     FJ_UNROLL
-    for (int j = 0; j < 10; j++) rasc += K.wgk[j] * (fabsf(fv1[j] - mean) + fabsf(fv2[j] - mean));
+    for (int jj = 0; jj < 10; jj++) {
+        const float f1 = (jj & 1) ? v[jj] : v[11 + jj], f2 = (jj & 1) ? v[jj + 1] : v[12 + jj];
+        rasc += K.wgk[jj] * (fabsf(f1 - mean) + fabsf(f2 - mean));
+    }
     const float err = (rk - rg) * half;
     rk *= half; ra *= ahalf; rasc *= ahalf;
     res = rk; resabs = ra; resasc = rasc;
     abserr = rescale_err_f(err, ra, rasc);
+}
+
+template <class F>
+FJ_HDNI void gk21_f(F &f, const GK21f &K, float a, float b, float &res, float &abserr, float &resabs, float &resasc)
+{
+    float v[21];
+    FJ_UNROLL
+    for (int e = 0; e < 21; e++) v[e] = f(gk21_abscissa(K, a, b, e));
+    gk21_sum(K, a, b, v, res, abserr, resabs, resasc);
 }
 
 FJ_HD void qelg_f(float *tab, int &n_io, float *res3, int &nres, float &result, float &abserr)
@@ -464,16 +540,33 @@ constexpr int kQagsCapF = 64;
 
 // QAGS (DQAGSE) in FP32 on [a,b] with the reference's tolerances; interval
 // list of kQagsCapF entries on the thread's stack.
+// QUADPACK DQAGSE (the reference's QAGS through wrp_GSLinteg) in two parts:
+// the first panel with its two early exits, and the rest -- bisection of the
+// interval of largest error, the error-ordered list (DQPSRT) and the Wynn
+// epsilon extrapolation (DQELG) -- whose pairs of half-interval panels come
+// from Pn::two, evaluated by one lane (LanePanels) or by a warp (CoopPanels).
+struct QagsHead { float a, b, res0, err0, resabs0, resasc0; };
+
+FJ_HD bool qags_head_done(const QagsHead &h, float epsabs, float epsrel)
+{
+    const float tol = fmaxf(epsabs, epsrel * fabsf(h.res0));
+    if (h.err0 <= 100 * FLT_EPSILON * h.resabs0 && h.err0 > tol) return true;
+    return (h.err0 <= tol && h.err0 != h.resasc0) || h.err0 == 0.0f;
+}
+
 template <class F>
-FJ_HDNI float qags_f(F &f, const GK21f &K, float a, float b, float epsabs, float epsrel, unsigned &fail)
+FJ_HD bool qags_first_f(F &f, const GK21f &K, float a, float b, float epsabs, float epsrel, QagsHead &h)
+{
+    h.a = a; h.b = b;
+    gk21_f(f, K, a, b, h.res0, h.err0, h.resabs0, h.resasc0);
+    return qags_head_done(h, epsabs, epsrel);
+}
+
+template <class Pn>
+FJ_HDNI float qags_rest_f(Pn &pn, const QagsHead &h, float epsabs, float epsrel, unsigned &fail)
 {
     const int limit = 1000;
-    float res0, err0, resabs0, resasc0;
-    gk21_f(f, K, a, b, res0, err0, resabs0, resasc0);
-    const float tol = fmaxf(epsabs, epsrel * fabsf(res0));
-    if (err0 <= 100 * FLT_EPSILON * resabs0 && err0 > tol) return res0;
-    if ((err0 <= tol && err0 != resasc0) || err0 == 0.0f) return res0;
-
+    const float a = h.a, b = h.b, res0 = h.res0, err0 = h.err0, resabs0 = h.resabs0;
     float alist[kQagsCapF], blist[kQagsCapF], rlist[kQagsCapF], elist[kQagsCapF];
     int iord[kQagsCapF];
     float rlist2[52], res3la[3];
@@ -492,8 +585,7 @@ FJ_HDNI float qags_f(F &f, const GK21f &K, float a, float b, float epsabs, float
         const float a2 = b1, b2 = blist[maxerr];
         const float erlast = errmax;
         float area1, error1, ra1, rasc1, area2, error2, ra2, rasc2;
-        gk21_f(f, K, a1, b1, area1, error1, ra1, rasc1);
-        gk21_f(f, K, a2, b2, area2, error2, ra2, rasc2);
+        pn.two(a1, b1, a2, b2, area1, error1, ra1, rasc1, area2, error2, ra2, rasc2);
         const float area12 = area1 + area2, erro12 = error1 + error2;
         errsum = errsum + erro12 - errmax;
         area = area + area12 - rlist[maxerr];
@@ -630,6 +722,27 @@ FJ_HDNI float qags_f(F &f, const GK21f &K, float a, float b, float epsabs, float
     return result;
 }
 
+template <class F>
+struct LanePanels {
+    F &f;
+    const GK21f &K;
+    FJ_HD void two(float a1, float b1, float a2, float b2, float &r1, float &e1, float &ra1, float &rc1, float &r2,
+                   float &e2, float &ra2, float &rc2)
+    {
+        gk21_f(f, K, a1, b1, r1, e1, ra1, rc1);
+        gk21_f(f, K, a2, b2, r2, e2, ra2, rc2);
+    }
+};
+
+template <class F>
+FJ_HD float qags_f(F &f, const GK21f &K, float a, float b, float epsabs, float epsrel, unsigned &fail)
+{
+    QagsHead h;
+    if (qags_first_f(f, K, a, b, epsabs, epsrel, h)) return h.res0;
+    LanePanels<F> pn{f, K};
+    return qags_rest_f(pn, h, epsabs, epsrel, fail);
+}
+
 // ----------------------------------------------------------- fudge, FP32
 // The u and v equations of uvOrb.cpp:38-52 written about the phase point
 // itself, in offsets that keep their relative precision when the orbit's
@@ -652,7 +765,7 @@ FJ_HDNI float qags_f(F &f, const GK21f &K, float a, float b, float epsabs, float
 struct FudgeF {
     PotViewF P;
     float Delta, D2, K, EC, C0, Lt, shu2, sv2, swp, svp, sinv, cosv, sinhu, coshu, pvterm;
-    float rpt, c2pt, Phipt;  // the point: radius, cos^2 of its polar angle, FP32 potential
+    float rpt, Phipt;  // the point: radius and FP32 potential
     double u_pt;
     float tb, Dt;  // Ju: centre and half-width of [t_in, t_out]
     float wt;      // Jv: turning point in w
@@ -663,12 +776,12 @@ struct FudgeF {
 // Deltau cos psi) and Jv (uvOrb.cpp:247-257, v = pi/2 - (pi/2 - vturn) cos psi).
 enum : int { kEvU = 0, kEvVw = 1, kEvVv = 2, kEvJu = 3, kEvJv = 4 };
 
-// The one evaluator of every FP32 turning-point search and momentum
-// integral: the position on the coordinate line and the exact geometry
-// differences, a single pot_dphi_f, then U or V as A + B dPhi.  Kept out of
-// line, so Brent, the bracket walks and QAGS each exist once in the binary
-// and the divergent warps' working set fits the instruction cache.
-FJ_HDNI float fudge_eval(const FudgeF &o, int mode, float x)
+// geometry of a position on the coordinate line, and U or V = A + Bc dPhi
+struct FGeo {
+    float R, z, dr2, dc2, A, Bc, fac;
+};
+
+FJ_HD void fudge_geom(const FudgeF &o, int mode, float x, FGeo &G)
 {
     float fac = 1.f;
     int m = mode;
@@ -683,7 +796,7 @@ FJ_HDNI float fudge_eval(const FudgeF &o, int mode, float x)
             else { x = kPIHf - w; m = kEvVv; }
         }
     }
-    float R, z, dr2, dc2, A, Bc;
+    G.fac = fac;
     if (m == kEvU) {
         float s, c, Ds, KE;
         if (fabsf(x) < .5f) {  // offsets: no cancellation for |t| < 1/2
@@ -702,12 +815,12 @@ FJ_HDNI float fudge_eval(const FudgeF &o, int mode, float x)
             KE = s * s * o.K + o.C0;
         }
         const float s2 = s * s, cv2 = o.swp * o.swp;
-        R = o.Delta * s * o.sinv;
-        z = o.Delta * c * o.cosv;
-        dr2 = o.D2 * Ds;
-        dc2 = -cv2 * o.sv2 * Ds / ((s2 + cv2) * (o.shu2 + cv2));
-        A = KE + (o.Lt > 0.f ? o.Lt * Ds / (s2 * o.shu2) : 0.f);
-        Bc = -(s2 + o.sv2);
+        G.R = o.Delta * s * o.sinv;
+        G.z = o.Delta * c * o.cosv;
+        G.dr2 = o.D2 * Ds;
+        G.dc2 = -cv2 * o.sv2 * Ds / ((s2 + cv2) * (o.shu2 + cv2));
+        G.A = KE + (o.Lt > 0.f ? o.Lt * Ds / (s2 * o.shu2) : 0.f);
+        G.Bc = -(s2 + o.sv2);
     } else {
         float sn, cs, Dv;
         sincosf(x, &sn, &cs);
@@ -718,16 +831,31 @@ FJ_HDNI float fudge_eval(const FudgeF &o, int mode, float x)
             Dv = (sn - o.svp) * (sn + o.svp);  // sin^2 v - sin^2 v_pt
         }
         const float s2 = sn * sn;
-        R = o.Delta * o.sinhu * sn;
-        z = o.Delta * o.coshu * cs;
-        dr2 = -o.D2 * Dv;
-        dc2 = -(1.f + o.shu2) * o.shu2 * Dv / ((o.shu2 + cs * cs) * (o.shu2 + o.swp * o.swp));
-        A = Dv * (o.K + (o.Lt > 0.f ? o.Lt / (o.sv2 * s2) : 0.f)) + o.pvterm;
-        Bc = -(o.shu2 + s2);
+        G.R = o.Delta * o.sinhu * sn;
+        G.z = o.Delta * o.coshu * cs;
+        G.dr2 = -o.D2 * Dv;
+        G.dc2 = -(1.f + o.shu2) * o.shu2 * Dv / ((o.shu2 + cs * cs) * (o.shu2 + o.swp * o.swp));
+        G.A = Dv * (o.K + (o.Lt > 0.f ? o.Lt / (o.sv2 * s2) : 0.f)) + o.pvterm;
+        G.Bc = -(o.shu2 + s2);
     }
-    const float dphi = pot_dphi_f(o.P, R, z, o.rpt, o.c2pt, dr2, dc2, o.Phipt);
-    const float val = A + Bc * dphi;
-    return mode >= kEvJu ? sqrtf(fmaxf(0.f, val)) * fac : val;
+}
+
+FJ_HD float fudge_finish(int mode, const FGeo &G, float dphi)
+{
+    const float val = G.A + G.Bc * dphi;
+    return mode >= kEvJu ? sqrtf(fmaxf(0.f, val)) * G.fac : val;
+}
+
+// The one evaluator of every FP32 turning-point search and momentum
+// integral: the position on the coordinate line and the exact geometry
+// differences, a single pot_dphi_f, then U or V as A + B dPhi.  Kept out of
+// line, so Brent, the bracket walks and QAGS each exist once in the binary
+// and the divergent warps' working set fits the instruction cache.
+FJ_HDNI float fudge_eval(const FudgeF &o, int mode, float x)
+{
+    FGeo G;
+    fudge_geom(o, mode, x, G);
+    return fudge_finish(mode, G, pot_dphi_f(o.P, G.R, G.z, o.rpt, G.dr2, G.dc2, o.Phipt));
 }
 
 // dU/du for the bracket's slope tests (uvOrb.cpp:54-61); E - Phi = K - (Phi - Phi_pt)
@@ -865,8 +993,31 @@ FJ_HDNI void fudge64_at_point(Fudge &o, const PotView &P, double Delta, double L
 // FP32 tables of PotViewF for the phase point whose potential is Phi_h;
 // entries i0, i0 + stride, ... (a block's threads share the work).  ih has
 // nr-1 entries, qc 4*kQuadIntervals.
+// cos^2 of the polar angle of the grid point (R, z) and the even Legendre
+// polynomials there, P_2k(c2) for k < npoly, by the recurrence of leg_f
+FJ_HD float point_c2_f(double R, double z)
+{
+    const double r2 = R * R + z * z;
+    return r2 > 0 ? (float)(z * z / r2) : 1.f;
+}
+
+FJ_HD void point_legendre_f(float y, int npoly, float *pyl)
+{
+    const LegCoefF &L = leg_f();
+    float p1 = 1.f, p2 = 1.f;
+    for (int k = 0; k < npoly; k++) {
+        const float pk = k == 0 ? 1.f : (k == 1 ? 1.5f * y - .5f : ((y - L.B[k]) * p1 - L.A[k] * p2) * L.C[k]);
+        pyl[k] = pk;
+        p2 = p1; p1 = pk;
+    }
+}
+
+// FP32 tables of one grid point (R, z): radii, potential multipoles shifted by
+// Phi_h, interval reciprocals, quadratic-correction constants and P_2k(c2pt);
+// threads i0, i0 + stride, ... share the work
 FJ_HD void mixed_tables_f(int nr, int npoly, const double *ar, const double *phil, const double *Pr, double Phi_h,
-                          float *far, float *fphil, float *fPr, float *ih, float *qc, int i0, int stride)
+                          double R, double z, float *far, float *fphil, float *fPr, float *ih, float *qc, float *pyl,
+                          int i0, int stride)
 {
     for (int i = i0; i < nr; i += stride) far[i] = (float)ar[i];
     for (int i = i0; i < nr - 1; i += stride) ih[i] = (float)(1.0 / (ar[i + 1] - ar[i]));
@@ -881,11 +1032,13 @@ FJ_HD void mixed_tables_f(int nr, int npoly, const double *ar, const double *phi
         fphil[i] = (float)(i % npoly == 0 ? phil[i] - Phi_h : phil[i]);
         fPr[i] = (float)Pr[i];
     }
+    if (i0 == 0) point_legendre_f(point_c2_f(R, z), npoly, pyl);
 }
 
 // PotViewF over tables built by mixed_tables_f
-FJ_HD PotViewF mixed_view_f(int nr, int npoly, const double *ar, const double *phil, double Phi_h, const float *far,
-                            const float *fphil, const float *fPr, const float *ih, const float *qc)
+FJ_HD PotViewF mixed_view_f(int nr, int npoly, const double *ar, const double *phil, double Phi_h, double R, double z,
+                            const float *far, const float *fphil, const float *fPr, const float *ih, const float *qc,
+                            const float *pyl)
 {
     PotViewF v;
     v.nr = nr; v.npoly = npoly; v.ar = far; v.phil = fphil; v.Pr = fPr; v.ih = ih; v.qc = qc;
@@ -893,6 +1046,8 @@ FJ_HD PotViewF mixed_view_f(int nr, int npoly, const double *ar, const double *p
     v.shift = (float)Phi_h;
     v.lr0 = (float)log(ar[0]);
     v.idl = (float)((nr - 1) / log(ar[nr - 1] / ar[0]));
+    v.c2pt = point_c2_f(R, z);
+    v.pyl = pyl;
     return v;
 }
 
@@ -901,11 +1056,27 @@ FJ_HD PotViewF mixed_view_f(int nr, int npoly, const double *ar, const double *p
 // with FP32 turning points and QAGS, FP64 turning points at the limits, and
 // the double-power-law DF (DF.cpp:65-76,108-119) in FP32.  PF is shifted by
 // PF.shift = Phi_h (mixed_tables_f); the node's energy enters shifted too.
-// Returns the DF (NaN -> 0 as DF.cpp:105); fail gets the kFail* bits,
-// esc = 1 when the FP64 turning-point path ran; J (optional) the actions.
-FJ_HDNI double mixed_node_df(const PotView &P, const PotViewF &PF, const GK21f &K, const DFDev &d, double Delta,
-                             double R, double z, double Phi_h, double V0, double V1, double V2, unsigned &fail,
-                             unsigned &esc, double *J = nullptr)
+// The work is split where the two momentum integrals have had their first
+// QAGS panel (mixed_node_begin), so that the rest of each integral can run on
+// one lane (mixed_node_df) or on the whole warp (the kernel's cooperative form).
+struct MixedNode {
+    FudgeF o;
+    QagsHead hu, hv;  // first panels of the Ju and Jv integrals
+    double Lz, Jr, Jz;
+    bool pend_u, pend_v;  // the integral goes on past its first panel
+};
+
+FJ_HD double mixed_ju(const FudgeF &o, float q) { return (double)(1.41421356237309505f * o.Delta * o.Dt * q / kPIf); }
+FJ_HD double mixed_jv(const FudgeF &o, float q)
+{
+    return (double)(2.f * 1.41421356237309505f * o.Delta * o.wt * q / kPIf);
+}
+
+// The node up to the first panels: fail gets the kFail* bits, esc = 1 when
+// the FP64 turning-point path ran
+FJ_HDNI void mixed_node_begin(const PotView &P, const PotViewF &PF, const GK21f &K, double Delta, double R, double z,
+                              double Phi_h, double V0, double V1, double V2, MixedNode &n, unsigned &fail,
+                              unsigned &esc)
 {
     const double Lz = R * V1, Lzsq = Lz * Lz;
     const double D2 = Delta * Delta, R2 = R * R, z2 = z * z, r2 = R2 + z2;
@@ -919,64 +1090,70 @@ FJ_HDNI double mixed_node_df(const PotView &P, const PotViewF &PF, const GK21f &
     const double pu = Delta * (V0 * chu * sv + V2 * shu * cv);
     const double pv = Delta * (V0 * shu * cv - V2 * chu * sv);
     const double E = .5 * (V0 * V0 + V2 * V2) + .5 * Lzsq / R2 + Phi_h;
-    double Jr = 1e31, Jz = 1e31;
-    if (!(E >= 0 || isnan(E))) {
-        FudgeF o;
-        o.P = PF;
-        o.Delta = (float)Delta;
-        o.D2 = (float)D2;
-        o.K = (float)(.5 * (V0 * V0 + V2 * V2) + .5 * Lzsq / R2);
-        o.EC = (float)(.5 * (pu * pu) / D2);
-        o.C0 = (float)(.5 * (pu * pu) / D2 - shu2 * (.5 * (V0 * V0 + V2 * V2) + .5 * Lzsq / R2));
-        o.Lt = (float)(.5 * Lzsq / D2);
-        o.shu2 = (float)shu2;
-        o.sv2 = (float)sv2;
-        o.swp = (float)fabs(cv);
-        o.svp = (float)sqrt(sv2);
-        double sn, cs;
-        sincos(v, &sn, &cs);
-        o.sinv = (float)sn; o.cosv = (float)cs;
-        o.sinhu = (float)shu; o.coshu = (float)chu;
-        o.pvterm = (float)(.5 * (pv * pv) / D2);
-        o.u_pt = u;
-        o.rpt = (float)(Delta * sqrt(shu2 + cv2));
-        o.c2pt = (float)((1 + shu2) * cv2 / (shu2 + cv2));
-        o.Phipt = pot_phi_f(PF, o.Delta * o.sinhu * o.sinv, o.Delta * o.coshu * o.cosv);
-        Fudge o64;
-        bool have64 = false;
-        const float rtwo = 1.41421356237309505f;
-        float tin, tout;
-        if (!get_turn_u_f(o, 1.0, tin, tout, fail)) {  // u limit: FP64 (uvOrb.cpp:131-201)
-            fudge64_at_point(o64, P, Delta, Lzsq, E, u, v, shu2, sv, cv, sv2, pu, pv);
-            have64 = true;
-            get_turn_u(o64, 1);
-            fail |= o64.fail;
-            tin = (float)(o64.uinner - u); tout = (float)(o64.uouter - u);
-            esc = 1u;
-        }
-        if (fabsf(tout - tin) < 1e-12f) Jr = 0;
-        else {
-            o.tb = .5f * (tin + tout);
-            o.Dt = .5f * (tout - tin);
-            const FudgeFn fju{&o, kEvJu};
-            Jr = (double)(rtwo * o.Delta * o.Dt * qags_f(fju, K, 0.f, kPIf, 1e-5f, 1e-3f, fail) / kPIf);
-        }
-        float wt;
-        if (!get_turn_v_f(o, wt, fail)) {  // v at the pole: FP64 (uvOrb.cpp:203-224)
-            if (!have64) fudge64_at_point(o64, P, Delta, Lzsq, E, u, v, shu2, sv, cv, sv2, pu, pv);
-            const double v64 = get_turn_v(o64, .5 * kPIH);
-            fail |= o64.fail;
-            wt = (float)(kPIH - v64);
-            esc = 1u;
-        }
-        if (wt < 1e-12f) Jz = 0;
-        else {
-            o.wt = wt;
-            const FudgeFn fjv{&o, kEvJv};
-            Jz = (double)(2.f * rtwo * o.Delta * wt * qags_f(fjv, K, 0.f, kPIHf, 1e-5f, 1e-3f, fail) / kPIf);
-        }
+    n.Lz = Lz;
+    n.Jr = 1e31; n.Jz = 1e31;
+    n.pend_u = n.pend_v = false;
+    if (E >= 0 || isnan(E)) return;
+    FudgeF &o = n.o;
+    o.P = PF;
+    o.Delta = (float)Delta;
+    o.D2 = (float)D2;
+    o.K = (float)(.5 * (V0 * V0 + V2 * V2) + .5 * Lzsq / R2);
+    o.EC = (float)(.5 * (pu * pu) / D2);
+    o.C0 = (float)(.5 * (pu * pu) / D2 - shu2 * (.5 * (V0 * V0 + V2 * V2) + .5 * Lzsq / R2));
+    o.Lt = (float)(.5 * Lzsq / D2);
+    o.shu2 = (float)shu2;
+    o.sv2 = (float)sv2;
+    o.swp = (float)fabs(cv);
+    o.svp = (float)sqrt(sv2);
+    double sn, cs;
+    sincos(v, &sn, &cs);
+    o.sinv = (float)sn; o.cosv = (float)cs;
+    o.sinhu = (float)shu; o.coshu = (float)chu;
+    o.pvterm = (float)(.5 * (pv * pv) / D2);
+    o.u_pt = u;
+    o.rpt = (float)(Delta * sqrt(shu2 + cv2));
+    o.Phipt = pot_phi_f(PF, o.Delta * o.sinhu * o.sinv, o.Delta * o.coshu * o.cosv);
+    o.tb = o.Dt = o.wt = 0.f;
+    Fudge o64;
+    bool have64 = false;
+    float tin, tout;
+    if (!get_turn_u_f(o, 1.0, tin, tout, fail)) {  // u limit: FP64 (uvOrb.cpp:131-201)
+        fudge64_at_point(o64, P, Delta, Lzsq, E, u, v, shu2, sv, cv, sv2, pu, pv);
+        have64 = true;
+        get_turn_u(o64, 1);
+        fail |= o64.fail;
+        tin = (float)(o64.uinner - u); tout = (float)(o64.uouter - u);
+        esc = 1u;
     }
-    if (J) { J[0] = Jr; J[1] = Jz; }
+    if (fabsf(tout - tin) < 1e-12f) n.Jr = 0;
+    else {
+        o.tb = .5f * (tin + tout);
+        o.Dt = .5f * (tout - tin);
+        const FudgeFn fju{&o, kEvJu};
+        if (qags_first_f(fju, K, 0.f, kPIf, 1e-5f, 1e-3f, n.hu)) n.Jr = mixed_ju(o, n.hu.res0);
+        else n.pend_u = true;
+    }
+    float wt;
+    if (!get_turn_v_f(o, wt, fail)) {  // v at the pole: FP64 (uvOrb.cpp:203-224)
+        if (!have64) fudge64_at_point(o64, P, Delta, Lzsq, E, u, v, shu2, sv, cv, sv2, pu, pv);
+        const double v64 = get_turn_v(o64, .5 * kPIH);
+        fail |= o64.fail;
+        wt = (float)(kPIH - v64);
+        esc = 1u;
+    }
+    if (wt < 1e-12f) n.Jz = 0;
+    else {
+        o.wt = wt;
+        const FudgeFn fjv{&o, kEvJv};
+        if (qags_first_f(fjv, K, 0.f, kPIHf, 1e-5f, 1e-3f, n.hv)) n.Jz = mixed_jv(o, n.hv.res0);
+        else n.pend_v = true;
+    }
+}
+
+// The DF from the actions (NaN -> 0 as DF.cpp:105)
+FJ_HD double mixed_df(const DFDev &d, double Lz, double Jr, double Jz)
+{
     const float Jphi = (float)Lz, jr = (float)Jr, jz = (float)Jz, J0 = (float)d.J0;
     const float h = jr + (float)d.dphi_h * fabsf(Jphi) + (float)d.dz_h * jz;
     const float g = jr + (float)d.dphi_g * fabsf(Jphi) + (float)d.dz_g * jz;
@@ -985,6 +1162,27 @@ FJ_HDNI double mixed_node_df(const PotView &P, const PotViewF &PF, const GK21f &
     float f = d.chi == 0. ? ev : ev + (float)d.k * tanhf((float)d.chi * Jphi / J0) * ev;
     if (isnan(f)) f = 0.f;
     return (double)f;
+}
+
+// The whole node on one lane.  Returns the DF; J (optional) gets the actions.
+FJ_HDNI double mixed_node_df(const PotView &P, const PotViewF &PF, const GK21f &K, const DFDev &d, double Delta,
+                             double R, double z, double Phi_h, double V0, double V1, double V2, unsigned &fail,
+                             unsigned &esc, double *J = nullptr)
+{
+    MixedNode n;
+    mixed_node_begin(P, PF, K, Delta, R, z, Phi_h, V0, V1, V2, n, fail, esc);
+    if (n.pend_u) {
+        const FudgeFn fju{&n.o, kEvJu};
+        LanePanels<const FudgeFn> pn{fju, K};
+        n.Jr = mixed_ju(n.o, qags_rest_f(pn, n.hu, 1e-5f, 1e-3f, fail));
+    }
+    if (n.pend_v) {
+        const FudgeFn fjv{&n.o, kEvJv};
+        LanePanels<const FudgeFn> pn{fjv, K};
+        n.Jz = mixed_jv(n.o, qags_rest_f(pn, n.hv, 1e-5f, 1e-3f, fail));
+    }
+    if (J) { J[0] = n.Jr; J[1] = n.Jz; }
+    return mixed_df(d, n.Lz, n.Jr, n.Jz);
 }
 
 }  // namespace fj

@@ -9,7 +9,7 @@
 #include <cstdint>
 
 #include "fj_internal.h"
-#include "fj_mixed_wave.cuh"
+#include "fj_mixed.cuh"
 
 namespace fj {
 
@@ -19,11 +19,16 @@ namespace fj {
 // order, and its threads take the list round-robin.  So no lane idles on an
 // unbound node, each thread's nodes are summed in a fixed order, and the
 // per-block sums are added in a fixed order by k_moments_finalize.
-// The kernel is built in two forms -- each thread running its nodes' solves
-// as nested loops (mixed_node_df), or the wavefront form (MixedLane: every
-// lane's next potential difference evaluated at one call site per step) --
-// and each in four register budgets (launch bounds of 3, 4, 6 and 8 resident
-// blocks per SM: 168, 128, 80 and 64 registers): kMixedVariants builds.
+// The kernel is built in two forms and each in four register budgets (launch
+// bounds of 3, 4, 6 and 8 resident blocks per SM: 168, 128, 80 and 64
+// registers): kMixedVariants builds.
+//  - nested: each thread runs its node's solves to the end (mixed_node_df);
+//  - cooperative: each thread runs its node to the first QAGS panel of both
+//    momentum integrals (mixed_node_begin), then the warp takes the integrals
+//    that go on, one at a time, each bisection's 42 evaluations spread over
+//    its 32 lanes (CoopPanels).  The adaptive integrals' lengths vary from 1
+//    to ~60 panels between nodes, so one lane per integral leaves most lanes
+//    of a warp waiting for its longest one.  Both forms give the same bits.
 // Which one, and the chunk size, is a per-context setting (fj_autotune_mixed).
 int mixed_blocks_per_point(long long nq3, int chunk) { return (int)((nq3 + chunk - 1) / chunk); }
 
@@ -31,11 +36,38 @@ size_t moment_mixed_smem_bytes(const MomentArgs &a)
 {
     const size_t nt = (size_t)a.P.nr * a.P.npoly;
     return (a.P.nr + 3 * nt + 2 * a.ngrid + 2 * a.nq + 6 * (kMixedBlock / 32) + 4) * sizeof(double) +
-           (2 * a.P.nr + 2 * nt + 4 * kQuadIntervals) * sizeof(float) + sizeof(GK21f) + 16 +
-           (kMixedBlock / 32) * sizeof(int) + (size_t)a.mixed_chunk * sizeof(unsigned short);
+           (2 * a.P.nr + 2 * nt + 4 * kQuadIntervals + a.P.npoly) * sizeof(float) + sizeof(GK21f) + 16 +
+           (kMixedBlock / 32) * sizeof(int) + (size_t)a.mixed_chunk * sizeof(unsigned short) + 16 +
+           (kMixedBlock / 32) * (sizeof(FudgeF) + sizeof(QagsHead) + 42 * sizeof(float));
 }
 
-template <int MINB, bool WAVE>
+// Two half-interval panels of one node's integral evaluated by the 32 lanes
+// of a warp: evaluation e (0..41: panel e / 21, abscissa e % 21) on lane
+// e % 32, the values exchanged through the warp's shared buffer, and the sums
+// formed by every lane from the same values in the same order -- so every
+// lane holds LanePanels' result bit for bit, and the QAGS bookkeeping around
+// it runs uniformly on all lanes.
+struct CoopPanels {
+    const FudgeF *o;
+    int mode;
+    const GK21f &K;
+    float *buf;
+    int lane;
+    __device__ void two(float a1, float b1, float a2, float b2, float &r1, float &e1, float &ra1, float &rc1, float &r2,
+                        float &e2, float &ra2, float &rc2)
+    {
+        for (int e = lane; e < 42; e += 32) {
+            const bool second = e >= 21;
+            buf[e] = fudge_eval(*o, mode, gk21_abscissa(K, second ? a2 : a1, second ? b2 : b1, second ? e - 21 : e));
+        }
+        __syncwarp();
+        gk21_sum(K, a1, b1, buf, r1, e1, ra1, rc1);
+        gk21_sum(K, a2, b2, buf + 21, r2, e2, ra2, rc2);
+        __syncwarp();
+    }
+};
+
+template <int MINB, bool COOP>
 __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs a0, MomentBatch batch)
 {
     extern __shared__ double sm[];
@@ -51,10 +83,13 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
     double *s_Eg = s_Pr2 + nt, *s_Dg = s_Eg + a.ngrid, *s_xq = s_Dg + a.ngrid, *s_wq = s_xq + a.nq;
     double *s_red = s_wq + a.nq, *s_pt = s_red + 6 * (kMixedBlock / 32);
     float *f_ar = (float *)(s_pt + 4), *f_phil = f_ar + nr, *f_Pr = f_phil + nt, *f_ih = f_Pr + nt;
-    float *f_qc = f_ih + nr;
-    GK21f *sK = (GK21f *)(((uintptr_t)(f_qc + 4 * kQuadIntervals) + 15) & ~(uintptr_t)15);
+    float *f_qc = f_ih + nr, *f_pyl = f_qc + 4 * kQuadIntervals;
+    GK21f *sK = (GK21f *)(((uintptr_t)(f_pyl + npoly) + 15) & ~(uintptr_t)15);
     int *s_wc = (int *)(sK + 1);
     unsigned short *s_list = (unsigned short *)(s_wc + kMixedBlock / 32);
+    FudgeF *s_fud = (FudgeF *)(((uintptr_t)(s_list + a.mixed_chunk) + 15) & ~(uintptr_t)15);
+    QagsHead *s_head = (QagsHead *)(s_fud + kMixedBlock / 32);
+    float *s_buf = (float *)(s_head + kMixedBlock / 32);
     for (int i = threadIdx.x; i < nr; i += blockDim.x) s_ar[i] = a.P.ar[i];
     for (int i = threadIdx.x; i < nt; i += blockDim.x) {
         s_phil[i] = a.P.phil[i]; s_Pr[i] = a.P.Pr[i]; s_Pr2[i] = a.P.Pr2[i];
@@ -85,7 +120,8 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
     }
     __syncthreads();
     const double R = s_pt[0], z = s_pt[1], Phi_h = s_pt[2], Ve = s_pt[3];
-    mixed_tables_f(nr, npoly, s_ar, s_phil, s_Pr, Phi_h, f_ar, f_phil, f_Pr, f_ih, f_qc, threadIdx.x, blockDim.x);
+    mixed_tables_f(nr, npoly, s_ar, s_phil, s_Pr, Phi_h, R, z, f_ar, f_phil, f_Pr, f_ih, f_qc, f_pyl, threadIdx.x,
+                   blockDim.x);
     const int nq = a.nq, nq2 = nq * nq;
     const long long nq3 = (long long)nq2 * nq;
     const int n0 = (int)(chunk * nq3 / B), n1 = (int)((chunk + 1) * nq3 / B);
@@ -113,59 +149,71 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
         __syncthreads();
         nbound += tot;
     }
-    const PotViewF PF = mixed_view_f(nr, npoly, s_ar, s_phil, Phi_h, f_ar, f_phil, f_Pr, f_ih, f_qc);
+    const PotViewF PF = mixed_view_f(nr, npoly, s_ar, s_phil, Phi_h, R, z, f_ar, f_phil, f_Pr, f_ih, f_qc, f_pyl);
     const double jacob = Ve * Ve * Ve;
 
     double m[6] = {0, 0, 0, 0, 0, 0};
     unsigned failed = 0, esc = 0;
-    if (WAVE) {
-        // wavefront form: each step every active lane evaluates its pending request at
-        // the one call site below; a lane that completes a node takes its next one
-        MixedLane L;
-        int q = threadIdx.x;
-        double V0 = 0, V1 = 0, V2 = 0, wj = 0;
-        bool active = false;
-        int cur_node = 0;
-        auto accumulate = [&]() {
-            if (a.jout) {
-                float *jo = a.jout + ((size_t)p * nq3 + cur_node) * 2;
-                jo[0] = (float)L.Jr;
-                jo[1] = (float)L.Jz;
-            }
-            failed += L.fail ? 1u : 0u;
-            esc += L.esc;
-            const double DF = (L.fail & (kFailBracket | kFailRoot)) ? 0. : L.df(a.df);
-            const double jd = wj * (jacob * DF);
-            m[0] += jd;
-            m[1] += jd * V1;
-            m[2] += jd * V0 * V0;
-            m[3] += jd * V1 * V1;
-            m[4] += jd * V2 * V2;
-            m[5] += jd * V0 * V2;
-        };
-        auto next = [&]() {  // the lane's next node with a pending request, or none
-            while (q < nbound) {
-                const int node = n0 + s_list[q];
-                cur_node = node;
-                q += kMixedBlock;
-                const int i = node / nq2, j = (node / nq) % nq, k = node % nq;
-                V0 = 1e-6 + Ve * s_xq[i]; V1 = 1e-6 + Ve * s_xq[j]; V2 = 1e-6 + Ve * s_xq[k];
-                wj = s_wq[i] * s_wq[j] * s_wq[k];
+    auto accumulate = [&](int node, double V0, double V1, double V2, double Jr, double Jz, double f, unsigned fail) {
+        if (a.jout) {
+            float *jo = a.jout + ((size_t)p * nq3 + node) * 2;
+            jo[0] = (float)Jr;
+            jo[1] = (float)Jz;
+        }
+        failed += fail ? 1u : 0u;
+        const int i = node / nq2, j = (node / nq) % nq, k = node % nq;
+        const double DF = (fail & (kFailBracket | kFailRoot)) ? 0. : f;
+        const double jd = (s_wq[i] * s_wq[j] * s_wq[k]) * (jacob * DF);
+        m[0] += jd;
+        m[1] += jd * V1;
+        m[2] += jd * V0 * V0;
+        m[3] += jd * V1 * V1;
+        m[4] += jd * V2 * V2;
+        m[5] += jd * V0 * V2;
+    };
+    if (COOP) {
+        // rounds over the list in which every lane of the block takes at most
+        // one node, so the warp's lanes stay together for the cooperative part
+        FudgeF &wf = s_fud[warp];
+        float *wbuf = s_buf + warp * 42;
+        for (int q0 = 0; q0 < nbound; q0 += kMixedBlock) {
+            const int q = q0 + threadIdx.x;
+            const bool has = q < nbound;
+            const int node = has ? n0 + s_list[q] : 0;
+            const int i = node / nq2, j = (node / nq) % nq, k = node % nq;
+            const double V0 = 1e-6 + Ve * s_xq[i], V1 = 1e-6 + Ve * s_xq[j], V2 = 1e-6 + Ve * s_xq[k];
+            MixedNode n;
+            n.pend_u = n.pend_v = false;
+            unsigned fail = 0, e = 0;
+            if (has) {
                 const double H = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h;
-                if (L.begin(PF, deltafn(s_Eg, s_Dg, a.ngrid, H), R, z, Phi_h, V0, V1, V2)) return true;
-                accumulate();  // E >= 0 after rounding: Jr = Jz = 1e31
+                mixed_node_begin(P, PF, *sK, deltafn(s_Eg, s_Dg, a.ngrid, H), R, z, Phi_h, V0, V1, V2, n, fail, e);
             }
-            return false;
-        };
-        active = next();
-        while (__any_sync(0xffffffffu, active)) {
-            if (active) {
-                const float val = fudge_eval(L.o, L.mode, L.x);
-                const float dval = L.want_du ? fudge_du(L.o, L.xdu) : 0.f;
-                if (L.feed(P, *sK, val, dval)) {
-                    accumulate();
-                    active = next();
+            for (int which = 0; which < 2; which++) {
+                unsigned pend = __ballot_sync(0xffffffffu, which == 0 ? n.pend_u : n.pend_v);
+                while (pend) {
+                    const int owner = __ffs(pend) - 1;
+                    pend &= pend - 1;
+                    if (lane == owner) {
+                        wf = n.o;
+                        s_head[warp] = which == 0 ? n.hu : n.hv;
+                    }
+                    __syncwarp();
+                    const QagsHead h = s_head[warp];
+                    CoopPanels pn{&wf, which == 0 ? kEvJu : kEvJv, *sK, wbuf, lane};
+                    unsigned qf = 0;
+                    const float r = qags_rest_f(pn, h, 1e-5f, 1e-3f, qf);
+                    if (lane == owner) {
+                        fail |= qf;
+                        if (which == 0) n.Jr = mixed_ju(n.o, r);
+                        else n.Jz = mixed_jv(n.o, r);
+                    }
+                    __syncwarp();
                 }
+            }
+            if (has) {
+                esc += e;
+                accumulate(node, V0, V1, V2, n.Jr, n.Jz, mixed_df(a.df, n.Lz, n.Jr, n.Jz), fail);
             }
         }
     } else
@@ -178,21 +226,8 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
         const double Delta = deltafn(s_Eg, s_Dg, a.ngrid, H);
         double J[2];
         const double f = mixed_node_df(P, PF, *sK, a.df, Delta, R, z, Phi_h, V0, V1, V2, fail, e, J);
-        if (a.jout) {
-            float *jo = a.jout + ((size_t)p * nq3 + node) * 2;
-            jo[0] = (float)J[0];
-            jo[1] = (float)J[1];
-        }
         esc += e;
-        failed += fail ? 1u : 0u;
-        const double DF = (fail & (kFailBracket | kFailRoot)) ? 0. : f;
-        const double jd = (s_wq[i] * s_wq[j] * s_wq[k]) * (jacob * DF);
-        m[0] += jd;
-        m[1] += jd * V1;
-        m[2] += jd * V0 * V0;
-        m[3] += jd * V1 * V1;
-        m[4] += jd * V2 * V2;
-        m[5] += jd * V0 * V2;
+        accumulate(node, V0, V1, V2, J[0], J[1], f, fail);
     }
 #pragma unroll
     for (int q = 0; q < 6; q++) {
@@ -224,16 +259,16 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
 }
 
 namespace {
-template <int MINB, bool WAVE>
+template <int MINB, bool COOP>
 cudaError_t launch_variant(const MomentArgs &a, const MomentBatch &b, long long nblocks, size_t smem,
                            cudaStream_t s)
 {
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_moments_mixed<MINB, WAVE>,
+        cudaError_t e = cudaFuncSetAttribute(k_moments_mixed<MINB, COOP>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    k_moments_mixed<MINB, WAVE><<<(unsigned)nblocks, kMixedBlock, smem, s>>>(a, b);
+    k_moments_mixed<MINB, COOP><<<(unsigned)nblocks, kMixedBlock, smem, s>>>(a, b);
     return cudaGetLastError();
 }
 
@@ -253,11 +288,11 @@ cudaError_t launch_mixed_any(const MomentArgs &a, const MomentBatch &b, long lon
     }
 }
 
-template <int MINB, bool WAVE>
+template <int MINB, bool COOP>
 size_t local_bytes()
 {
     cudaFuncAttributes at;
-    return cudaFuncGetAttributes(&at, k_moments_mixed<MINB, WAVE>) == cudaSuccess ? at.localSizeBytes : 0;
+    return cudaFuncGetAttributes(&at, k_moments_mixed<MINB, COOP>) == cudaSuccess ? at.localSizeBytes : 0;
 }
 }  // namespace
 

@@ -202,18 +202,18 @@ int fj_surrogate_moments(fj_surrogate *s, const fj_potential *pot, const fj_df_p
 
 /* Configuration of the mixed-precision phase-space kernel (no reference
    counterpart: the reference has one CPU loop).  variant 0..7: 0..3 run each
-   node's solve as nested loops, 4..7 in the wavefront form (all lanes of a
-   warp evaluate their next potential difference together); within each, the
-   register budget of the build (launch bounds of 3, 4, 6, 8 resident blocks
-   per SM),
+   node's solve on one lane, 4..7 hand each momentum integral that goes on
+   past its first QAGS panel to the whole warp (the 42 evaluations of each
+   bisection on 32 lanes); within each, the register budget of the build
+   (launch bounds of 3, 4, 6, 8 resident blocks per SM),
    nodes_per_block = velocity nodes of one point per block (128..8192).
    fj_autotune_mixed times every variant x {2048, 4096, 8192} with
    fj_moments_points on the given device sample points (out6 device
    [6][npts] scratch), keeps the fastest in the context and returns its
    kernel time (all_ms, if not NULL: host [8][3] times of every variant x
    {2048, 4096, 8192}); results are the same in every configuration up to
-   the summation order of the per-thread sums (and, between the two forms,
-   the compiler's contraction of the same FP32 expressions). */
+   the summation order of the per-thread sums (the two forms give the same
+   bits at the same nodes_per_block). */
 int fj_set_mixed_config(fj_ctx *ctx, int variant, int nodes_per_block);
 int fj_get_mixed_config(fj_ctx *ctx, int *variant, int *nodes_per_block);
 int fj_autotune_mixed(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
