@@ -31,7 +31,7 @@ struct fj_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t own = nullptr;
     std::string err;
-    DevBuf partial, counters, poisson_ws, rule, misc;
+    DevBuf partial, counters, rule, misc;
     std::map<int, DevBuf> gauss_nodes;                 // ngauss -> [2][ngauss] (ci, wi)
     std::map<std::pair<int, int>, DevBuf> poly;        // (ngauss, npoly) -> [npoly][ngauss]
     std::map<int, DevBuf> gl_rules;                    // jquad -> [2][n]
@@ -347,7 +347,7 @@ int fj_ctx_destroy(fj_ctx *ctx)
     if (!ctx) return FJ_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (DevBuf *b : {&ctx->partial, &ctx->counters, &ctx->poisson_ws, &ctx->rule, &ctx->misc})
+    for (DevBuf *b : {&ctx->partial, &ctx->counters, &ctx->rule, &ctx->misc})
         if (b->p) cudaFree(b->p);
     for (auto &kv : ctx->gauss_nodes) cudaFree(kv.second.p);
     for (auto &kv : ctx->poly) cudaFree(kv.second.p);
@@ -473,7 +473,7 @@ int fj_autotune_mixed(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table
 {
     if (!ctx || !rule || rule->precision != FJ_PREC_MIXED || !Rz || npts < 1 || !out6)
         return fail(ctx, FJ_ERR_ARG, "autotune_mixed: needs a mixed-precision rule and sample points");
-    static const int chunks[] = {2048, 4096, 8192};
+    static const int chunks[] = {1024, 2048, 4096};
     const int v0 = ctx->mixed_variant, c0 = ctx->mixed_chunk;
     int bv = v0, bc = c0;
     double best = -1;
@@ -510,11 +510,9 @@ int fj_poisson(fj_ctx *ctx, int nr, int npoly, const double *ar, const double *r
 {
     if (!ctx || nr < 2 || npoly < 1 || npoly > kMaxPoly || !ar || !rhl || !phil || !Pr || !Pr2)
         return fail(ctx, FJ_ERR_ARG, "poisson: bad arguments");
-    int rc = ensure(ctx, ctx->poisson_ws, poisson_ws_bytes(nr, npoly));
+    int rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long));
     if (rc) return rc;
-    if ((rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long)))) return rc;
-    FJ_CUDA(launch_poisson(nr, npoly, ar, rhl, phil, Pr, Pr2, ctx->poisson_ws.p,
-                           (unsigned long long *)ctx->counters.p, ctx->stream));
+    FJ_CUDA(launch_poisson(nr, npoly, ar, rhl, phil, Pr, Pr2, (unsigned long long *)ctx->counters.p, ctx->stream));
     return FJ_OK;
 }
 

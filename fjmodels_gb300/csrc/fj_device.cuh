@@ -377,30 +377,77 @@ FJ_HD double rescale_err(double err, double resabs, double resasc)
     return err;
 }
 
-template <int RULE, class F>
-FJ_HD void gk_panel(F &f, double a, double b, double &res, double &abserr, double &resabs, double &resasc)
+// Gauss-Kronrod panels (DQK21, DQK15) as abscissas and sums, so that one
+// lane or a whole warp can evaluate a panel's function values: the e-th
+// abscissa (e < 2 nk - 1) in the evaluation order of the QUADPACK routine --
+// the centre, then -/+ the Gauss-point offsets xgk[1], xgk[3], .., then -/+
+// xgk[0], xgk[2], .. -- and the sums over the values in that order.
+template <int RULE>
+struct GKRule {
+    static constexpr int nk = RULE == 21 ? 11 : 8;  // Kronrod abscissas in [0, 1]
+    static constexpr int npts = 2 * nk - 1;         // function values per panel
+    static constexpr int n1 = (nk - 1) / 2;         // Gauss-point pairs
+};
+
+FJ_HD double dmul_rn(double x, double y)
 {
-    constexpr int nk = RULE == 21 ? 11 : 8;
 #ifdef __CUDA_ARCH__
-    const double *xgk = RULE == 21 ? fj_xgk21_d : fj_xgk15_d;
-    const double *wgk = RULE == 21 ? fj_wgk21_d : fj_wgk15_d;
-    const double *wg = RULE == 21 ? fj_wg10_d : fj_wg7_d;
+    return __dmul_rn(x, y);
 #else
-    const double *xgk = RULE == 21 ? fj_xgk21 : fj_xgk15;
-    const double *wgk = RULE == 21 ? fj_wgk21 : fj_wgk15;
-    const double *wg = RULE == 21 ? fj_wg10 : fj_wg7;
+    return x * y;
 #endif
-    double fv1[nk], fv2[nk];
-    const double center = 0.5 * (a + b), half = 0.5 * (b - a), ahalf = fabs(half);
-    const double fc = f(center);
+}
+FJ_HD double dadd_rn(double x, double y)
+{
+#ifdef __CUDA_ARCH__
+    return __dadd_rn(x, y);
+#else
+    return x + y;
+#endif
+}
+
+template <int RULE>
+FJ_HD void gk_tables(const double *&xgk, const double *&wgk, const double *&wg)
+{
+#ifdef __CUDA_ARCH__
+    xgk = RULE == 21 ? fj_xgk21_d : fj_xgk15_d;
+    wgk = RULE == 21 ? fj_wgk21_d : fj_wgk15_d;
+    wg = RULE == 21 ? fj_wg10_d : fj_wg7_d;
+#else
+    xgk = RULE == 21 ? fj_xgk21 : fj_xgk15;
+    wgk = RULE == 21 ? fj_wgk21 : fj_wgk15;
+    wg = RULE == 21 ? fj_wg10 : fj_wg7;
+#endif
+}
+
+template <int RULE>
+FJ_HD double gk_abscissa(double a, double b, int e)
+{
+    using G = GKRule<RULE>;
+    const double *xgk, *wgk, *wg;
+    gk_tables<RULE>(xgk, wgk, wg);
+    const double center = dmul_rn(0.5, dadd_rn(a, b)), half = dmul_rn(0.5, dadd_rn(b, -a));
+    if (e == 0) return center;
+    const int jj = e <= 2 * G::n1 ? 2 * ((e - 1) >> 1) + 1 : 2 * ((e - 1 - 2 * G::n1) >> 1);
+    const double x = dmul_rn(half, xgk[jj]);
+    return ((e - 1) & 1) ? dadd_rn(center, x) : dadd_rn(center, -x);
+}
+
+template <int RULE>
+FJ_HD void gk_sum(double a, double b, const double *v, double &res, double &abserr, double &resabs, double &resasc)
+{
+    using G = GKRule<RULE>;
+    constexpr int nk = G::nk, n1 = G::n1;
+    const double *xgk, *wgk, *wg;
+    gk_tables<RULE>(xgk, wgk, wg);
+    const double half = dmul_rn(0.5, dadd_rn(b, -a)), ahalf = fabs(half);
+    const double fc = v[0];
     double rg = 0, rk = fc * wgk[nk - 1], ra = fabs(rk);
     if (nk % 2 == 0) rg = fc * wg[nk / 2 - 1];
 FJ_UNROLL
-    for (int j = 0; j < (nk - 1) / 2; j++) {
+    for (int j = 0; j < n1; j++) {
         const int jj = 2 * j + 1;
-        const double x = half * xgk[jj];
-        const double f1 = f(center - x), f2 = f(center + x);
-        fv1[jj] = f1; fv2[jj] = f2;
+        const double f1 = v[1 + 2 * j], f2 = v[2 + 2 * j];
         rg += wg[j] * (f1 + f2);
         rk += wgk[jj] * (f1 + f2);
         ra += wgk[jj] * (fabs(f1) + fabs(f2));
@@ -408,20 +455,30 @@ FJ_UNROLL
 FJ_UNROLL
     for (int j = 0; j < nk / 2; j++) {
         const int jj = 2 * j;
-        const double x = half * xgk[jj];
-        const double f1 = f(center - x), f2 = f(center + x);
-        fv1[jj] = f1; fv2[jj] = f2;
+        const double f1 = v[1 + 2 * n1 + 2 * j], f2 = v[2 + 2 * n1 + 2 * j];
         rk += wgk[jj] * (f1 + f2);
         ra += wgk[jj] * (fabs(f1) + fabs(f2));
     }
     const double mean = 0.5 * rk;
     double rasc = wgk[nk - 1] * fabs(fc - mean);
 FJ_UNROLL
-    for (int j = 0; j < nk - 1; j++) rasc += wgk[j] * (fabs(fv1[j] - mean) + fabs(fv2[j] - mean));
+    for (int jj = 0; jj < nk - 1; jj++) {
+        const int em = (jj & 1) ? jj : 1 + 2 * n1 + jj;
+        rasc += wgk[jj] * (fabs(v[em] - mean) + fabs(v[em + 1] - mean));
+    }
     const double err = (rk - rg) * half;
     rk *= half; ra *= ahalf; rasc *= ahalf;
     res = rk; resabs = ra; resasc = rasc;
     abserr = rescale_err(err, ra, rasc);
+}
+
+template <int RULE, class F>
+FJ_HD void gk_panel(F &f, double a, double b, double &res, double &abserr, double &resabs, double &resasc)
+{
+    double v[GKRule<RULE>::npts];
+FJ_UNROLL
+    for (int e = 0; e < GKRule<RULE>::npts; e++) v[e] = f(gk_abscissa<RULE>(a, b, e));
+    gk_sum<RULE>(a, b, v, res, abserr, resabs, resasc);
 }
 
 // Wynn epsilon step (DQELG); tab[0..n-1] with room for n+2
@@ -488,18 +545,26 @@ struct QagsWs {
 // QAGS on [a,b].  limit is the reference's nominal limit (it only enters the
 // ordering rule of DQPSRT); ws.cap is the storage actually available.
 // Returns the QUADPACK error class (0 = success); fail gets kFailQuad on overflow.
-template <int RULE, class F>
-FJ_HDNI int qags(F &f, double a, double b, double epsabs, double epsrel, int limit, double &result,
-               double &abserr, unsigned &fail, const QagsWs &ws)
+// The first panel's early exits: returns the QUADPACK error class of a
+// finished call (result and abserr set), or -1 when the bisection goes on.
+FJ_HD int qags_head(double res0, double err0, double resabs0, double resasc0, double epsabs, double epsrel, int limit,
+                    double &result, double &abserr)
 {
-    const int CAP = ws.cap;
-    double res0, err0, resabs0, resasc0;
-    gk_panel<RULE>(f, a, b, res0, err0, resabs0, resasc0);
-    double tol = epsabs > epsrel * fabs(res0) ? epsabs : epsrel * fabs(res0);
+    const double tol = epsabs > epsrel * fabs(res0) ? epsabs : epsrel * fabs(res0);
     if (err0 <= 100 * DBL_EPSILON * resabs0 && err0 > tol) { result = res0; abserr = err0; return 2; }
     if ((err0 <= tol && err0 != resasc0) || err0 == 0.0) { result = res0; abserr = err0; return 0; }
     if (limit == 1) { result = res0; abserr = err0; return 1; }
+    return -1;
+}
 
+// The rest of QAGS after a first panel (res0, err0, resabs0) that did not
+// finish it: Pn::two evaluates the two half-interval panels of each bisection
+// (LanePanels64: one thread; the Poisson kernel's warp form: one warp).
+template <int RULE, class Pn>
+FJ_HDNI int qags_rest(Pn &pn, double a, double b, double res0, double err0, double resabs0, double epsabs,
+                      double epsrel, int limit, double &result, double &abserr, unsigned &fail, const QagsWs &ws)
+{
+    const int CAP = ws.cap;
     double *alist = ws.alist, *blist = ws.blist, *rlist = ws.rlist, *elist = ws.elist;
     int *iord = ws.iord;
     double rlist2[52], res3la[3];
@@ -520,8 +585,7 @@ FJ_HDNI int qags(F &f, double a, double b, double epsabs, double epsrel, int lim
         const double a2 = b1, b2 = blist[maxerr];
         const double erlast = errmax;
         double area1, error1, ra1, rasc1, area2, error2, ra2, rasc2;
-        gk_panel<RULE>(f, a1, b1, area1, error1, ra1, rasc1);
-        gk_panel<RULE>(f, a2, b2, area2, error2, ra2, rasc2);
+        pn.two(a1, b1, a2, b2, area1, error1, ra1, rasc1, area2, error2, ra2, rasc2);
         const double area12 = area1 + area2, erro12 = error1 + error2;
         errsum = errsum + erro12 - errmax;
         area = area + area12 - rlist[maxerr];
@@ -677,6 +741,29 @@ FJ_HDNI int qags(F &f, double a, double b, double epsabs, double epsrel, int lim
     }
     if (ier > 2) ier--;
     return ier;
+}
+
+template <int RULE, class F>
+struct LanePanels64 {
+    F &f;
+    FJ_HD void two(double a1, double b1, double a2, double b2, double &r1, double &e1, double &ra1, double &rc1,
+                   double &r2, double &e2, double &ra2, double &rc2)
+    {
+        gk_panel<RULE>(f, a1, b1, r1, e1, ra1, rc1);
+        gk_panel<RULE>(f, a2, b2, r2, e2, ra2, rc2);
+    }
+};
+
+template <int RULE, class F>
+FJ_HDNI int qags(F &f, double a, double b, double epsabs, double epsrel, int limit, double &result,
+               double &abserr, unsigned &fail, const QagsWs &ws)
+{
+    double res0, err0, resabs0, resasc0;
+    gk_panel<RULE>(f, a, b, res0, err0, resabs0, resasc0);
+    const int h = qags_head(res0, err0, resabs0, resasc0, epsabs, epsrel, limit, result, abserr);
+    if (h >= 0) return h;
+    LanePanels64<RULE, F> pn{f};
+    return qags_rest<RULE>(pn, a, b, res0, err0, resabs0, epsabs, epsrel, limit, result, abserr, fail, ws);
 }
 
 // ----------------------------------------------------------------------------

@@ -86,11 +86,11 @@ cudaError_t launch_potential_eval(PotView P, const double *Rz, size_t n, double 
 // projection: poly [npoly][ngauss] = 2 P_2l(c_g) w_g
 cudaError_t launch_project(int nr, int ngauss, int npoly, const double *ar, const double *poly,
                            const double *grids6, double *coef6, cudaStream_t s);
-// Poisson: ws = scratch for 2*nr*npoly QAGS interval lists of kPoissonCap entries
+// Poisson: one warp per (n, l), QAGS interval lists of kPoissonCap entries in
+// shared memory (no device workspace)
 constexpr int kPoissonCap = 256;
-size_t poisson_ws_bytes(int nr, int npoly);
 cudaError_t launch_poisson(int nr, int npoly, const double *ar, const double *rhl, double *phil,
-                           double *Pr, double *Pr2, void *ws, unsigned long long *counters, cudaStream_t s);
+                           double *Pr, double *Pr2, unsigned long long *counters, cudaStream_t s);
 cudaError_t launch_sum3(int n, const double *a0, const double *a1, const double *a2, const double *b0,
                         const double *b1, const double *b2, double *o0, double *o1, double *o2, cudaStream_t s);
 // o = a + b elementwise (summed component densities)

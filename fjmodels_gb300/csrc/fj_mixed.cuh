@@ -410,9 +410,8 @@ FJ_HD float rescale_err_f(float err, float resabs, float resasc)
 
 struct GK21f { float xgk[11], wgk[11], wg[5]; };
 
-// FP32 products and sums that are never contracted into an FMA, so a value
-// computed in different code (one lane's panel or a warp's shared panel) has
-// the same bits
+// FP32 products and sums that are never contracted into an FMA: the panel
+// abscissas have the same bits wherever the code is compiled (device, host)
 FJ_HD float mul_rn(float x, float y)
 {
 #ifdef __CUDA_ARCH__
@@ -540,33 +539,16 @@ constexpr int kQagsCapF = 64;
 
 // QAGS (DQAGSE) in FP32 on [a,b] with the reference's tolerances; interval
 // list of kQagsCapF entries on the thread's stack.
-// QUADPACK DQAGSE (the reference's QAGS through wrp_GSLinteg) in two parts:
-// the first panel with its two early exits, and the rest -- bisection of the
-// interval of largest error, the error-ordered list (DQPSRT) and the Wynn
-// epsilon extrapolation (DQELG) -- whose pairs of half-interval panels come
-// from Pn::two, evaluated by one lane (LanePanels) or by a warp (CoopPanels).
-struct QagsHead { float a, b, res0, err0, resabs0, resasc0; };
-
-FJ_HD bool qags_head_done(const QagsHead &h, float epsabs, float epsrel)
-{
-    const float tol = fmaxf(epsabs, epsrel * fabsf(h.res0));
-    if (h.err0 <= 100 * FLT_EPSILON * h.resabs0 && h.err0 > tol) return true;
-    return (h.err0 <= tol && h.err0 != h.resasc0) || h.err0 == 0.0f;
-}
-
 template <class F>
-FJ_HD bool qags_first_f(F &f, const GK21f &K, float a, float b, float epsabs, float epsrel, QagsHead &h)
-{
-    h.a = a; h.b = b;
-    gk21_f(f, K, a, b, h.res0, h.err0, h.resabs0, h.resasc0);
-    return qags_head_done(h, epsabs, epsrel);
-}
-
-template <class Pn>
-FJ_HDNI float qags_rest_f(Pn &pn, const QagsHead &h, float epsabs, float epsrel, unsigned &fail)
+FJ_HDNI float qags_f(F &f, const GK21f &K, float a, float b, float epsabs, float epsrel, unsigned &fail)
 {
     const int limit = 1000;
-    const float a = h.a, b = h.b, res0 = h.res0, err0 = h.err0, resabs0 = h.resabs0;
+    float res0, err0, resabs0, resasc0;
+    gk21_f(f, K, a, b, res0, err0, resabs0, resasc0);
+    const float tol = fmaxf(epsabs, epsrel * fabsf(res0));
+    if (err0 <= 100 * FLT_EPSILON * resabs0 && err0 > tol) return res0;
+    if ((err0 <= tol && err0 != resasc0) || err0 == 0.0f) return res0;
+
     float alist[kQagsCapF], blist[kQagsCapF], rlist[kQagsCapF], elist[kQagsCapF];
     int iord[kQagsCapF];
     float rlist2[52], res3la[3];
@@ -585,7 +567,8 @@ FJ_HDNI float qags_rest_f(Pn &pn, const QagsHead &h, float epsabs, float epsrel,
         const float a2 = b1, b2 = blist[maxerr];
         const float erlast = errmax;
         float area1, error1, ra1, rasc1, area2, error2, ra2, rasc2;
-        pn.two(a1, b1, a2, b2, area1, error1, ra1, rasc1, area2, error2, ra2, rasc2);
+        gk21_f(f, K, a1, b1, area1, error1, ra1, rasc1);
+        gk21_f(f, K, a2, b2, area2, error2, ra2, rasc2);
         const float area12 = area1 + area2, erro12 = error1 + error2;
         errsum = errsum + erro12 - errmax;
         area = area + area12 - rlist[maxerr];
@@ -720,27 +703,6 @@ FJ_HDNI float qags_rest_f(Pn &pn, const QagsHead &h, float epsabs, float epsrel,
     }
     (void)ksgn;
     return result;
-}
-
-template <class F>
-struct LanePanels {
-    F &f;
-    const GK21f &K;
-    FJ_HD void two(float a1, float b1, float a2, float b2, float &r1, float &e1, float &ra1, float &rc1, float &r2,
-                   float &e2, float &ra2, float &rc2)
-    {
-        gk21_f(f, K, a1, b1, r1, e1, ra1, rc1);
-        gk21_f(f, K, a2, b2, r2, e2, ra2, rc2);
-    }
-};
-
-template <class F>
-FJ_HD float qags_f(F &f, const GK21f &K, float a, float b, float epsabs, float epsrel, unsigned &fail)
-{
-    QagsHead h;
-    if (qags_first_f(f, K, a, b, epsabs, epsrel, h)) return h.res0;
-    LanePanels<F> pn{f, K};
-    return qags_rest_f(pn, h, epsabs, epsrel, fail);
 }
 
 // ----------------------------------------------------------- fudge, FP32
@@ -1056,27 +1018,11 @@ FJ_HD PotViewF mixed_view_f(int nr, int npoly, const double *ar, const double *p
 // with FP32 turning points and QAGS, FP64 turning points at the limits, and
 // the double-power-law DF (DF.cpp:65-76,108-119) in FP32.  PF is shifted by
 // PF.shift = Phi_h (mixed_tables_f); the node's energy enters shifted too.
-// The work is split where the two momentum integrals have had their first
-// QAGS panel (mixed_node_begin), so that the rest of each integral can run on
-// one lane (mixed_node_df) or on the whole warp (the kernel's cooperative form).
-struct MixedNode {
-    FudgeF o;
-    QagsHead hu, hv;  // first panels of the Ju and Jv integrals
-    double Lz, Jr, Jz;
-    bool pend_u, pend_v;  // the integral goes on past its first panel
-};
-
-FJ_HD double mixed_ju(const FudgeF &o, float q) { return (double)(1.41421356237309505f * o.Delta * o.Dt * q / kPIf); }
-FJ_HD double mixed_jv(const FudgeF &o, float q)
-{
-    return (double)(2.f * 1.41421356237309505f * o.Delta * o.wt * q / kPIf);
-}
-
-// The node up to the first panels: fail gets the kFail* bits, esc = 1 when
-// the FP64 turning-point path ran
-FJ_HDNI void mixed_node_begin(const PotView &P, const PotViewF &PF, const GK21f &K, double Delta, double R, double z,
-                              double Phi_h, double V0, double V1, double V2, MixedNode &n, unsigned &fail,
-                              unsigned &esc)
+// Returns the DF (NaN -> 0 as DF.cpp:105); fail gets the kFail* bits,
+// esc = 1 when the FP64 turning-point path ran; J (optional) the actions.
+FJ_HDNI double mixed_node_df(const PotView &P, const PotViewF &PF, const GK21f &K, const DFDev &d, double Delta,
+                             double R, double z, double Phi_h, double V0, double V1, double V2, unsigned &fail,
+                             unsigned &esc, double *J = nullptr)
 {
     const double Lz = R * V1, Lzsq = Lz * Lz;
     const double D2 = Delta * Delta, R2 = R * R, z2 = z * z, r2 = R2 + z2;
@@ -1090,70 +1036,63 @@ FJ_HDNI void mixed_node_begin(const PotView &P, const PotViewF &PF, const GK21f 
     const double pu = Delta * (V0 * chu * sv + V2 * shu * cv);
     const double pv = Delta * (V0 * shu * cv - V2 * chu * sv);
     const double E = .5 * (V0 * V0 + V2 * V2) + .5 * Lzsq / R2 + Phi_h;
-    n.Lz = Lz;
-    n.Jr = 1e31; n.Jz = 1e31;
-    n.pend_u = n.pend_v = false;
-    if (E >= 0 || isnan(E)) return;
-    FudgeF &o = n.o;
-    o.P = PF;
-    o.Delta = (float)Delta;
-    o.D2 = (float)D2;
-    o.K = (float)(.5 * (V0 * V0 + V2 * V2) + .5 * Lzsq / R2);
-    o.EC = (float)(.5 * (pu * pu) / D2);
-    o.C0 = (float)(.5 * (pu * pu) / D2 - shu2 * (.5 * (V0 * V0 + V2 * V2) + .5 * Lzsq / R2));
-    o.Lt = (float)(.5 * Lzsq / D2);
-    o.shu2 = (float)shu2;
-    o.sv2 = (float)sv2;
-    o.swp = (float)fabs(cv);
-    o.svp = (float)sqrt(sv2);
-    double sn, cs;
-    sincos(v, &sn, &cs);
-    o.sinv = (float)sn; o.cosv = (float)cs;
-    o.sinhu = (float)shu; o.coshu = (float)chu;
-    o.pvterm = (float)(.5 * (pv * pv) / D2);
-    o.u_pt = u;
-    o.rpt = (float)(Delta * sqrt(shu2 + cv2));
-    o.Phipt = pot_phi_f(PF, o.Delta * o.sinhu * o.sinv, o.Delta * o.coshu * o.cosv);
-    o.tb = o.Dt = o.wt = 0.f;
-    Fudge o64;
-    bool have64 = false;
-    float tin, tout;
-    if (!get_turn_u_f(o, 1.0, tin, tout, fail)) {  // u limit: FP64 (uvOrb.cpp:131-201)
-        fudge64_at_point(o64, P, Delta, Lzsq, E, u, v, shu2, sv, cv, sv2, pu, pv);
-        have64 = true;
-        get_turn_u(o64, 1);
-        fail |= o64.fail;
-        tin = (float)(o64.uinner - u); tout = (float)(o64.uouter - u);
-        esc = 1u;
+    double Jr = 1e31, Jz = 1e31;
+    if (!(E >= 0 || isnan(E))) {
+        FudgeF o;
+        o.P = PF;
+        o.Delta = (float)Delta;
+        o.D2 = (float)D2;
+        o.K = (float)(.5 * (V0 * V0 + V2 * V2) + .5 * Lzsq / R2);
+        o.EC = (float)(.5 * (pu * pu) / D2);
+        o.C0 = (float)(.5 * (pu * pu) / D2 - shu2 * (.5 * (V0 * V0 + V2 * V2) + .5 * Lzsq / R2));
+        o.Lt = (float)(.5 * Lzsq / D2);
+        o.shu2 = (float)shu2;
+        o.sv2 = (float)sv2;
+        o.swp = (float)fabs(cv);
+        o.svp = (float)sqrt(sv2);
+        double sn, cs;
+        sincos(v, &sn, &cs);
+        o.sinv = (float)sn; o.cosv = (float)cs;
+        o.sinhu = (float)shu; o.coshu = (float)chu;
+        o.pvterm = (float)(.5 * (pv * pv) / D2);
+        o.u_pt = u;
+        o.rpt = (float)(Delta * sqrt(shu2 + cv2));
+        o.Phipt = pot_phi_f(PF, o.Delta * o.sinhu * o.sinv, o.Delta * o.coshu * o.cosv);
+        Fudge o64;
+        bool have64 = false;
+        const float rtwo = 1.41421356237309505f;
+        float tin, tout;
+        if (!get_turn_u_f(o, 1.0, tin, tout, fail)) {  // u limit: FP64 (uvOrb.cpp:131-201)
+            fudge64_at_point(o64, P, Delta, Lzsq, E, u, v, shu2, sv, cv, sv2, pu, pv);
+            have64 = true;
+            get_turn_u(o64, 1);
+            fail |= o64.fail;
+            tin = (float)(o64.uinner - u); tout = (float)(o64.uouter - u);
+            esc = 1u;
+        }
+        if (fabsf(tout - tin) < 1e-12f) Jr = 0;
+        else {
+            o.tb = .5f * (tin + tout);
+            o.Dt = .5f * (tout - tin);
+            const FudgeFn fju{&o, kEvJu};
+            Jr = (double)(rtwo * o.Delta * o.Dt * qags_f(fju, K, 0.f, kPIf, 1e-5f, 1e-3f, fail) / kPIf);
+        }
+        float wt;
+        if (!get_turn_v_f(o, wt, fail)) {  // v at the pole: FP64 (uvOrb.cpp:203-224)
+            if (!have64) fudge64_at_point(o64, P, Delta, Lzsq, E, u, v, shu2, sv, cv, sv2, pu, pv);
+            const double v64 = get_turn_v(o64, .5 * kPIH);
+            fail |= o64.fail;
+            wt = (float)(kPIH - v64);
+            esc = 1u;
+        }
+        if (wt < 1e-12f) Jz = 0;
+        else {
+            o.wt = wt;
+            const FudgeFn fjv{&o, kEvJv};
+            Jz = (double)(2.f * rtwo * o.Delta * wt * qags_f(fjv, K, 0.f, kPIHf, 1e-5f, 1e-3f, fail) / kPIf);
+        }
     }
-    if (fabsf(tout - tin) < 1e-12f) n.Jr = 0;
-    else {
-        o.tb = .5f * (tin + tout);
-        o.Dt = .5f * (tout - tin);
-        const FudgeFn fju{&o, kEvJu};
-        if (qags_first_f(fju, K, 0.f, kPIf, 1e-5f, 1e-3f, n.hu)) n.Jr = mixed_ju(o, n.hu.res0);
-        else n.pend_u = true;
-    }
-    float wt;
-    if (!get_turn_v_f(o, wt, fail)) {  // v at the pole: FP64 (uvOrb.cpp:203-224)
-        if (!have64) fudge64_at_point(o64, P, Delta, Lzsq, E, u, v, shu2, sv, cv, sv2, pu, pv);
-        const double v64 = get_turn_v(o64, .5 * kPIH);
-        fail |= o64.fail;
-        wt = (float)(kPIH - v64);
-        esc = 1u;
-    }
-    if (wt < 1e-12f) n.Jz = 0;
-    else {
-        o.wt = wt;
-        const FudgeFn fjv{&o, kEvJv};
-        if (qags_first_f(fjv, K, 0.f, kPIHf, 1e-5f, 1e-3f, n.hv)) n.Jz = mixed_jv(o, n.hv.res0);
-        else n.pend_v = true;
-    }
-}
-
-// The DF from the actions (NaN -> 0 as DF.cpp:105)
-FJ_HD double mixed_df(const DFDev &d, double Lz, double Jr, double Jz)
-{
+    if (J) { J[0] = Jr; J[1] = Jz; }
     const float Jphi = (float)Lz, jr = (float)Jr, jz = (float)Jz, J0 = (float)d.J0;
     const float h = jr + (float)d.dphi_h * fabsf(Jphi) + (float)d.dz_h * jz;
     const float g = jr + (float)d.dphi_g * fabsf(Jphi) + (float)d.dz_g * jz;
@@ -1162,27 +1101,6 @@ FJ_HD double mixed_df(const DFDev &d, double Lz, double Jr, double Jz)
     float f = d.chi == 0. ? ev : ev + (float)d.k * tanhf((float)d.chi * Jphi / J0) * ev;
     if (isnan(f)) f = 0.f;
     return (double)f;
-}
-
-// The whole node on one lane.  Returns the DF; J (optional) gets the actions.
-FJ_HDNI double mixed_node_df(const PotView &P, const PotViewF &PF, const GK21f &K, const DFDev &d, double Delta,
-                             double R, double z, double Phi_h, double V0, double V1, double V2, unsigned &fail,
-                             unsigned &esc, double *J = nullptr)
-{
-    MixedNode n;
-    mixed_node_begin(P, PF, K, Delta, R, z, Phi_h, V0, V1, V2, n, fail, esc);
-    if (n.pend_u) {
-        const FudgeFn fju{&n.o, kEvJu};
-        LanePanels<const FudgeFn> pn{fju, K};
-        n.Jr = mixed_ju(n.o, qags_rest_f(pn, n.hu, 1e-5f, 1e-3f, fail));
-    }
-    if (n.pend_v) {
-        const FudgeFn fjv{&n.o, kEvJv};
-        LanePanels<const FudgeFn> pn{fjv, K};
-        n.Jz = mixed_jv(n.o, qags_rest_f(pn, n.hv, 1e-5f, 1e-3f, fail));
-    }
-    if (J) { J[0] = n.Jr; J[1] = n.Jz; }
-    return mixed_df(d, n.Lz, n.Jr, n.Jz);
 }
 
 }  // namespace fj

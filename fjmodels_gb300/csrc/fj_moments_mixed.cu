@@ -22,13 +22,16 @@ namespace fj {
 // The kernel is built in two forms and each in four register budgets (launch
 // bounds of 3, 4, 6 and 8 resident blocks per SM: 168, 128, 80 and 64
 // registers): kMixedVariants builds.
-//  - nested: each thread runs its node's solves to the end (mixed_node_df);
-//  - cooperative: each thread runs its node to the first QAGS panel of both
-//    momentum integrals (mixed_node_begin), then the warp takes the integrals
-//    that go on, one at a time, each bisection's 42 evaluations spread over
-//    its 32 lanes (CoopPanels).  The adaptive integrals' lengths vary from 1
-//    to ~60 panels between nodes, so one lane per integral leaves most lanes
-//    of a warp waiting for its longest one.  Both forms give the same bits.
+//  - static: thread t takes list entries t, t + 128, .. and sums its nodes'
+//    moments as it goes;
+//  - dynamic: a lane that finishes a node takes the next untaken entry
+//    (shared counter), stores the node's DF in a shared array, and after
+//    the list the threads sum the moments of entries t, t + 128, .. from it.
+//    The time per node varies by two orders of magnitude (QAGS takes 1 to
+//    ~60 panels per integral), so with static shares the block waits for its
+//    unluckiest thread; the dynamic form keeps all lanes busy to the end.
+//    Its sums are those of the static form term by term, so both give the
+//    same bits.
 // Which one, and the chunk size, is a per-context setting (fj_autotune_mixed).
 int mixed_blocks_per_point(long long nq3, int chunk) { return (int)((nq3 + chunk - 1) / chunk); }
 
@@ -38,36 +41,10 @@ size_t moment_mixed_smem_bytes(const MomentArgs &a)
     return (a.P.nr + 3 * nt + 2 * a.ngrid + 2 * a.nq + 6 * (kMixedBlock / 32) + 4) * sizeof(double) +
            (2 * a.P.nr + 2 * nt + 4 * kQuadIntervals + a.P.npoly) * sizeof(float) + sizeof(GK21f) + 16 +
            (kMixedBlock / 32) * sizeof(int) + (size_t)a.mixed_chunk * sizeof(unsigned short) + 16 +
-           (kMixedBlock / 32) * (sizeof(FudgeF) + sizeof(QagsHead) + 42 * sizeof(float));
+           (size_t)a.mixed_chunk * sizeof(float) + sizeof(int);
 }
 
-// Two half-interval panels of one node's integral evaluated by the 32 lanes
-// of a warp: evaluation e (0..41: panel e / 21, abscissa e % 21) on lane
-// e % 32, the values exchanged through the warp's shared buffer, and the sums
-// formed by every lane from the same values in the same order -- so every
-// lane holds LanePanels' result bit for bit, and the QAGS bookkeeping around
-// it runs uniformly on all lanes.
-struct CoopPanels {
-    const FudgeF *o;
-    int mode;
-    const GK21f &K;
-    float *buf;
-    int lane;
-    __device__ void two(float a1, float b1, float a2, float b2, float &r1, float &e1, float &ra1, float &rc1, float &r2,
-                        float &e2, float &ra2, float &rc2)
-    {
-        for (int e = lane; e < 42; e += 32) {
-            const bool second = e >= 21;
-            buf[e] = fudge_eval(*o, mode, gk21_abscissa(K, second ? a2 : a1, second ? b2 : b1, second ? e - 21 : e));
-        }
-        __syncwarp();
-        gk21_sum(K, a1, b1, buf, r1, e1, ra1, rc1);
-        gk21_sum(K, a2, b2, buf + 21, r2, e2, ra2, rc2);
-        __syncwarp();
-    }
-};
-
-template <int MINB, bool COOP>
+template <int MINB, bool DYN>
 __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs a0, MomentBatch batch)
 {
     extern __shared__ double sm[];
@@ -87,9 +64,8 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
     GK21f *sK = (GK21f *)(((uintptr_t)(f_pyl + npoly) + 15) & ~(uintptr_t)15);
     int *s_wc = (int *)(sK + 1);
     unsigned short *s_list = (unsigned short *)(s_wc + kMixedBlock / 32);
-    FudgeF *s_fud = (FudgeF *)(((uintptr_t)(s_list + a.mixed_chunk) + 15) & ~(uintptr_t)15);
-    QagsHead *s_head = (QagsHead *)(s_fud + kMixedBlock / 32);
-    float *s_buf = (float *)(s_head + kMixedBlock / 32);
+    float *s_df = (float *)(((uintptr_t)(s_list + a.mixed_chunk) + 15) & ~(uintptr_t)15);
+    int *s_next = (int *)(s_df + a.mixed_chunk);
     for (int i = threadIdx.x; i < nr; i += blockDim.x) s_ar[i] = a.P.ar[i];
     for (int i = threadIdx.x; i < nt; i += blockDim.x) {
         s_phil[i] = a.P.phil[i]; s_Pr[i] = a.P.Pr[i]; s_Pr2[i] = a.P.Pr2[i];
@@ -154,70 +130,8 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
 
     double m[6] = {0, 0, 0, 0, 0, 0};
     unsigned failed = 0, esc = 0;
-    auto accumulate = [&](int node, double V0, double V1, double V2, double Jr, double Jz, double f, unsigned fail) {
-        if (a.jout) {
-            float *jo = a.jout + ((size_t)p * nq3 + node) * 2;
-            jo[0] = (float)Jr;
-            jo[1] = (float)Jz;
-        }
-        failed += fail ? 1u : 0u;
-        const int i = node / nq2, j = (node / nq) % nq, k = node % nq;
-        const double DF = (fail & (kFailBracket | kFailRoot)) ? 0. : f;
-        const double jd = (s_wq[i] * s_wq[j] * s_wq[k]) * (jacob * DF);
-        m[0] += jd;
-        m[1] += jd * V1;
-        m[2] += jd * V0 * V0;
-        m[3] += jd * V1 * V1;
-        m[4] += jd * V2 * V2;
-        m[5] += jd * V0 * V2;
-    };
-    if (COOP) {
-        // rounds over the list in which every lane of the block takes at most
-        // one node, so the warp's lanes stay together for the cooperative part
-        FudgeF &wf = s_fud[warp];
-        float *wbuf = s_buf + warp * 42;
-        for (int q0 = 0; q0 < nbound; q0 += kMixedBlock) {
-            const int q = q0 + threadIdx.x;
-            const bool has = q < nbound;
-            const int node = has ? n0 + s_list[q] : 0;
-            const int i = node / nq2, j = (node / nq) % nq, k = node % nq;
-            const double V0 = 1e-6 + Ve * s_xq[i], V1 = 1e-6 + Ve * s_xq[j], V2 = 1e-6 + Ve * s_xq[k];
-            MixedNode n;
-            n.pend_u = n.pend_v = false;
-            unsigned fail = 0, e = 0;
-            if (has) {
-                const double H = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h;
-                mixed_node_begin(P, PF, *sK, deltafn(s_Eg, s_Dg, a.ngrid, H), R, z, Phi_h, V0, V1, V2, n, fail, e);
-            }
-            for (int which = 0; which < 2; which++) {
-                unsigned pend = __ballot_sync(0xffffffffu, which == 0 ? n.pend_u : n.pend_v);
-                while (pend) {
-                    const int owner = __ffs(pend) - 1;
-                    pend &= pend - 1;
-                    if (lane == owner) {
-                        wf = n.o;
-                        s_head[warp] = which == 0 ? n.hu : n.hv;
-                    }
-                    __syncwarp();
-                    const QagsHead h = s_head[warp];
-                    CoopPanels pn{&wf, which == 0 ? kEvJu : kEvJv, *sK, wbuf, lane};
-                    unsigned qf = 0;
-                    const float r = qags_rest_f(pn, h, 1e-5f, 1e-3f, qf);
-                    if (lane == owner) {
-                        fail |= qf;
-                        if (which == 0) n.Jr = mixed_ju(n.o, r);
-                        else n.Jz = mixed_jv(n.o, r);
-                    }
-                    __syncwarp();
-                }
-            }
-            if (has) {
-                esc += e;
-                accumulate(node, V0, V1, V2, n.Jr, n.Jz, mixed_df(a.df, n.Lz, n.Jr, n.Jz), fail);
-            }
-        }
-    } else
-    for (int q = threadIdx.x; q < nbound; q += kMixedBlock) {
+    // one node's solve; returns the DF that enters the moments
+    auto solve = [&](int q) {
         const int node = n0 + s_list[q];
         const int i = node / nq2, j = (node / nq) % nq, k = node % nq;
         const double V0 = 1e-6 + Ve * s_xq[i], V1 = 1e-6 + Ve * s_xq[j], V2 = 1e-6 + Ve * s_xq[k];
@@ -226,8 +140,38 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
         const double Delta = deltafn(s_Eg, s_Dg, a.ngrid, H);
         double J[2];
         const double f = mixed_node_df(P, PF, *sK, a.df, Delta, R, z, Phi_h, V0, V1, V2, fail, e, J);
+        if (a.jout) {
+            float *jo = a.jout + ((size_t)p * nq3 + node) * 2;
+            jo[0] = (float)J[0];
+            jo[1] = (float)J[1];
+        }
         esc += e;
-        accumulate(node, V0, V1, V2, J[0], J[1], f, fail);
+        failed += fail ? 1u : 0u;
+        return (fail & (kFailBracket | kFailRoot)) ? 0. : f;
+    };
+    auto accumulate = [&](int q, double DF) {
+        const int node = n0 + s_list[q];
+        const int i = node / nq2, j = (node / nq) % nq, k = node % nq;
+        const double V0 = 1e-6 + Ve * s_xq[i], V1 = 1e-6 + Ve * s_xq[j], V2 = 1e-6 + Ve * s_xq[k];
+        const double jd = (s_wq[i] * s_wq[j] * s_wq[k]) * (jacob * DF);
+        m[0] += jd;
+        m[1] += jd * V1;
+        m[2] += jd * V0 * V0;
+        m[3] += jd * V1 * V1;
+        m[4] += jd * V2 * V2;
+        m[5] += jd * V0 * V2;
+    };
+    if (DYN) {
+        if (threadIdx.x == 0) *s_next = kMixedBlock;
+        __syncthreads();
+        for (int q = threadIdx.x; q < nbound;) {
+            s_df[q] = (float)solve(q);  // the DF is an FP32 value
+            q = atomicAdd(s_next, 1);
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < nbound; q += kMixedBlock) accumulate(q, (double)s_df[q]);
+    } else {
+        for (int q = threadIdx.x; q < nbound; q += kMixedBlock) accumulate(q, solve(q));
     }
 #pragma unroll
     for (int q = 0; q < 6; q++) {
@@ -259,16 +203,16 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
 }
 
 namespace {
-template <int MINB, bool COOP>
+template <int MINB, bool DYN>
 cudaError_t launch_variant(const MomentArgs &a, const MomentBatch &b, long long nblocks, size_t smem,
                            cudaStream_t s)
 {
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(k_moments_mixed<MINB, COOP>,
+        cudaError_t e = cudaFuncSetAttribute(k_moments_mixed<MINB, DYN>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    k_moments_mixed<MINB, COOP><<<(unsigned)nblocks, kMixedBlock, smem, s>>>(a, b);
+    k_moments_mixed<MINB, DYN><<<(unsigned)nblocks, kMixedBlock, smem, s>>>(a, b);
     return cudaGetLastError();
 }
 
@@ -288,11 +232,11 @@ cudaError_t launch_mixed_any(const MomentArgs &a, const MomentBatch &b, long lon
     }
 }
 
-template <int MINB, bool COOP>
+template <int MINB, bool DYN>
 size_t local_bytes()
 {
     cudaFuncAttributes at;
-    return cudaFuncGetAttributes(&at, k_moments_mixed<MINB, COOP>) == cudaSuccess ? at.localSizeBytes : 0;
+    return cudaFuncGetAttributes(&at, k_moments_mixed<MINB, DYN>) == cudaSuccess ? at.localSizeBytes : 0;
 }
 }  // namespace
 

@@ -67,33 +67,85 @@ struct IExternalT {  // I_external (pot/Potential.cpp:90-101) on x = a + (1-t)/t
     }
 };
 
-size_t poisson_ws_bytes(int nr, int npoly)
+// One warp per (n, l) pair.  The QAGS calls of a pair run on all 32 lanes
+// at once: the function values of each Gauss-Kronrod panel (21 or 15, 42 or
+// 30 per bisection) are spread over the lanes and exchanged through shared
+// memory, every lane forms the panel sums from them in the same order, and
+// the adaptive bookkeeping runs uniformly on every lane over an interval
+// list in the warp's shared memory (identical values, identical writes).
+// The results are those of one thread running the same QAGS: the same
+// function values enter the same sums in the same order.  With one thread
+// per pair the 2 nr npoly integrals (560 on 80 x 7) sat on a few SMs, each
+// thread evaluating its thousands of integrand values one after another.
+constexpr int kPoissonWarps = 4;
+
+template <int RULE, class F>
+struct WarpPanels64 {
+    F &f;
+    double *buf;
+    int lane;
+    __device__ void one(double a, double b, double &r, double &e, double &ra, double &rc)
+    {
+        constexpr int n = GKRule<RULE>::npts;
+        for (int i = lane; i < n; i += 32) buf[i] = f(gk_abscissa<RULE>(a, b, i));
+        __syncwarp();
+        gk_sum<RULE>(a, b, buf, r, e, ra, rc);
+        __syncwarp();
+    }
+    __device__ void two(double a1, double b1, double a2, double b2, double &r1, double &e1, double &ra1,
+                        double &rc1, double &r2, double &e2, double &ra2, double &rc2)
+    {
+        constexpr int n = GKRule<RULE>::npts;
+        for (int i = lane; i < 2 * n; i += 32) {
+            const bool second = i >= n;
+            buf[i] = f(gk_abscissa<RULE>(second ? a2 : a1, second ? b2 : b1, second ? i - n : i));
+        }
+        __syncwarp();
+        gk_sum<RULE>(a1, b1, buf, r1, e1, ra1, rc1);
+        gk_sum<RULE>(a2, b2, buf + n, r2, e2, ra2, rc2);
+        __syncwarp();
+    }
+};
+
+template <int RULE, class F>
+__device__ int qags_warp(F &f, double a, double b, double epsabs, double epsrel, int limit, double &result,
+                         double &abserr, unsigned &fail, const QagsWs &ws, double *buf, int lane)
 {
-    return (size_t)nr * npoly * kPoissonCap * (4 * sizeof(double) + sizeof(int));
+    WarpPanels64<RULE, F> pn{f, buf, lane};
+    double res0, err0, resabs0, resasc0;
+    pn.one(a, b, res0, err0, resabs0, resasc0);
+    const int h = qags_head(res0, err0, resabs0, resasc0, epsabs, epsrel, limit, result, abserr);
+    if (h >= 0) return h;
+    return qags_rest<RULE>(pn, a, b, res0, err0, resabs0, epsabs, epsrel, limit, result, abserr, fail, ws);
 }
 
-// computeInts + computePhil (pot/Potential.cpp:110-200): one thread per (n, l)
-__global__ void k_poisson(int nr, int npoly, const double *ar, const double *rhl, double *phil, double *Pr,
-                          double *Pr2, char *ws, unsigned long long *counters)
+// computeInts + computePhil (pot/Potential.cpp:110-200)
+__global__ void __launch_bounds__(32 * kPoissonWarps) k_poisson(int nr, int npoly, const double *ar,
+                                                                 const double *rhl, double *phil, double *Pr,
+                                                                 double *Pr2, unsigned long long *counters)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double s_list[kPoissonWarps][4 * kPoissonCap];
+    __shared__ int s_iord[kPoissonWarps][kPoissonCap];
+    __shared__ double s_vals[kPoissonWarps][42];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = blockIdx.x * kPoissonWarps + warp;
     const int nt = nr * npoly;
-    if (t >= nt) return;
+    if (t >= nt) return;  // the whole warp
     const int n = t / npoly, np = t % npoly, l = 2 * np;
-    double *dws = (double *)ws + (size_t)t * 4 * kPoissonCap;
-    int *iws = (int *)((double *)ws + (size_t)nt * 4 * kPoissonCap) + (size_t)t * kPoissonCap;
-    const QagsWs W{dws, dws + kPoissonCap, dws + 2 * kPoissonCap, dws + 3 * kPoissonCap, iws, kPoissonCap};
+    double *dws = s_list[warp];
+    const QagsWs W{dws, dws + kPoissonCap, dws + 2 * kPoissonCap, dws + 3 * kPoissonCap, s_iord[warp], kPoissonCap};
     unsigned fail = 0;
     double Iint, Iext, err;
     IInternal fi{ar, rhl, npoly, np, l, nr};
-    qags<21>(fi, 0., ar[n], 1e-4, 1e-3, 1000, Iint, err, fail, W);
+    qags_warp<21>(fi, 0., ar[n], 1e-4, 1e-3, 1000, Iint, err, fail, W, s_vals[warp], lane);
     IExternalT fe{ar, rhl, npoly, np, l, nr, ar[n]};
     double epsabs = 1e-4, epsrel = 1e-3;
     int status = 1, tries = 0;
     while (status != 0 && tries < 60) {
-        status = qags<15>(fe, 0.0, 1.0, epsabs, epsrel, 1000, Iext, err, fail, W);
+        status = qags_warp<15>(fe, 0.0, 1.0, epsabs, epsrel, 1000, Iext, err, fail, W, s_vals[warp], lane);
         epsabs *= 2; epsrel *= 2; tries++;
     }
+    if (lane != 0) return;
     if (fail && counters) atomicAdd(&counters[2], 1ull);
     const double r = ar[n];
     const double G = 1;
@@ -104,10 +156,11 @@ __global__ void k_poisson(int nr, int npoly, const double *ar, const double *rhl
 }
 
 cudaError_t launch_poisson(int nr, int npoly, const double *ar, const double *rhl, double *phil,
-                           double *Pr, double *Pr2, void *ws, unsigned long long *counters, cudaStream_t s)
+                           double *Pr, double *Pr2, unsigned long long *counters, cudaStream_t s)
 {
     const int nt = nr * npoly;
-    k_poisson<<<(nt + 63) / 64, 64, 0, s>>>(nr, npoly, ar, rhl, phil, Pr, Pr2, (char *)ws, counters);
+    k_poisson<<<(nt + kPoissonWarps - 1) / kPoissonWarps, 32 * kPoissonWarps, 0, s>>>(nr, npoly, ar, rhl, phil, Pr,
+                                                                                      Pr2, counters);
     return cudaGetLastError();
 }
 

@@ -201,17 +201,17 @@ int fj_surrogate_moments(fj_surrogate *s, const fj_potential *pot, const fj_df_p
                          int ngauss, double *grids6, double *ms, int fused);
 
 /* Configuration of the mixed-precision phase-space kernel (no reference
-   counterpart: the reference has one CPU loop).  variant 0..7: 0..3 run each
-   node's solve on one lane, 4..7 hand each momentum integral that goes on
-   past its first QAGS panel to the whole warp (the 42 evaluations of each
-   bisection on 32 lanes); within each, the register budget of the build
+   counterpart: the reference has one CPU loop).  variant 0..7: 0..3 give
+   each thread a fixed share of a block's velocity nodes, 4..7 let a thread
+   take the next untaken node when it finishes one (the time per node varies
+   by two orders of magnitude); within each, the register budget of the build
    (launch bounds of 3, 4, 6, 8 resident blocks per SM),
    nodes_per_block = velocity nodes of one point per block (128..8192).
-   fj_autotune_mixed times every variant x {2048, 4096, 8192} with
+   fj_autotune_mixed times every variant x {1024, 2048, 4096} with
    fj_moments_points on the given device sample points (out6 device
    [6][npts] scratch), keeps the fastest in the context and returns its
    kernel time (all_ms, if not NULL: host [8][3] times of every variant x
-   {2048, 4096, 8192}); results are the same in every configuration up to
+   {1024, 2048, 4096}); results are the same in every configuration up to
    the summation order of the per-thread sums (the two forms give the same
    bits at the same nodes_per_block). */
 int fj_set_mixed_config(fj_ctx *ctx, int variant, int nodes_per_block);
@@ -233,19 +233,16 @@ int fj_legendre_project(fj_ctx *ctx, int nr, int ngauss, int npoly, const double
 int fj_poisson(fj_ctx *ctx, int nr, int npoly, const double *ar, const double *rhl,
                double *phil, double *Pr, double *Pr2);
 
-/* Poisson solve that allocates nothing.  It has no counterpart in the
-   reference: it is fj_poisson for callers that cannot allocate device memory
-   on their call path (an application whose device memory belongs to its own
-   pool allocator, a latency-bound loop).  The quadrature workspace is a
-   file-scope device array of the library, sized for nr*npoly <=
-   FJ_POISSON_NOALLOC_MAX_COEFS (9 MiB, held on every device that loads the
-   library until exit); larger requests return FJ_ERR_ARG.  No context:
-   inputs and outputs are device pointers on the current device, work is
-   queued on `stream` (a cudaStream_t; NULL = legacy default stream).  The
-   first call on a device looks up the array's address on that device, so
-   make that first call before any stream capture.  All calls share the
-   array: calls whose work overlaps on the GPU race and must be serialised by
-   the caller. */
+/* Poisson solve that allocates nothing and needs no context.  It has no
+   counterpart in the reference: it is fj_poisson for callers that hold no
+   fj_ctx or cannot allocate device memory on their call path (an
+   application whose device memory belongs to its own pool allocator, a
+   latency-bound loop).  The quadrature workspace lives in the kernel's
+   shared memory.  Inputs and outputs are device pointers on the current
+   device, work is queued on `stream` (a cudaStream_t; NULL = legacy default
+   stream); calls on different streams are independent.
+   FJ_POISSON_NOALLOC_MAX_COEFS is kept for source compatibility: any
+   nr*npoly that fj_poisson accepts is accepted. */
 #define FJ_POISSON_NOALLOC_MAX_COEFS 1024
 int fj_poisson_noalloc(int nr, int npoly, const double *ar, const double *rhl, double *phil,
                        double *Pr, double *Pr2, void *stream);

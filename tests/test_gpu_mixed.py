@@ -154,11 +154,11 @@ def test_mixed_rejects_unsupported(ctx):
 
 def test_mixed_configurations_agree(ctx):
     """Every build and node range of the mixed kernel gives the same moments: within one
-    form (one lane per node: variants 0-3; a warp per momentum integral past its first
-    panel: 4-7) up to the summation order of the per-thread sums (relative 1e-12), and the
-    two forms give the same bits for the same node range (each node's arithmetic is the
-    same; the cooperative panel sums run every lane through the one-lane code).  The
-    autotuner keeps one of them, and out-of-range settings are argument errors."""
+    form (static shares of the node list: variants 0-3; nodes taken as lanes free up:
+    4-7) up to the summation order of the per-thread sums (relative 1e-12), and the two
+    forms give the same bits for the same node range (the dynamic form sums the same terms
+    in the same order after the solves).  The autotuner keeps one of them, and
+    out-of-range settings are argument errors."""
     (ar, phil, Pr, Pr2, E, D), M, df = _nfw_80(None)
     pot = ctx.potential(dev(ar), dev(phil), dev(Pr), dev(Pr2))
     delta = ctx.delta(dev(E), dev(D))
@@ -180,7 +180,7 @@ def test_mixed_configurations_agree(ctx):
             for v in range(4):
                 assert np.array_equal(outs[v + 4, c], outs[v, c]), (v, c)
         v, c, ms = ctx.autotune_mixed(pot, delta, df, rule, Mt)
-        assert 0 <= v < 8 and c in (2048, 4096, 8192) and ms > 0
+        assert 0 <= v < 8 and c in (1024, 2048, 4096) and ms > 0
         for bad in ((8, 2048), (0, 64), (0, 8193)):
             with pytest.raises(F.FJError, match="set_mixed_config"):
                 ctx.set_mixed_config(*bad)
