@@ -5,11 +5,12 @@ include/fjgpu.h); this package holds its ctypes bindings and a host-side mirror
 of the reference's calls.  There is no CPU fallback.
 """
 from . import _abi
-from .api import (XPT11, XW11, Context, DFParams, FJError, Rule, Surrogate, composeName, gauleg, guess_rhl,
-                  log_grid, readParam, tabulate_delta, tanh_sinh_rule, writeOut)
+from .api import (OUT_TABLES, XPT11, XW11, Context, DFParams, FJError, Rule, Surrogate, composeName, gauleg, guess_rhl,
+                  log_grid, readOut, readParam, tabulate_delta, tanh_sinh_rule, writeOut)
 
 __all__ = ["Context", "DFParams", "Rule", "Surrogate", "FJError", "XPT11", "XW11", "log_grid", "gauleg", "guess_rhl",
-           "tabulate_delta", "writeOut", "composeName", "readParam", "tanh_sinh_rule", "load_library"]
+           "tabulate_delta", "writeOut", "readOut", "OUT_TABLES", "composeName", "readParam", "tanh_sinh_rule",
+           "load_library"]
 
 
 def load_library():

@@ -62,7 +62,7 @@ class fj_model_config(C.Structure):
                 ("df", fj_df_params), ("rule", fj_quad_rule), ("itermax", C.c_int), ("tol", C.c_double),
                 ("Egrid_in", DP), ("Dgrid_in", DP), ("ncomp", C.c_int), ("guess2", C.c_int),
                 ("mass2", C.c_double), ("r0_2", C.c_double), ("q2", C.c_double), ("df2", fj_df_params),
-                ("twocomp_order", C.c_int)]
+                ("twocomp_order", C.c_int), ("ar_in", DP), ("phil_in", DP), ("Pr_in", DP), ("Pr2_in", DP)]
 
 
 class fj_model_result(C.Structure):
@@ -123,6 +123,8 @@ SIGNATURES = {
     "fj_guess_rhl": ([C.c_int, C.c_int, C.c_int, DP, C.c_int, C.c_double, C.c_double, C.c_double, DP], C.c_int),
     "fj_tabulate_delta": ([P(fj_potential), C.c_int, DP, DP], C.c_int),
     "fj_write_out": ([C.c_char_p, C.c_int, C.c_int, C.c_int, DP, DP, DP], C.c_int),
+    "fj_write_out_digits": ([C.c_char_p, C.c_int, C.c_int, C.c_int, DP, DP, DP, C.c_int], C.c_int),
+    "fj_read_out": ([C.c_char_p, P(C.c_int), P(C.c_int), P(C.c_int), DP, DP, DP], C.c_int),
     "fj_run_model": ([CTX, P(fj_model_config), P(fj_model_result)], C.c_int),
 }
 

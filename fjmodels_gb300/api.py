@@ -314,14 +314,22 @@ class Context:
 
     # ---------------------------------------------------------------- whole model
     def run_model(self, nr, ngauss, npoly, rmin, rmax, df, rule, itermax, tol=0.0, ngrid=30, q=1.0,
-                  keep_grids=False, delta_table=None, df2=None, q2=1.0, twocomp_order=A.FJ_TWOCOMP_SUMMED):
+                  keep_grids=False, delta_table=None, df2=None, q2=1.0, twocomp_order=A.FJ_TWOCOMP_SUMMED,
+                  restart=None):
         """Self-consistent model (oneComp, fJmodels.cpp:86-144; with df2, the two-component
         loop of fJmodels.cpp:38-84 in `twocomp_order`) with host buffers.
-        delta_table = (Egrid, Dgrid) uses a given focal-distance table instead of tabulating one."""
+        delta_table = (Egrid, Dgrid) uses a given focal-distance table instead of tabulating one;
+        restart = a dict with ar, phil, Pr, Pr2 (readOut, or an earlier result) iterates on from
+        those tables instead of the guess density (rmin, rmax are then unused)."""
         self.use_own_stream()
         din = [None, None] if delta_table is None else [_f64(delta_table[0]), _f64(delta_table[1])]
         cfg = A.fj_model_config(nr, ngauss, npoly, ngrid, rmin, rmax, A.FJ_GUESS.get(df.model, 0), df.mass, df.r0,
                                 q, df.c, rule.c, itermax, tol, *[_dp(d) if d is not None else None for d in din])
+        if restart is not None:
+            rs = {k: _f64(restart[k]) for k in ("ar", "phil", "Pr", "Pr2")}
+            if rs["ar"].size != nr or any(rs[k].size != nr * npoly for k in ("phil", "Pr", "Pr2")):
+                raise FJError("run_model: restart tables do not match nr, npoly")
+            cfg.ar_in, cfg.phil_in, cfg.Pr_in, cfg.Pr2_in = (_dp(rs[k]) for k in ("ar", "phil", "Pr", "Pr2"))
         if df2 is not None:
             cfg.ncomp, cfg.guess2, cfg.mass2, cfg.r0_2, cfg.q2 = 2, A.FJ_GUESS.get(df2.model, 0), df2.mass, df2.r0, q2
             cfg.df2 = df2.c
@@ -378,17 +386,41 @@ def tabulate_delta(ar, phil, Pr, Pr2, ngrid=30):
     return E, D, rc
 
 
-def writeOut(path, ar, mats9, ngauss, header):
-    """_writeOut (io/writeOut.cpp:74-138).  header = (dphi_h, dz_h, dphi_g, dz_g, chi, mass, r0, A, B)."""
+def writeOut(path, ar, mats9, ngauss, header, digits=0):
+    """_writeOut (io/writeOut.cpp:74-138).  header = (dphi_h, dz_h, dphi_g, dz_g, chi, mass, r0, A, B).
+    digits = 0 writes the reference's bytes; 17 writes every value exactly (a full-precision restart)."""
     ar = _f64(ar)
     m = _f64(mats9)
     nr = len(ar)
     npoly = m.size // (9 * nr)
     hdr = np.zeros(10)
     hdr[:9] = header
-    rc = A.load().fj_write_out(path.encode(), nr, npoly, ngauss, _dp(hdr), _dp(ar), _dp(m))
+    rc = A.load().fj_write_out_digits(path.encode(), nr, npoly, ngauss, _dp(hdr), _dp(ar), _dp(m), digits)
     if rc != A.FJ_OK:
         raise FJError(f"writeOut failed ({rc}) for {path}")
+
+
+OUT_TABLES = ("rhl", "vrotl", "sigRl", "sigpl", "sigzl", "sigRzl", "phil", "Pr", "Pr2")
+
+
+def readOut(path):
+    """A coefficient file of writeOut read back: dict with nr, npoly, ngauss, header (the nine
+    values of writeOut's header), ar [nr] and the nine [nr][npoly] tables by their names
+    (OUT_TABLES).  Its ar, phil, Pr and Pr2 restart a model: Context.run_model(restart=...)."""
+    lib = A.load()
+    nr, npoly, ngauss = C.c_int(), C.c_int(), C.c_int()
+    hdr = np.zeros(10)
+    rc = lib.fj_read_out(path.encode(), C.byref(nr), C.byref(npoly), C.byref(ngauss), _dp(hdr), None, None)
+    if rc != A.FJ_OK:
+        raise FJError(f"readOut failed ({rc}) for {path}")
+    ar = np.zeros(nr.value)
+    mats = np.zeros((9, nr.value, npoly.value))
+    rc = lib.fj_read_out(path.encode(), C.byref(nr), C.byref(npoly), C.byref(ngauss), _dp(hdr), _dp(ar), _dp(mats))
+    if rc != A.FJ_OK:
+        raise FJError(f"readOut failed ({rc}) for {path}")
+    out = {"nr": nr.value, "npoly": npoly.value, "ngauss": ngauss.value, "header": hdr[:9].copy(), "ar": ar}
+    out.update({k: mats[i] for i, k in enumerate(OUT_TABLES)})
+    return out
 
 
 def _to_string(x, eps=2):

@@ -889,9 +889,16 @@ extern "C" int fj_tabulate_delta(const fj_potential *pot, int ngrid, double *Egr
 extern "C" int fj_write_out(const char *path, int nr, int npoly, int ngauss, const double *hdr10, const double *ar,
                             const double *mats9)
 {
-    if (!path || nr < 1 || npoly < 1 || !hdr10 || !ar || !mats9) return FJ_ERR_ARG;
+    return fj_write_out_digits(path, nr, npoly, ngauss, hdr10, ar, mats9, 0);
+}
+
+extern "C" int fj_write_out_digits(const char *path, int nr, int npoly, int ngauss, const double *hdr10,
+                                   const double *ar, const double *mats9, int digits)
+{
+    if (!path || nr < 1 || npoly < 1 || !hdr10 || !ar || !mats9 || digits < 0 || digits > 17) return FJ_ERR_ARG;
     std::ofstream outF(path, std::ios::out);
     if (!outF.is_open()) return FJ_ERR_IO;
+    if (digits > 0) outF.precision(digits);
     // header (io/writeOut.cpp:81-85): sizes, h/g coefficients, chi mass r0, A B
     outF << nr << " " << npoly << " " << ngauss << std::endl;
     outF << hdr10[0] << " " << hdr10[1] << " " << hdr10[2] << " " << hdr10[3] << std::endl;
@@ -905,6 +912,28 @@ extern "C" int fj_write_out(const char *path, int nr, int npoly, int ngauss, con
         }
     outF.close();
     return outF.fail() ? FJ_ERR_IO : FJ_OK;
+}
+
+// The file of fj_write_out read back: header, ar, nine [nr][npoly] tables.
+extern "C" int fj_read_out(const char *path, int *nr, int *npoly, int *ngauss, double *hdr10, double *ar,
+                           double *mats9)
+{
+    if (!path || !nr || !npoly || !ngauss || !hdr10 || (!ar != !mats9)) return FJ_ERR_ARG;
+    std::ifstream in(path);
+    if (!in.is_open()) return FJ_ERR_IO;
+    long long n = 0, np = 0, ng = 0;
+    if (!(in >> n >> np >> ng) || n < 1 || np < 1 || ng < 0 || n > (1 << 20) || np > (1 << 10)) return FJ_ERR_ARG;
+    for (int i = 0; i < 9; i++)
+        if (!(in >> hdr10[i])) return FJ_ERR_ARG;
+    hdr10[9] = 0;
+    *nr = (int)n; *npoly = (int)np; *ngauss = (int)ng;
+    if (!ar) return FJ_OK;
+    for (long long i = 0; i < n; i++)
+        if (!(in >> ar[i])) return FJ_ERR_ARG;
+    for (long long i = 0; i < 9 * n * np; i++)
+        if (!(in >> mats9[i])) return FJ_ERR_ARG;
+    double extra;
+    return (in >> extra) ? FJ_ERR_ARG : FJ_OK;  // nothing may follow the last table
 }
 
 // ------------------------------------------------------------ whole model
@@ -923,12 +952,23 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
     const bool ref_order = two && cfg->twocomp_order == FJ_TWOCOMP_REFERENCE;
     auto t0 = std::chrono::steady_clock::now();
     int rc;
-    if ((rc = fj_log_grid(cfg->rmin, cfg->rmax, nr, res->ar))) return fail(ctx, rc, "run_model: grid");
+    const bool resume = cfg->phil_in || cfg->Pr_in || cfg->Pr2_in;
+    if (resume && !(cfg->phil_in && cfg->Pr_in && cfg->Pr2_in))
+        return fail(ctx, FJ_ERR_ARG, "run_model: a restart needs phil_in, Pr_in and Pr2_in");
+    if (cfg->ar_in) {
+        for (int i = 0; i < nr; i++)
+            if (!(cfg->ar_in[i] > 0) || (i && !(cfg->ar_in[i] > cfg->ar_in[i - 1])))
+                return fail(ctx, FJ_ERR_ARG, "run_model: ar_in must be positive and increasing");
+        memcpy(res->ar, cfg->ar_in, nr * sizeof(double));
+    } else if ((rc = fj_log_grid(cfg->rmin, cfg->rmax, nr, res->ar))) return fail(ctx, rc, "run_model: grid");
     std::vector<double> rhl(2 * (size_t)nt);
-    if ((rc = fj_guess_rhl(nr, ng, npl, res->ar, cfg->guess, cfg->mass, cfg->r0, cfg->q, rhl.data())))
-        return fail(ctx, rc, "run_model: guess");
-    if (two && (rc = fj_guess_rhl(nr, ng, npl, res->ar, cfg->guess2, cfg->mass2, cfg->r0_2, cfg->q2, rhl.data() + nt)))
-        return fail(ctx, rc, "run_model: guess of component 2");
+    if (!resume) {
+        if ((rc = fj_guess_rhl(nr, ng, npl, res->ar, cfg->guess, cfg->mass, cfg->r0, cfg->q, rhl.data())))
+            return fail(ctx, rc, "run_model: guess");
+        if (two &&
+            (rc = fj_guess_rhl(nr, ng, npl, res->ar, cfg->guess2, cfg->mass2, cfg->r0_2, cfg->q2, rhl.data() + nt)))
+            return fail(ctx, rc, "run_model: guess of component 2");
+    }
     // device layout: ar | rhl (2) | pot A, B (total, 3 tables each) | pot C, D (components) | Eg | Dg |
     // grids6 (2) | coef6 (2)
     const size_t nd = nr + 2 * (size_t)nt + 12 * (size_t)nt + 2 * ngrid + 12 * (size_t)nr * ng + 12 * (size_t)nt;
@@ -942,7 +982,11 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
     cudaStream_t s = ctx->stream;
     FJ_CUDA(cudaMemcpyAsync(d_ar, res->ar, nr * sizeof(double), cudaMemcpyHostToDevice, s));
     FJ_CUDA(cudaMemcpyAsync(d_rhl, rhl.data(), 2 * nt * sizeof(double), cudaMemcpyHostToDevice, s));
-    if (!two) {
+    if (resume) {  // the written total potential (fJmodels.cpp:63 state at the restart iteration)
+        FJ_CUDA(cudaMemcpyAsync(potA, cfg->phil_in, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+        FJ_CUDA(cudaMemcpyAsync(potA + nt, cfg->Pr_in, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+        FJ_CUDA(cudaMemcpyAsync(potA + 2 * nt, cfg->Pr2_in, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+    } else if (!two) {
         if ((rc = fj_poisson(ctx, nr, npl, d_ar, d_rhl, potA, potA + nt, potA + 2 * nt))) return rc;
     } else {  // each component's guess potential, total = their sum (fJmodels.cpp:49-59)
         if ((rc = fj_poisson(ctx, nr, npl, d_ar, d_rhl, potC, potC + nt, potC + 2 * nt))) return rc;
@@ -950,7 +994,7 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
         FJ_CUDA(launch_sum3(nt, potC, potC + nt, potC + 2 * nt, potD, potD + nt, potD + 2 * nt, potA, potA + nt,
                             potA + 2 * nt, s));
     }
-    // focal-distance table from the guess potential (fJmodels.cpp:63, 127)
+    // focal-distance table from the guess (or restart) potential (fJmodels.cpp:63, 127)
     std::vector<double> hp(3 * nt);
     FJ_CUDA(cudaMemcpyAsync(hp.data(), potA, 3 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
     FJ_CUDA(cudaStreamSynchronize(s));
@@ -1052,6 +1096,8 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
         if (c.nr < 11 || c.ngauss < 1 || c.npoly < 1 || c.npoly > kMaxPoly || c.ngrid < 2 || c.itermax < 1 ||
             c.ncomp > 1)
             return fail(ctx, FJ_ERR_ARG, "run_model_batch: bad sizes (one-component models only)");
+        if (c.ar_in || c.phil_in || c.Pr_in || c.Pr2_in)
+            return fail(ctx, FJ_ERR_ARG, "run_model_batch: restart tables are a fj_run_model option");
         if (c.rule.nq != rule.nq || c.rule.precision != rule.precision || c.rule.jquad != rule.jquad ||
             memcmp(c.rule.xq, rule.xq, rule.nq * sizeof(double)) || memcmp(c.rule.wq, rule.wq, rule.nq * sizeof(double)))
             return fail(ctx, FJ_ERR_ARG, "run_model_batch: all models must share one velocity rule");
@@ -1228,6 +1274,8 @@ extern "C" int fj_run_model_surrogate(fj_ctx *ctx, const fj_model_config *cfg, c
         cfg->rule.precision != FJ_PREC_MIXED || cfg->df.kind != FJ_DF_DPL || sch->exact_first < 1 ||
         sch->exact_last < 0 || sch->audit_stride < 1 || sch->samples < 1 || sch->epochs_first < 1 || sch->epochs < 1)
         return fail(ctx, FJ_ERR_ARG, "run_model_surrogate: needs one DPL component, the mixed rule and a valid schedule");
+    if (cfg->ar_in || cfg->phil_in || cfg->Pr_in || cfg->Pr2_in)
+        return fail(ctx, FJ_ERR_ARG, "run_model_surrogate: restart tables are a fj_run_model option");
     fj_surrogate_report rp{};
     auto now = [] { return std::chrono::steady_clock::now(); };
     auto ms_since = [](std::chrono::steady_clock::time_point t) {

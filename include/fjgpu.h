@@ -301,6 +301,18 @@ int fj_tabulate_delta(const fj_potential *pot_host, int ngrid, double *Egrid, do
    rhl, vrotl, sigRl, sigpl, sigzl, sigRzl, phil, Pr, Pr2. */
 int fj_write_out(const char *path, int nr, int npoly, int ngauss, const double *hdr10,
                  const double *ar, const double *mats9);
+/* The same file with `digits` significant digits per value (0 = the
+   reference's default stream precision, i.e. fj_write_out; 17 = every double
+   read back exactly, for a full-precision restart). */
+int fj_write_out_digits(const char *path, int nr, int npoly, int ngauss, const double *hdr10,
+                        const double *ar, const double *mats9, int digits);
+/* Reader of that file format (no reference counterpart: the reference writes
+   its models but never reads them back).  Call with ar = mats9 = NULL to get
+   nr, npoly, ngauss and hdr10[0..8] (dphi_h dz_h dphi_g dz_g chi mass r0 A B);
+   then with host ar [nr] and mats9 [9][nr*npoly] for the arrays.  FJ_ERR_IO
+   if the file cannot be opened, FJ_ERR_ARG if it is not in the format. */
+int fj_read_out(const char *path, int *nr, int *npoly, int *ngauss, double *hdr10, double *ar,
+                double *mats9);
 
 /* ------------------------------------------- whole model (host buffers) */
 
@@ -322,6 +334,12 @@ typedef struct fj_model_config {
     double mass2, r0_2, q2;
     fj_df_params df2;
     int twocomp_order;           /* FJ_TWOCOMP_* */
+    /* restart from written tables (fj_read_out; fj_run_model only): optional
+       host arrays, NULL = start from the guess density's potential */
+    const double *ar_in;         /* radial grid [nr] instead of the log grid of (rmin, rmax) */
+    const double *phil_in;       /* total potential tables [nr*npoly] to iterate from; */
+    const double *Pr_in;         /* the focal-distance table is tabulated from them unless */
+    const double *Pr2_in;        /* Egrid_in/Dgrid_in are given                           */
 } fj_model_config;
 
 /* Two-component iteration order.  SUMMED: both components' moments in the

@@ -95,3 +95,37 @@ def test_read_param_two_component_quirk(tmp_path):
 def test_compose_name():
     assert F.composeName("Hernquist", 0.55, 0.55, 1, 1, 3) == os.path.join("models", "Hernq_0.55_0.55_1.00_1.00_3.out")
     assert F.composeName("NFW", 0.5, 2, 1, 4, 0, comp=2).endswith("NFW_0.50_2.00_1.00_4.00_0.out2c")
+
+
+@pytest.mark.parametrize("name", ["hern_dpl", "nfw_dpl_rot"])
+def test_read_out_of_the_reference_file(name, tmp_path):
+    """The reference's own coefficient file (6 significant digits) read back: sizes, header
+    and every table within the rounding of the printed digits; a full-precision copy
+    (17 digits) reads back exactly; a truncated or missing file is an error."""
+    g, meta, _ = load_golden(name)
+    nr, ng, npl = meta["nr"], meta["ng"], meta["np"]
+    p = meta["p"]
+    name_ref = F.composeName(p["model"], p["dphi_h"], p["dz_h"], p["dphi_g"], p["dz_g"], 0)
+    f = tmp_path / "ref.out"
+    f.write_bytes(g["outfile_" + os.path.basename(name_ref).replace(".", "_")].tobytes())
+    r = F.readOut(str(f))
+    assert (r["nr"], r["npoly"], r["ngauss"]) == (nr, npl, ng)
+    assert np.allclose(r["header"][:7], [p["dphi_h"], p["dz_h"], p["dphi_g"], p["dz_g"], p["chi"], p["mass"], p["r0"]])
+    assert np.all(np.abs(r["ar"] - g["ar"]) <= 5e-6 * np.abs(g["ar"]))
+    keys = ("rhl", "vrotl", "sigRl", "sigpl", "sigzl", "sigRzl", "phil", "Pr", "Pr2")
+    for k in keys:
+        ref = g["it0_" + k].reshape(nr, npl)
+        assert np.all(np.abs(r[k] - ref) <= 5e-6 * np.abs(ref) + 1e-300), k
+    mats = np.stack([g["it0_" + k].reshape(nr, npl) for k in keys])
+    full = tmp_path / "full.out"
+    F.writeOut(str(full), g["ar"], mats, ng, r["header"], digits=17)
+    r17 = F.readOut(str(full))
+    assert np.array_equal(r17["ar"], g["ar"]) and np.array_equal(r17["header"], r["header"])
+    for i, k in enumerate(keys):
+        assert np.array_equal(r17[k], mats[i]), k
+    cut = tmp_path / "cut.out"
+    cut.write_bytes(full.read_bytes()[:-200])
+    with pytest.raises(F.FJError):
+        F.readOut(str(cut))
+    with pytest.raises(F.FJError):
+        F.readOut(str(tmp_path / "missing.out"))
