@@ -85,6 +85,19 @@ double orc_merge_distance(int nr, int npoly, const double *phil_new, const doubl
 /* focal-distance table (tabulate.cpp:13-38 + Delta.cpp) */
 int orc_tabulate_delta(const orc_model *m, double *Egrid, double *Dgrid);
 
+/* ---- projected density, line profile, velocity distributions (Integ.cpp:32-43,63-135,168-220) ---- */
+#define ORC_LOS_SIGMA 0  /* SigmaDF(R, z) from the density multipoles rhl      */
+#define ORC_LOS_LINE 1   /* line_profile(R, z, vx): v = vx in units of Ve      */
+#define ORC_LOS_PVPHI 2  /* P_vp(R, z, vphi)                                   */
+#define ORC_LOS_PVZ 3    /* P_vz(R, z, vz)                                     */
+#define ORC_LOS_PVR 4    /* P_vr(R, z, vR)                                     */
+/* the 22-point tanh-sinh table on [0,1] of include/GaussPts.h (xpt01/xw01) */
+void orc_tanh_sinh01(double *x, double *w);
+/* one value; the model's rule (xq, wq) is the [-1,1] rule (xpt11/xw11), x01/w01 the
+   [0,1] rule (22 points), rhl [nr*npoly] the density multipoles for SigmaDF */
+double orc_los(const orc_model *m, const double *rhl, int kind, double R, double z, double v,
+               const double *x01, const double *w01, orc_stats *st);
+
 #ifdef __cplusplus
 }
 #endif

@@ -94,6 +94,9 @@ def lib():
         L.orc_merge_distance.argtypes = [C.c_int, C.c_int, DP, DP]
         L.orc_merge_distance.restype = C.c_double
         L.orc_tabulate_delta.argtypes = [M, DP, DP]
+        L.orc_tanh_sinh01.argtypes = [DP, DP]
+        L.orc_los.argtypes = [M, DP, C.c_int, C.c_double, C.c_double, C.c_double, DP, DP, S]
+        L.orc_los.restype = C.c_double
         _LIB = L
     return _LIB
 
@@ -104,6 +107,17 @@ def _p(a):
 
 def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
+
+
+LOS_SIGMA, LOS_LINE, LOS_PVPHI, LOS_PVZ, LOS_PVR = range(5)
+
+
+def tanh_sinh01():
+    """The reference's 22-point tanh-sinh table on [0,1] (include/GaussPts.h:91-134)."""
+    x = np.zeros(22)
+    w = np.zeros(22)
+    lib().orc_tanh_sinh01(_p(x), _p(w))
+    return x, w
 
 
 def gauleg(x1, x2, n):
@@ -210,6 +224,13 @@ class Model:
         c6 = _f64(coef6)
         lib().orc_vir2(self.c(), _p(c6), _p(out))
         return dict(zip(("KRR", "Kzz", "WRR", "Wzz", "pot", "mass_pr", "mass_sum"), out))
+
+    def los(self, rhl, kind, R, z, v=0.0):
+        """SigmaDF / line_profile / P_vp / P_vz / P_vr (integ/Integ.cpp:168-220) at one (R, z, v);
+        rhl [nr][npoly] density multipoles (SigmaDF); the model's rule is the [-1,1] rule."""
+        x01, w01 = tanh_sinh01()
+        r = _f64(rhl)
+        return lib().orc_los(self.c(), _p(r), kind, R, z, v, _p(x01), _p(w01), None)
 
     def tabulate_delta(self, ngrid=30):
         E = np.zeros(ngrid)

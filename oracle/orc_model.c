@@ -10,6 +10,7 @@
  * capped here; hitting a cap counts a failure instead of hanging.
  */
 #include <float.h>
+#include <stdio.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -1032,4 +1033,94 @@ int orc_tabulate_delta(const orc_model *m, double *Egrid, double *Dgrid)
     }
     free(d);
     return fail;
+}
+
+/* ---------------- projected density, line profile, velocity distributions ---------------- */
+/* The 22-point tanh-sinh rule on [0,1] tabulated in include/GaussPts.h:91-134 (xpt01/xw01):
+   x_k = (1 + tanh(pi/2 sinh(k h)))/2, w_k = h pi/4 cosh(k h) / cosh^2(pi/2 sinh(k h)),
+   h = 2/11, k = -11..10, each printed to 12 significant digits. */
+void orc_tanh_sinh01(double *x, double *w)
+{
+    const double h = 2. / 11.;
+    for (int i = 0; i < 22; i++) {
+        const double t = (i - 11) * h, u = PI / 2 * sinh(t);
+        char buf[32];
+        snprintf(buf, sizeof buf, "%.12g", .5 * (1 + tanh(u)));
+        x[i] = strtod(buf, NULL);
+        snprintf(buf, sizeof buf, "%.12g", h * PI / 4 * cosh(t) / pow(cosh(u), 2));
+        w[i] = strtod(buf, NULL);
+    }
+}
+
+/* ev_dens, 1-field (include/UtilsLeg.h:285-298, 323-334): density from the multipoles rhl */
+static double ev_dens1(const orc_model *m, const double *rhl, double R, double z)
+{
+    const int nr = m->nr, np = m->npoly;
+    double pol[64], densp[64] = {0};
+    const double c = z / sqrt(R * R + z * z), r = sqrt(R * R + z * z);
+    orc_evenlegend(np, c, pol);
+    if (r > m->ar[nr - 1]) {
+        for (int i = 0; i < np; i++) densp[i] = 0;
+    } else {
+        int top, bot;
+        topbottom(m->ar, nr, r, &bot, &top);
+        const double f = (r - m->ar[bot]) / (m->ar[top] - m->ar[bot]);
+        for (int i = 0; i < np; i++) densp[i] = f * rhl[top * np + i] + (1 - f) * rhl[bot * np + i];
+    }
+    double dens = .5 * densp[0];
+    for (int l = 1; l < np; l++) dens += .5 * (4 * l + 1) * densp[l] * pol[l];
+    return dens;
+}
+
+/* SigmaDF (Integ.cpp:168-172) with SigmaInteg (:32-43) on the [0,1] rule */
+static double sigma_df(const orc_model *m, const double *rhl, double R, double z, const double *x01,
+                       const double *w01)
+{
+    const double rmax = m->ar[m->nr - 1], jac = rmax - R;
+    double s = 0;
+    for (int i = 0; i < 22; i++) s += w01[i] * (jac * ev_dens1(m, rhl, R + x01[i] * jac, z));
+    return 2 * s;
+}
+
+double orc_los(const orc_model *m, const double *rhl, int kind, double R, double z, double v,
+               const double *x01, const double *w01, orc_stats *st)
+{
+    if (kind == ORC_LOS_SIGMA) return sigma_df(m, rhl, R, z, x01, w01);
+    const double rmax = m->ar[m->nr - 1];
+    const double Phi = orc_phi(m, R, z), Ve = sqrt(-2 * (Phi - orc_phi(m, 10 * rmax, 10 * rmax)));
+    const int nq = m->nq;
+    const double *x11 = m->xq, *w11 = m->wq;
+    double sum = 0;
+    if (kind == ORC_LOS_LINE) {  /* Int3D_111111 of lineProfile (Integ.cpp:63-92, 177-186) */
+        for (int i = 0; i < nq; i++)
+            for (int j = 0; j < nq; j++)
+                for (int k = 0; k < nq; k++) {
+                    const double vy = x11[i], x = x11[j], vz = x11[k];
+                    const double Rp = sqrt(pow(R, 2) + pow(x * rmax, 2)), y = R;
+                    const double vabs = sqrt(v * v + vy * vy);
+                    const double alpha = acos(v / vabs), theta = atan2(y, x);
+                    const double vr = vabs * cos(alpha + theta), vphi = vabs * sin(alpha + theta);
+                    const double V[3] = {1e-6 + Ve * vr, 1e-6 + Ve * vphi, 1e-6 + Ve * vz};
+                    const double jacob = Ve * Ve * (fabs(x) * pow(rmax, 2)) / Rp;
+                    sum += w11[i] * w11[j] * w11[k] * (jacob * orc_df(m, R, z, Phi, V, st));
+                }
+        return sum / sigma_df(m, rhl, R, z, x01, w01);
+    }
+    if (kind == ORC_LOS_PVPHI) {  /* Int2D_0101 of Pvphi (Integ.cpp:97-109, 191-198) */
+        for (int i = 0; i < 22; i++)
+            for (int j = 0; j < 22; j++) {
+                const double V[3] = {1e-6 + Ve * x01[i], v, 1e-6 + Ve * x01[j]};
+                sum += w01[i] * w01[j] * (Ve * Ve * orc_df(m, R, z, Phi, V, st));
+            }
+        return sum;
+    }
+    /* Int2D_0111 of Pvz / Pvr (Integ.cpp:110-135, 202-220) */
+    for (int i = 0; i < 22; i++)
+        for (int j = 0; j < nq; j++) {
+            double V[3];
+            if (kind == ORC_LOS_PVZ) { V[0] = 1e-6 + Ve * x01[i]; V[1] = 1e-6 + Ve * x11[j]; V[2] = v; }
+            else { V[0] = v; V[1] = 1e-6 + Ve * x11[j]; V[2] = 1e-6 + Ve * x01[i]; }
+            sum += w01[i] * w11[j] * (Ve * Ve * orc_df(m, R, z, Phi, V, st));
+        }
+    return sum;
 }

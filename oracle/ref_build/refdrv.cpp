@@ -9,7 +9,10 @@
  *   refdrv <param file> <rmin> <rmax> <points file or -> <dump file>
  *
  * Points file lines: "P R z" (potential and gradient), "A R z vR vphi vz"
- * (actions with Delta from the table, as df() does), "M R z" (rhofDF).
+ * (actions with Delta from the table, as df() does), "M R z" (rhofDF),
+ * "S R z" (SigmaDF), "L R z vx" (line_profile), "F R z vphi" (P_vp),
+ * "Z R z vz" (P_vz), "X R z vR" (P_vr), all in the guess potential with the
+ * guess density multipoles.
  * FJREF_DELTA_FILE, when set, names a file with a focal-distance table
  * (Egrid then Dgrid) used instead of tabulateDelta.
  */
@@ -107,8 +110,16 @@ int main(int argc, char **argv)
     dumpv("Dgrid", Dgrid, NGRID);
 
     setDF(&fJP, &p, 1);
-    std::vector<double> av, mv;
+    std::vector<double> av, mv, lv;
     for (auto &v : pts) {
+        switch ((char)v[0]) {
+        case 'S': lv.push_back(SigmaDF(v[1], v[2])); break;
+        case 'L': lv.push_back(line_profile(v[1], v[2], v[3], &p)); break;
+        case 'F': lv.push_back(P_vp(v[1], v[2], v[3], &p)); break;
+        case 'Z': lv.push_back(P_vz(v[1], v[2], v[3], &p)); break;
+        case 'X': lv.push_back(P_vr(v[1], v[2], v[3], &p)); break;
+        default: break;
+        }
         if ((char)v[0] == 'A') {
             double x[3] = {v[1], v[2], p(v[1], v[2])}, vel[2] = {v[3], v[5]};
             double H = .5 * (v[3] * v[3] + v[4] * v[4] + v[5] * v[5]) + x[2];
@@ -125,6 +136,7 @@ int main(int argc, char **argv)
     }
     dumpv("actions", av.data(), (int)av.size());
     dumpv("moments", mv.data(), (int)mv.size());
+    dumpv("los", lv.data(), (int)lv.size());
     fflush(out);
 
     for (int k = 0; k < fJP.itermax; k++) {

@@ -62,6 +62,14 @@ def points(seed):
         lines.append(f"A {r * np.sqrt(1 - c * c):.17g} {r * c:.17g} {v[0]:.17g} {v[1]:.17g} {v[2]:.17g}")
     for R, z in ((0.8, 0.3), (2.0, 1.5)):
         lines.append(f"M {R:.17g} {z:.17g}")
+    # projected density, line profiles and velocity distributions (Integ.cpp:168-220)
+    for R, z in ((0.5, 0.2), (3.0, 0.05)):
+        lines.append(f"S {R:.17g} {z:.17g}")
+    for R, z, v in ((0.5, 0.2, 0.3), (0.5, 0.2, -0.05), (3.0, 0.05, 0.6)):
+        lines.append(f"L {R:.17g} {z:.17g} {v:.17g}")
+    for kind in "FZX":
+        for R, z, v in ((0.5, 0.2, 0.2), (3.0, 0.05, -0.1)):
+            lines.append(f"{kind} {R:.17g} {z:.17g} {v:.17g}")
     return "\n".join(lines) + "\n"
 
 

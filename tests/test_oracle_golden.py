@@ -87,3 +87,39 @@ def test_first_iteration_matches_reference(name):
     mine = [v["mass_pr"], v["mass_sum"], K, v["pot"], v["pot"] / K, v["KRR"], v["WRR"], v["WRR"] / v["KRR"],
             v["Kzz"], v["Wzz"], v["Wzz"] / v["Kzz"]]
     assert np.max(_nan_diff(np.array(mine), g["vir2"][0])) < 1.5e-6
+
+
+LOS_KINDS = {"S": O.LOS_SIGMA, "L": O.LOS_LINE, "F": O.LOS_PVPHI, "Z": O.LOS_PVZ, "X": O.LOS_PVR}
+
+
+def los_items(pts):
+    """(kind, R, z, v) of the projected-density, line-profile and velocity-distribution
+    points, in fixture order."""
+    return [(LOS_KINDS[a[0]], float(a[1]), float(a[2]), float(a[3]) if len(a) > 3 else 0.0)
+            for a in pts if a[0] in LOS_KINDS]
+
+
+@pytest.mark.parametrize("name", SCENARIOS)
+def test_line_profiles_and_velocity_distributions_match_reference(name):
+    """SigmaDF, line_profile, P_vp, P_vz, P_vr (integ/Integ.cpp:168-220) in the guess
+    potential with the guess density multipoles; the reference sums its tensor rules in
+    OpenMP order, so agreement is to rounding (1e-12 relative)."""
+    g, meta, pts = load_golden(name)
+    nr, npl = meta["nr"], meta["np"]
+    m = oracle_model(g, meta, g["guess_phil"].reshape(nr, npl), g["guess_Pr"].reshape(nr, npl),
+                     g["guess_Pr2"].reshape(nr, npl))
+    items = los_items(pts)
+    got = np.array([m.los(g["guess_rhl"].reshape(nr, npl), *it) for it in items])
+    ref = g["los"]
+    assert len(items) == len(ref) == 11
+    assert np.all(np.isfinite(ref)) and np.all(ref > 0)
+    assert rel(got, ref) < 1e-12, np.abs(got / ref - 1)
+
+
+def test_tanh_sinh_table_is_the_reference_table():
+    """orc_tanh_sinh01 regenerates include/GaussPts.h's 22-point [0,1] table from the
+    tanh-sinh formula (h = 2/11, 12 significant digits): symmetric about 1/2 and
+    integrating polynomials on [0, 1]."""
+    x, w = O.tanh_sinh01()
+    assert np.all(np.diff(x) > 0) and x[11] == 0.5 and abs(w.sum() - 1) < 4e-5  # the table stops at k = 10 and -11
+    assert np.allclose(x[1:] + x[:0:-1], 1, atol=2e-12)
