@@ -47,7 +47,7 @@ FP64_FLOPS_PER_EVAL = {"plain": 1.23e5, "gl": None}
 # FP32 operations (fadd + fmul + 2*ffma) executed by active lanes per phase-space
 # evaluation of the mixed form, from ncu on a 240-point spread of the same workload
 # (profiles/moments_mixed_nfw_80x40.md)
-FP32_FLOPS_PER_EVAL = {"mixed": 4.78e4}
+FP32_FLOPS_PER_EVAL = {"mixed": 4.68e4}
 
 
 def parse():
