@@ -48,6 +48,11 @@ FP64_FLOPS_PER_EVAL = {"plain": 1.23e5, "gl": None}
 # evaluation of the mixed form, from ncu on a 240-point spread of the same workload
 # (profiles/moments_mixed_nfw_80x40.md)
 FP32_FLOPS_PER_EVAL = {"mixed": 4.68e4}
+# DRAM bytes (read + write) per phase-space evaluation from the same captures:
+# 418.6 MB over 2,555,520 evaluations (mixed; local-memory and partial-sum
+# traffic, the inputs are < 16 KB), 53.4 MB over 255,552 (plain FP64); a launch's
+# traffic scales with its evaluations
+DRAM_BYTES_PER_EVAL = {"mixed": 418.6e6 / 2555520, "plain": 53.4e6 / 255552}
 
 
 def parse():
@@ -259,7 +264,9 @@ def run_ours(args, rank, world):
                      "achieved": achieved, "peak": float(peak[0]),
                      "unit": "TFLOP/s", "frac": (achieved / peak[0]) if achieved else None,
                      "peak_source": f"fj_measure_fma_peak ({'FP32' if fp32 else 'FP64'} FMA chains, this GPU)",
-                     "flops_per_eval": flops, "traffic": None},
+                     "flops_per_eval": flops,
+                     "traffic": (DRAM_BYTES_PER_EVAL[args.form] * nodes) if args.form in DRAM_BYTES_PER_EVAL else None,
+                     "traffic_unit": "bytes per launch (ncu capture of a 240-point case, scaled by evaluations)"},
         "clocks": clk.summary(),
     }
     ctx.close()
