@@ -73,6 +73,7 @@ class fj_model_result(C.Structure):
 
 
 P = C.POINTER
+FJ_LOS_SIGMA, FJ_LOS_LINE, FJ_LOS_PVPHI, FJ_LOS_PVZ, FJ_LOS_PVR = range(5)
 CTX = C.c_void_p
 SIGNATURES = {
     "fj_version": ([], C.c_char_p),
@@ -116,6 +117,9 @@ SIGNATURES = {
                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, P(fj_moment_stats)], C.c_int),
     "fj_actions": ([CTX, P(fj_potential), P(fj_delta_table), C.c_void_p, C.c_size_t, C.c_int, C.c_void_p], C.c_int),
     "fj_potential_eval": ([CTX, P(fj_potential), C.c_void_p, C.c_size_t, C.c_void_p], C.c_int),
+    "fj_los": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule), C.c_void_p, C.c_int,
+                C.c_void_p, C.c_int, C.c_void_p, P(fj_moment_stats)], C.c_int),
+    "fj_tanh_sinh01": ([DP, DP], C.c_int),
     "fj_vir2": ([CTX, P(fj_potential), C.c_int, C.c_void_p, DP], C.c_int),
     "fj_measure_fma_peak": ([C.c_int, DP], C.c_int),
     "fj_log_grid": ([C.c_double, C.c_double, C.c_int, DP], C.c_int),

@@ -306,6 +306,49 @@ class Context:
         self._check(self.lib.fj_potential_eval(self.h, C.byref(pot.c), _ptr(Rz), Rz.shape[0], _ptr(out)),
                     "fj_potential_eval")
 
+    def los(self, pot, delta, df, rule, rhl, kind, Rzv, out):
+        """SigmaDF / line_profile / P_vp / P_vz / P_vr (integ/Integ.cpp:168-220) at Rzv (device
+        [n][3] = R, z, v) into out (device [n]); rhl device [nr][npoly] density multipoles
+        (needed by SIGMA and LINE, else may be None).  Returns the fj_moment_stats."""
+        self._on_torch_stream()
+        st = A.fj_moment_stats()
+        self._check(self.lib.fj_los(self.h, C.byref(pot.c), C.byref(delta.c), C.byref(df.c), C.byref(rule.c),
+                                    _ptr(rhl) if rhl is not None else None, kind, _ptr(Rzv), Rzv.shape[0],
+                                    _ptr(out), C.byref(st)), "fj_los")
+        return st
+
+    def line_profile_file(self, path, pot, delta, df, rule, rhl, size_lp=150):
+        """The line-profile file of writeOut (io/writeOut.cpp:159-187, its LINEPROFILE block):
+        size_lp rows of (vx, line profile) at the centre (ar[0], ar[0]), at ar[2 nr/3] and at
+        ar[5 nr/6] (z = ar[0]), vx = 3 v_i on a signed log grid in units of each point's
+        escape speed, the first column of each pair scaled by it.  pot's tables on the device."""
+        import torch
+        ar = pot.owners[0].cpu().numpy()
+        nr = len(ar)
+        rmax = ar[-1]
+        pts = torch.tensor([[ar[0], ar[0]], [ar[nr * 2 // 3], ar[0]], [ar[nr * 5 // 6], ar[0]],
+                            [10 * rmax, 10 * rmax]], dtype=torch.float64, device="cuda")
+        ph = torch.zeros((4, 3), dtype=torch.float64, device="cuda")
+        self.potential_eval(pot, pts, ph)
+        phi = ph[:, 0].cpu().numpy()
+        ve = np.sqrt(-2 * (phi[:3] - phi[3]))
+        half = size_lp // 2
+        v = np.zeros(size_lp)
+        for i in range(half):
+            v[i] = -10.0 ** (-3.0 + (half - 1 - i) * 3.0 / (half - 1))
+        for i in range(half, size_lp):
+            v[i] = 10.0 ** (-3.0 + (i - half) * 3.0 / (half - 1))
+        Rz = [(ar[0], ar[0]), (ar[nr * 2 // 3], ar[0]), (ar[nr * 5 // 6], ar[0])]
+        rzv = torch.tensor([[R, z, 3.0 * vi] for R, z in Rz for vi in v], dtype=torch.float64, device="cuda")
+        out = torch.zeros(rzv.shape[0], dtype=torch.float64, device="cuda")
+        self.los(pot, delta, df, rule, rhl, A.FJ_LOS_LINE, rzv, out)
+        lp = out.cpu().numpy().reshape(3, size_lp)
+        with open(path, "w") as f:
+            for i in range(size_lp):
+                f.write(" ".join(f"{x:g}" for x in (ve[0] * 3.0 * v[i], lp[0, i], ve[1] * 3.0 * v[i], lp[1, i],
+                                                    ve[2] * 3.0 * v[i], lp[2, i])) + "\n")
+        return lp
+
     def vir2(self, pot, ngauss, coef6):
         self._on_torch_stream()
         out = np.zeros(7)
@@ -360,6 +403,14 @@ def log_grid(rmin, rmax, n):
     if A.load().fj_log_grid(rmin, rmax, n, _dp(ar)) != A.FJ_OK:
         raise FJError("log_grid: bad arguments")
     return ar
+
+
+def tanh_sinh01():
+    """The reference's 22-point tanh-sinh table on [0,1] (include/GaussPts.h:91-134)."""
+    x = np.zeros(22)
+    w = np.zeros(22)
+    A.load().fj_tanh_sinh01(_dp(x), _dp(w))
+    return x, w
 
 
 def gauleg(x1, x2, n):

@@ -574,6 +574,57 @@ int fj_vir2(fj_ctx *ctx, const fj_potential *pot, int ngauss, const double *coef
     return FJ_OK;
 }
 
+// ------------------------------------------- line of sight, velocity PDFs
+// the 22-point [0,1] tanh-sinh table of include/GaussPts.h:91-134:
+// x_k = (1 + tanh(pi/2 sinh(k h)))/2, w_k = h pi/4 cosh(k h)/cosh^2(pi/2 sinh(k h)),
+// h = 2/11, k = -11..10, each rounded to the table's 12 significant digits
+int fj_tanh_sinh01(double *x, double *w)
+{
+    if (!x || !w) return FJ_ERR_ARG;
+    const double h = 2. / 11.;
+    for (int i = 0; i < kLos01; i++) {
+        const double t = (i - 11) * h, u = kPI / 2 * sinh(t);
+        char buf[40];
+        snprintf(buf, sizeof buf, "%.12g", .5 * (1 + tanh(u)));
+        x[i] = strtod(buf, nullptr);
+        snprintf(buf, sizeof buf, "%.12g", h * kPI / 4 * cosh(t) / pow(cosh(u), 2));
+        w[i] = strtod(buf, nullptr);
+    }
+    return FJ_OK;
+}
+
+int fj_los(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
+           const fj_quad_rule *rule, const double *rhl, int kind, const double *Rzv, int n, double *out,
+           fj_moment_stats *stats)
+{
+    if (!ctx) return FJ_ERR_ARG;
+    if (kind < FJ_LOS_SIGMA || kind > FJ_LOS_PVR || !Rzv || n < 1 || !out)
+        return fail(ctx, FJ_ERR_ARG, "los: bad kind, points or output");
+    if ((kind == FJ_LOS_SIGMA || kind == FJ_LOS_LINE) && !rhl)
+        return fail(ctx, FJ_ERR_ARG, "los: SigmaDF needs the density multipoles");
+    if (!rule || rule->precision != FJ_PREC_FP64) return fail(ctx, FJ_ERR_ARG, "los: FP64 rule only");
+    LosArgs a;
+    bool mixed = false;
+    int rc = build_args(ctx, pot, delta, df, rule, 0, Rzv, n, out, a.m, mixed);
+    if (rc) return rc;
+    if ((rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long)))) return rc;
+    a.m.counters = (unsigned long long *)ctx->counters.p;
+    a.rhl = rhl; a.kind = kind; a.Rzv = Rzv; a.n = n; a.out = out;
+    fj_tanh_sinh01(a.x01, a.w01);
+    FJ_CUDA(cudaMemsetAsync(ctx->counters.p, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    FJ_CUDA(launch_los(a, ctx->stream));
+    FJ_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (stats) {
+        const long long nq = rule->nq;
+        const long long per = kind == FJ_LOS_LINE ? nq * nq * nq
+                              : kind == FJ_LOS_PVPHI ? (long long)kLos01 * kLos01
+                              : kind == FJ_LOS_SIGMA ? 0 : kLos01 * nq;
+        return read_stats(ctx, per * n, stats);
+    }
+    return FJ_OK;
+}
+
 // ------------------------------------------------------------ host setup
 int fj_log_grid(double rmin, double rmax, int n, double *ar)
 {

@@ -39,6 +39,21 @@ struct MomentArgs {
     double *out6;            // [6][npts]
 };
 
+// Projected density, line profiles and velocity distributions (fj_los.cu):
+// n values at Rzv [n][3] (R, z, v) of one kind (FJ_LOS_*), on m's potential,
+// focal-distance table, [-1,1] rule and DF, with the 22-point [0,1] table
+constexpr int kLos01 = 22;
+struct LosArgs {
+    MomentArgs m;
+    const double *rhl;  // [nr*npoly] density multipoles (SigmaDF)
+    int kind;
+    const double *Rzv;
+    int n;
+    double *out;        // [n]
+    double x01[kLos01], w01[kLos01];
+};
+cudaError_t launch_los(const LosArgs &a, cudaStream_t s);
+
 // Several models' phase-space launches in one grid: model m owns blocks
 // [block_start[m], block_start[m+1]) and grid points [point_start[m],
 // point_start[m+1]) of the batched finalize.  All pointers are device memory;

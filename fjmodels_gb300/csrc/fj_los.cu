@@ -1,0 +1,170 @@
+// fj_los.cu -- projected density, line-of-sight velocity profiles and
+// velocity distributions of a model (integ/Integ.cpp:32-43, 63-135, 168-220):
+// the phase-space kernel's node body (Staeckel-fudge actions + DF, plain FP64)
+// under 3-D and 2-D tensor rules.
+//
+// One block per requested value.  Its threads take the rule's nodes
+// round-robin and each sums its nodes in node order; the block adds the
+// thread sums in a fixed order, so a value is the same run to run.
+//   SIGMA  SigmaDF(R, z) = 2 sum_i w01_i (rmax - R) rho(R + x01_i (rmax - R), z),
+//          rho from the density multipoles (ev_dens, UtilsLeg.h:285-298, 323-334)
+//   LINE   line_profile(R, z, vx): [-1,1]^3 rule over (vy, x, vz), the DF at the
+//          point's (R, z, Phi) with the velocity rotated by the line-of-sight
+//          angle and the Jacobian Ve^2 |x| rmax^2 / R' (Integ.cpp:63-92), / SigmaDF
+//   PVPHI  P_vp(R, z, vphi): [0,1]^2 over (vR, vz)                 (Integ.cpp:97-109)
+//   PVZ    P_vz(R, z, vz):   [0,1] x [-1,1] over (vR, vphi)       (Integ.cpp:110-122)
+//   PVR    P_vr(R, z, vR):   [0,1] x [-1,1] over (vz, vphi)       (Integ.cpp:123-135)
+// Built without FMA contraction, like the phase-space kernel it shares its
+// arithmetic with.
+#include "../../include/fjgpu.h"
+#include "fj_internal.h"
+
+namespace fj {
+
+namespace {
+
+constexpr int kLosBlock = 128;
+
+__device__ __forceinline__ double los_warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// ev_dens, 1-field (include/UtilsLeg.h:285-298, 323-334)
+__device__ double ev_dens1(const PotView &P, const double *rhl, double R, double z)
+{
+    const int nr = P.nr, np = P.npoly;
+    double pol[kMaxPoly], densp[kMaxPoly];
+    const double c = z / sqrt(R * R + z * z), r = sqrt(R * R + z * z);
+    const double c2 = c * c;
+    pol[0] = 1;
+    if (np > 1) pol[1] = 1.5 * c2 - .5;
+    for (int l = 2; l < np; l++) pol[l] = evenleg_next(l, c2, pol[l - 2], pol[l - 1]);
+    if (r > P.ar[nr - 1]) {
+        for (int i = 0; i < np; i++) densp[i] = 0;
+    } else {
+        int top = 0, bot = 0;
+        topbottom(P.ar, nr, r, bot, top);
+        const double f = (r - P.ar[bot]) / (P.ar[top] - P.ar[bot]);
+        for (int i = 0; i < np; i++) densp[i] = f * rhl[top * np + i] + (1 - f) * rhl[bot * np + i];
+    }
+    double dens = .5 * densp[0];
+    for (int l = 1; l < np; l++) dens += .5 * (4 * l + 1) * densp[l] * pol[l];
+    return dens;
+}
+
+__device__ double sigma_df(const PotView &P, const double *rhl, const LosArgs &a, double R, double z)
+{
+    const double rmax = P.ar[P.nr - 1], jac = rmax - R;
+    double s = 0;
+    for (int i = 0; i < kLos01; i++) s += a.w01[i] * (jac * ev_dens1(P, rhl, R + a.x01[i] * jac, z));
+    return 2 * s;
+}
+
+__global__ void __launch_bounds__(kLosBlock) k_los(LosArgs a)
+{
+    extern __shared__ double sm[];
+    const MomentArgs &m = a.m;
+    const int nr = m.P.nr, npoly = m.P.npoly, nt = nr * npoly;
+    double *s_ar = sm, *s_phil = s_ar + nr, *s_Pr = s_phil + nt, *s_Pr2 = s_Pr + nt;
+    double *s_Eg = s_Pr2 + nt, *s_Dg = s_Eg + m.ngrid, *s_xq = s_Dg + m.ngrid, *s_wq = s_xq + m.nq;
+    double *s_glx = s_wq + m.nq, *s_glw = s_glx + m.gl.n, *s_rhl = s_glw + m.gl.n, *s_red = s_rhl + nt;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) s_ar[i] = m.P.ar[i];
+    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+        s_phil[i] = m.P.phil[i]; s_Pr[i] = m.P.Pr[i]; s_Pr2[i] = m.P.Pr2[i];
+        s_rhl[i] = a.rhl ? a.rhl[i] : 0.;
+    }
+    for (int i = threadIdx.x; i < m.ngrid; i += blockDim.x) { s_Eg[i] = m.Eg[i]; s_Dg[i] = m.Dg[i]; }
+    for (int i = threadIdx.x; i < m.nq; i += blockDim.x) { s_xq[i] = m.xq[i]; s_wq[i] = m.wq[i]; }
+    for (int i = threadIdx.x; i < m.gl.n; i += blockDim.x) { s_glx[i] = m.gl.x01[i]; s_glw[i] = m.gl.w01[i]; }
+    __syncthreads();
+    const PotView P{nr, npoly, s_ar, s_phil, s_Pr, s_Pr2};
+    const GLRule gl{m.gl.n, s_glx, s_glw};
+    const int item = blockIdx.x;
+    const double R = a.Rzv[3 * item], z = a.Rzv[3 * item + 1], v = a.Rzv[3 * item + 2];
+    if (a.kind == FJ_LOS_SIGMA) {
+        if (threadIdx.x == 0) a.out[item] = sigma_df(P, s_rhl, a, R, z);
+        return;
+    }
+    const double rmax = s_ar[nr - 1];
+    const double Phi = pot_phi(P, R, z), Ve = sqrt(-2 * (Phi - pot_phi(P, 10 * rmax, 10 * rmax)));
+    const int nq = m.nq;
+    const int nnodes = a.kind == FJ_LOS_LINE ? nq * nq * nq : (a.kind == FJ_LOS_PVPHI ? kLos01 * kLos01 : kLos01 * nq);
+    double sum = 0;
+    unsigned failed = 0, bound = 0;
+    for (int node = threadIdx.x; node < nnodes; node += kLosBlock) {
+        double V[3], w, jacob;
+        if (a.kind == FJ_LOS_LINE) {  // lineProfile(vy, x, vz), Integ.cpp:63-92
+            const int i = node / (nq * nq), j = (node / nq) % nq, k = node % nq;
+            const double vy = s_xq[i], x = s_xq[j], vz = s_xq[k];
+            const double Rp = sqrt(R * R + (x * rmax) * (x * rmax)), y = R;
+            const double vabs = sqrt(v * v + vy * vy);
+            const double alpha = acos(v / vabs), theta = atan2(y, x);
+            const double vr = vabs * cos(alpha + theta), vphi = vabs * sin(alpha + theta);
+            V[0] = 1e-6 + Ve * vr; V[1] = 1e-6 + Ve * vphi; V[2] = 1e-6 + Ve * vz;
+            jacob = Ve * Ve * (fabs(x) * (rmax * rmax)) / Rp;
+            w = s_wq[i] * s_wq[j] * s_wq[k];
+        } else if (a.kind == FJ_LOS_PVPHI) {  // Pvphi(vr, vz), Integ.cpp:97-109
+            const int i = node / kLos01, j = node % kLos01;
+            V[0] = 1e-6 + Ve * a.x01[i]; V[1] = v; V[2] = 1e-6 + Ve * a.x01[j];
+            jacob = Ve * Ve;
+            w = a.w01[i] * a.w01[j];
+        } else {  // Pvz(vr, vphi) / Pvr(vz, vphi), Integ.cpp:110-135
+            const int i = node / nq, j = node % nq;
+            if (a.kind == FJ_LOS_PVZ) { V[0] = 1e-6 + Ve * a.x01[i]; V[1] = 1e-6 + Ve * s_xq[j]; V[2] = v; }
+            else { V[0] = v; V[1] = 1e-6 + Ve * s_xq[j]; V[2] = 1e-6 + Ve * a.x01[i]; }
+            jacob = Ve * Ve;
+            w = a.w01[i] * s_wq[j];
+        }
+        const double H = .5 * (V[0] * V[0] + V[1] * V[1] + V[2] * V[2]) + Phi;
+        double DF = 0.;
+        if (H < 0) {  // df(), DF.cpp:78-124
+            unsigned fail = 0;
+            double Jr, Jz;
+            fudge_actions(P, deltafn(s_Eg, s_Dg, m.ngrid, H), R, z, Phi, V[0], V[1], V[2], gl, Jr, Jz, fail);
+            DF = df_value(m.df, P, R, Jr, Jz, R * V[1], fail);
+            if (fail & (kFailBracket | kFailRoot)) DF = 0.;
+            failed += fail ? 1u : 0u;
+            bound++;
+        }
+        sum += w * (jacob * DF);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double ws = los_warp_sum(sum);
+    if (lane == 0) s_red[warp] = ws;
+    const int nb = __syncthreads_count(bound);
+    const int nf = __syncthreads_count(failed);
+    if (threadIdx.x == 0) {
+        double s = 0;
+        for (int q = 0; q < kLosBlock / 32; q++) s += s_red[q];
+        if (a.kind == FJ_LOS_LINE) s /= sigma_df(P, s_rhl, a, R, z);
+        a.out[item] = s;
+        if (a.m.counters) {
+            if (nb) atomicAdd(&a.m.counters[0], (unsigned long long)nb);
+            if (nf) atomicAdd(&a.m.counters[1], (unsigned long long)nf);
+        }
+    }
+}
+
+}  // namespace
+
+size_t los_smem_bytes(const MomentArgs &m)
+{
+    const size_t nt = (size_t)m.P.nr * m.P.npoly;
+    return (m.P.nr + 4 * nt + 2 * m.ngrid + 2 * m.nq + 2 * m.gl.n + kLosBlock / 32) * sizeof(double);
+}
+
+cudaError_t launch_los(const LosArgs &a, cudaStream_t s)
+{
+    const size_t smem = los_smem_bytes(a.m);
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(k_los, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    k_los<<<a.n, kLosBlock, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace fj

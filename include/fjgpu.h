@@ -131,6 +131,31 @@ int fj_moments_points(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table
                       const fj_df_params *df, const fj_quad_rule *rule, const double *Rz, int npts,
                       double *out6, fj_moment_stats *stats);
 
+/* Projected density, line-of-sight velocity profile and velocity
+   distributions: SigmaDF, line_profile, P_vp, P_vz, P_vr (integ/Integ.cpp:
+   168-220 with SigmaInteg :32-43, lineProfile :63-92, Pvphi/Pvz/Pvr
+   :97-135), n values of one kind at device Rzv [n][3] = (R, z, v):
+     FJ_LOS_SIGMA  v unused: 2 x the line-of-sight integral of the density
+                   from R to ar[nr-1] at height z, from the multipoles rhl;
+     FJ_LOS_LINE   v = vx in units of the escape speed: the [-1,1]^3 rule over
+                   (vy, x, vz), divided by SigmaDF (so rhl is needed too);
+     FJ_LOS_PVPHI, FJ_LOS_PVZ, FJ_LOS_PVR  v = the fixed velocity component.
+   The [-1,1] axes take `rule` (host arrays; precision FJ_PREC_FP64; jquad as
+   for the moments), the [0,1] axes the reference's 22-point tanh-sinh table
+   (fj_tanh_sinh01).  rhl device [nr*npoly] (may be NULL for PVPHI, PVZ,
+   PVR); out device [n].  Plain FP64, one thread block per value. */
+#define FJ_LOS_SIGMA 0
+#define FJ_LOS_LINE 1
+#define FJ_LOS_PVPHI 2
+#define FJ_LOS_PVZ 3
+#define FJ_LOS_PVR 4
+int fj_los(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, const fj_df_params *df,
+           const fj_quad_rule *rule, const double *rhl, int kind, const double *Rzv, int n, double *out,
+           fj_moment_stats *stats);
+/* The 22-point tanh-sinh table on [0,1] of include/GaussPts.h:91-134
+   (xpt01/xw01), regenerated from its formula; host x[22], w[22]. */
+int fj_tanh_sinh01(double *x, double *w);
+
 /* Many models' phase-space integrals in one launch (no reference counterpart:
    the reference builds one model per process).  Item m is one model's
    computeRhl grid (pot/potLeg.cpp:35-70): its own device potential, Delta
