@@ -62,7 +62,8 @@ class fj_model_config(C.Structure):
                 ("df", fj_df_params), ("rule", fj_quad_rule), ("itermax", C.c_int), ("tol", C.c_double),
                 ("Egrid_in", DP), ("Dgrid_in", DP), ("ncomp", C.c_int), ("guess2", C.c_int),
                 ("mass2", C.c_double), ("r0_2", C.c_double), ("q2", C.c_double), ("df2", fj_df_params),
-                ("twocomp_order", C.c_int), ("ar_in", DP), ("phil_in", DP), ("Pr_in", DP), ("Pr2_in", DP)]
+                ("twocomp_order", C.c_int), ("ar_in", DP), ("phil_in", DP), ("Pr_in", DP), ("Pr2_in", DP),
+                ("delta_gpu", C.c_int), ("delta_every", C.c_int)]
 
 
 class fj_model_result(C.Structure):
@@ -120,6 +121,8 @@ SIGNATURES = {
     "fj_los": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule), C.c_void_p, C.c_int,
                 C.c_void_p, C.c_int, C.c_void_p, P(fj_moment_stats)], C.c_int),
     "fj_tanh_sinh01": ([DP, DP], C.c_int),
+    "fj_tabulate_delta_batch": ([CTX, C.c_int, P(fj_potential), C.c_int, C.c_void_p, C.c_void_p, P(C.c_int)],
+                                C.c_int),
     "fj_vir2": ([CTX, P(fj_potential), C.c_int, C.c_void_p, DP], C.c_int),
     "fj_measure_fma_peak": ([C.c_int, DP], C.c_int),
     "fj_log_grid": ([C.c_double, C.c_double, C.c_int, DP], C.c_int),

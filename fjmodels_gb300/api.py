@@ -212,9 +212,12 @@ class Context:
                    setup_ms=res.setup_ms)
         return out, {f: getattr(rep, f) for f, _ in A.fj_surrogate_report._fields_}
 
-    def run_model_batch(self, models, rule, itermax, tol=0.0, ngrid=30, use_graph=True):
+    def run_model_batch(self, models, rule, itermax, tol=0.0, ngrid=30, use_graph=True, delta_gpu=False,
+                        delta_every=0):
         """Several one-component models iterated together (fj_run_model_batch).  models = list of
-        dicts with nr, ngauss, npoly, rmin, rmax, df (DFParams) and optional q, delta_table."""
+        dicts with nr, ngauss, npoly, rmin, rmax, df (DFParams) and optional q, delta_table.
+        delta_gpu: focal-distance tables on the GPU, all models in one launch; delta_every = 1
+        tabulates them again before every later iteration."""
         self.use_own_stream()
         n = len(models)
         cfgs = (A.fj_model_config * n)()
@@ -228,6 +231,7 @@ class Context:
             cfgs[i] = A.fj_model_config(nr, ng, npl, ngrid, m["rmin"], m["rmax"], A.FJ_GUESS.get(df.model, 0), df.mass,
                                         df.r0, m.get("q", 1.0), df.c, rule.c, itermax, tol,
                                         *[_dp(d) if d is not None else None for d in din])
+            cfgs[i].delta_gpu, cfgs[i].delta_every = int(delta_gpu), int(delta_every)
             out = {"ar": np.zeros(nr), "coef6": np.zeros((6, nr, npl)), "phil": np.zeros((nr, npl)),
                    "Pr": np.zeros((nr, npl)), "Pr2": np.zeros((nr, npl)), "Egrid": np.zeros(ngrid),
                    "Dgrid": np.zeros(ngrid)}
@@ -239,6 +243,20 @@ class Context:
             out.update(vir7=np.array(r.vir7[:]), iterations=r.iterations, last_change=r.last_change, bound=r.bound,
                        failures=r.failures, wall_ms=r.wall_ms, kernel_ms=r.kernel_ms, setup_ms=r.setup_ms)
         return outs
+
+    def tabulate_delta_batch(self, pots, ngrid=30):
+        """Focal-distance tables of several models on the GPU (fj_tabulate_delta_batch); pots from
+        potential().  Returns device (Egrid, Dgrid) [n][ngrid] and the per-model status list."""
+        import torch
+        self._on_torch_stream()
+        n = len(pots)
+        arr = (A.fj_potential * n)(*[p.c for p in pots])
+        E = torch.zeros((n, ngrid), dtype=torch.float64, device="cuda")
+        D = torch.zeros_like(E)
+        st = (C.c_int * n)()
+        self._check(self.lib.fj_tabulate_delta_batch(self.h, n, arr, ngrid, _ptr(E), _ptr(D), st),
+                    "fj_tabulate_delta_batch")
+        return E, D, list(st)
 
     def tc_gemm(self, a, b, c, ksplit=1):
         """c = a @ b.T on the tensor cores: a [M][K], b [N][K] bfloat16, c [M][N] float32 (device)."""
@@ -358,16 +376,19 @@ class Context:
     # ---------------------------------------------------------------- whole model
     def run_model(self, nr, ngauss, npoly, rmin, rmax, df, rule, itermax, tol=0.0, ngrid=30, q=1.0,
                   keep_grids=False, delta_table=None, df2=None, q2=1.0, twocomp_order=A.FJ_TWOCOMP_SUMMED,
-                  restart=None):
+                  restart=None, delta_gpu=False, delta_every=0):
         """Self-consistent model (oneComp, fJmodels.cpp:86-144; with df2, the two-component
         loop of fJmodels.cpp:38-84 in `twocomp_order`) with host buffers.
         delta_table = (Egrid, Dgrid) uses a given focal-distance table instead of tabulating one;
         restart = a dict with ar, phil, Pr, Pr2 (readOut, or an earlier result) iterates on from
-        those tables instead of the guess density (rmin, rmax are then unused)."""
+        those tables instead of the guess density (rmin, rmax are then unused).
+        delta_gpu tabulates the focal-distance table on the GPU; delta_every = k > 0 tabulates it
+        again from the new potential after every k-th iteration (the reference: once)."""
         self.use_own_stream()
         din = [None, None] if delta_table is None else [_f64(delta_table[0]), _f64(delta_table[1])]
         cfg = A.fj_model_config(nr, ngauss, npoly, ngrid, rmin, rmax, A.FJ_GUESS.get(df.model, 0), df.mass, df.r0,
                                 q, df.c, rule.c, itermax, tol, *[_dp(d) if d is not None else None for d in din])
+        cfg.delta_gpu, cfg.delta_every = int(delta_gpu), int(delta_every)
         if restart is not None:
             rs = {k: _f64(restart[k]) for k in ("ar", "phil", "Pr", "Pr2")}
             if rs["ar"].size != nr or any(rs[k].size != nr * npoly for k in ("phil", "Pr", "Pr2")):

@@ -24,7 +24,7 @@ LIB = os.path.join(HERE, "libfjgpu.so")
 # contraction and uses the 2-ulp FP32 division and square root.
 SOURCES = {"fj_moments.cu": ["--fmad=false"], "fj_multipole.cu": ["--fmad=false"], "fj_api.cu": [],
            "fj_peak.cu": [], "fj_noalloc.cu": [], "fj_moments_mixed.cu": ["-prec-div=false", "-prec-sqrt=false"], "fj_mlp.cu": [],
-           "fj_los.cu": ["--fmad=false"]}
+           "fj_los.cu": ["--fmad=false"], "fj_delta.cu": ["--fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xcompiler", "-Wall,-Wno-unused-function,-ffp-contract=off"]

@@ -15,6 +15,7 @@
 
 #include "../../include/fjgpu.h"
 #include "fj_internal.h"
+#include "fj_delta.cuh"
 
 // the host-only functors below instantiate the __host__ __device__ Brent template on the host only
 #pragma nv_diag_suppress 20011, 20014
@@ -41,6 +42,7 @@ struct fj_ctx {
     float *jout = nullptr;                             // mixed form: actions of every bound node (fj_set_action_output)
     DevBuf batch;                                      // batched launch: MomentArgs[n] | block_start | point_start
     std::vector<char> batch_host;                      // what `batch` holds (re-uploaded only when it changes)
+    DevBuf delta_ws;                                   // GPU focal-distance tables: views | Eg ptrs | Dg ptrs | flags
 };
 
 namespace fj {
@@ -324,9 +326,8 @@ int fj_ctx_create(int device, fj_ctx **out)
     // call stack (about 5.5 KB, ptxas "cumulative stack size"); the function
     // attributes do not report call-stack frames, so the floor is explicit.
     size_t need = moments_local_bytes();
-    const size_t need2 = multipole_local_bytes(), need3 = moments_mixed_local_bytes();
-    if (need2 > need) need = need2;
-    if (need3 > need) need = need3;
+    for (size_t n2 : {multipole_local_bytes(), moments_mixed_local_bytes(), delta_local_bytes(), los_local_bytes()})
+        if (n2 > need) need = n2;
     need = (need + 1024 + 1023) / 1024 * 1024;
     if (need < kStackBytes) need = kStackBytes;
     size_t cur = 0;
@@ -676,264 +677,92 @@ int fj_guess_rhl(int nr, int ngauss, int npoly, const double *ar, int kind, doub
 }  // extern "C"
 
 // --------------------------------------------------- focal-distance table
-// tabulateDelta (delta/tabulate.cpp:13-38) and the Delta class
-// (delta/Delta.cpp) on the host.  Orbits use an extrapolated modified-
-// midpoint step (Bulirsch-Stoer) under the y-error step control of the
-// reference's integrator setup (abs 1e-10, rel 1e-9, Delta.cpp:59-69).
-namespace {
-
-constexpr int kOrbSize = 200;
-
-struct DeltaFit {
-    PotView P;
-    double E, Lz, Rc, R0, D2, sqDR, v0, cv, sv, Ri, zi;
-    double R[kOrbSize], z[kOrbSize];
-    int N;
-    bool bad;
-};
-
-void orbit_rhs(const DeltaFit &d, const double *y, double *f)
-{
-    double phi, dR, dz;
-    pot_grad(d.P, y[0], y[1], phi, dR, dz);
-    f[0] = y[2];
-    f[1] = y[3];
-    f[2] = -dR + pow(d.Lz, 2.0) / pow(y[0], 3.0);
-    f[3] = -dz;
-}
-
-void gbs_step(const DeltaFit &d, double h, const double *y0, double *y1, double *yerr)
-{
-    constexpr int K = 6;
-    double T[K][4], prev[4] = {0, 0, 0, 0};
-    for (int k = 0; k < K; k++) {
-        const int ns = 2 * (k + 1);
-        const double hs = h / ns;
-        double zm[4], zc[4], dy[4];
-        orbit_rhs(d, y0, dy);
-        for (int i = 0; i < 4; i++) { zm[i] = y0[i]; zc[i] = y0[i] + hs * dy[i]; }
-        for (int s = 1; s < ns; s++) {
-            orbit_rhs(d, zc, dy);
-            for (int i = 0; i < 4; i++) { const double zn = zm[i] + 2 * hs * dy[i]; zm[i] = zc[i]; zc[i] = zn; }
-        }
-        orbit_rhs(d, zc, dy);
-        for (int i = 0; i < 4; i++) T[k][i] = 0.5 * (zm[i] + zc[i] + hs * dy[i]);
-        for (int j = k - 1; j >= 0; j--) {
-            const double r = (double)(k + 1) / (double)(j + 1), fac = r * r - 1.0;
-            for (int i = 0; i < 4; i++) T[j][i] = T[j + 1][i] + (T[j + 1][i] - T[j][i]) / fac;
-        }
-        if (k == K - 2) for (int i = 0; i < 4; i++) prev[i] = T[0][i];
-    }
-    for (int i = 0; i < 4; i++) { y1[i] = T[0][i]; yerr[i] = T[0][i] - prev[i]; }
-}
-
-bool evolve_step(const DeltaFit &d, double &t, double t1, double &h, double *y)
-{
-    const double S = 0.9, ord = 8.0, epsabs = 1e-10, epsrel = 1e-9;
-    double h0 = h;
-    bool final = false;
-    if (h0 > t1 - t) { h0 = t1 - t; final = true; }
-    double y1[4], yerr[4];
-    for (int tries = 0; tries < 200; tries++) {
-        gbs_step(d, h0, y, y1, yerr);
-        double rmax = 0;
-        for (int i = 0; i < 4; i++) {
-            const double D0 = epsrel * fabs(y1[i]) + epsabs;
-            const double r = fabs(yerr[i]) / fabs(D0);
-            if (r > rmax) rmax = r;
-        }
-        if (rmax > 1.1 && h0 > 0) {
-            double r = S / pow(rmax, 1.0 / ord);
-            if (r < 0.2) r = 0.2;
-            h0 *= r;
-            final = false;
-            continue;
-        }
-        t = final ? t1 : t + h0;
-        for (int i = 0; i < 4; i++) y[i] = y1[i];
-        if (rmax < 0.5) {
-            double r = S / pow(rmax, 1.0 / (ord + 1.0));
-            if (r > 5.0) r = 5.0;
-            if (r < 1.0) r = 1.0;
-            h = r * h0;
-        } else h = h0;
-        return true;
-    }
-    return false;
-}
-
-double vsq(const DeltaFit &d, double x) { return 2 * (d.E - (pot_phi(d.P, x, 0.) + .5 * pow(d.Lz / x, 2))); }
-
-int evolve_orbit(DeltaFit &d, double x0, int cond)
-{
-    double steph = 2e-3, y[4] = {x0, 0., 0., sqrt(vsq(d, x0))}, t = 0;
-    int i = 0;
-    d.R[0] = y[0];
-    d.z[0] = y[1];
-    const double t1 = 5 * x0 / sqrt(vsq(d, x0));
-    while (i < kOrbSize - 1 && (cond == 0 ? y[1] >= 0. : y[3] >= 0.)) {
-        if (!evolve_step(d, t, t1, steph, y)) d.bad = true;
-        i++;
-        d.R[i] = y[0];
-        d.z[i] = y[1];
-    }
-    return i;
-}
-
-struct GetDRF {
-    DeltaFit *d;
-    double operator()(double x0) const
-    {
-        const int N = evolve_orbit(*d, x0, 0);
-        const double *R = d->R, *z = d->z;
-        if (fabs(z[N - 1] - z[N]) > 0 && fabs(R[N - 1] - R[N]) != 0)
-            return x0 - (R[N] - z[N] * (R[N - 1] - R[N]) / (z[N - 1] - z[N]));
-        return x0 - R[N];
-    }
-};
-
-double dphi_eff(const DeltaFit &d, double x)
-{
-    double phi, dR, dz;
-    pot_grad(d.P, x, 0, phi, dR, dz);
-    return dR - pow(d.Lz, 2) / pow(x, 3);
-}
-
-double ensure_vsq(DeltaFit &d, double x0)
-{
-    int count = 0;
-    while (vsq(d, x0) < 0) {
-        if (dphi_eff(d, x0) < 0) x0 *= 1.1; else x0 *= .9;
-        if (++count > 50) { d.bad = true; break; }
-    }
-    return x0;
-}
-
-double get_jr0(DeltaFit &d)
-{
-    GetDRF f{&d};
-    double x0 = d.Rc, x1, dx0, dx1, A = .8;
-    int k = 0;
-    x0 = ensure_vsq(d, x0); dx0 = f(x0);
-    x1 = ensure_vsq(d, x0 / A); dx1 = f(x1);
-    while (dx0 * dx1 > 0) {
-        if (fabs(dx1) < fabs(dx0)) { x0 = x1; dx0 = dx1; }
-        else A = pow(A, -0.9);
-        x1 = ensure_vsq(d, x0 * A); dx1 = f(x1);
-        if (++k == 21) {
-            if (fabs(dx0) < 1.e-7) return -x0;
-            return -1;  // Delta.cpp:145-151 goes on with -1
-        }
-    }
-    double r;
-    if (brent_root(f, x0 < x1 ? x0 : x1, x0 < x1 ? x1 : x0, r)) d.bad = true;
-    return r;
-}
-
-struct Ds2dvF {
-    DeltaFit *d;
-    double operator()(double v) const { return 2 * (d->zi * d->sqDR * sin(v) - cos(v) * (d->Ri * d->R0 + d->D2 * sin(v))); }
-};
-
-struct Ds2dD2F {
-    DeltaFit *d;
-    double operator()(double D2h) const
-    {
-        d->D2 = D2h;
-        d->sqDR = sqrt(d->D2 + d->R0 * d->R0);
-        Ds2dvF g{d};
-        double sum = 0.;
-        for (int i = 0; i < d->N; i++) {
-            d->Ri = d->R[i];
-            d->zi = d->z[i];
-            const double lo = 0, hi = kPIH;
-            if (fabs(g(lo)) < 1e-8) d->v0 = lo;
-            else if (fabs(g(hi)) < 1e-8) d->v0 = hi;
-            else if (brent_root(g, lo, hi, d->v0)) d->bad = true;
-            d->sv = sin(d->v0);
-            d->cv = cos(d->v0);
-            const double sv = d->sv, cv = d->cv, zi = d->zi, sq = d->sqDR;
-            const double dvdD2 = .5 * sv * (zi / sq - 2 * cv) / (cv * zi * sq + sv * d->Ri * d->R0 - d->D2 * (cv * cv - sv * sv));
-            sum += (cv - zi / sq) * cv + g(d->v0) * dvdD2;
-        }
-        return sum;
-    }
-};
-
-double get_rc_host(const PotView &P, double Lzsq, double R, bool &bad)
-{
-    unsigned f = 0;
-    const double r = get_rc(P, Lzsq, R, f);
-    if (f) bad = true;
-    return r;
-}
-
-struct RcEF {
-    PotView P; double E;
-    double operator()(double R) const
-    {
-        double phi, dR, dz;
-        pot_grad(P, R, 0, phi, dR, dz);
-        return .5 * R * dR + pot_phi(P, R, 0) - E;
-    }
-};
-
-}  // namespace
-
+// tabulateDelta (delta/tabulate.cpp:13-38) on the host, one energy after the
+// other (fj_delta.cuh); fj_tabulate_delta_batch runs the same code per
+// (model, energy) on the GPU.
 extern "C" int fj_tabulate_delta(const fj_potential *pot, int ngrid, double *Egrid, double *Dgrid)
 {
     if (!pot || pot->nr < 11 || pot->npoly < 1 || pot->npoly > kMaxPoly || ngrid < 2 || !Egrid || !Dgrid)
         return FJ_ERR_ARG;
     const PotView P = view(pot);
-    const double *ar = pot->ar;
-    const int nr = pot->nr;
-    bool bad = false;
-    const double Rmax = ar[nr - 1];
-    double phi, dRv, dzv;
-    const double Lzmax = Rmax * 0.98 * sqrt(-2 * pot_phi(P, Rmax, 0)), Rmin = 1e-3 * Rmax;
-    pot_grad(P, Rmin, 0, phi, dRv, dzv);
-    const double Lzmin = Rmin * sqrt(Rmin * dRv);
-    double R = .01 * Rmax, Lz1 = 0, Rg1 = 0, Ec1 = 0, Vmax1 = 0;
-    for (int i = 0; i < 2; i++) {  // only entries 0 and 1 of the reference's per-radius loop feed the table
-        const double Lzi = Lzmin + i * (Lzmax - Lzmin) / (double)(nr - 1);
-        R = get_rc_host(P, pow(Lzi, 2), R, bad);
-        pot_grad(P, R, 0, phi, dRv, dzv);
-        const double vc2 = R * dRv;
-        const double Ec = .5 * vc2 + pot_phi(P, R, 0);
-        Lz1 = Lzi; Rg1 = R; Ec1 = Ec; Vmax1 = .98 * sqrt(-2 * Ec);
-    }
+    const DeltaBase base = delta_base(P);
+    bool bad = base.bad;
     std::vector<DeltaFit> fits(1);
-    DeltaFit &d = fits[0];
-    for (int nE = 0; nE < ngrid; nE++) {
-        Egrid[nE] = Ec1 + .5 * pow(Vmax1 * (nE + 1) / (double)ngrid, 2);
-        memset(&d, 0, sizeof d);
-        d.P = P;
-        d.E = Egrid[nE];
-        d.Lz = .25 * Lz1;
-        // RcE (include/Utils.h:220-236)
-        RcEF fe{P, d.E};
-        double R0 = .8 * Rg1, f0 = fe(R0);
-        for (int it = 0; f0 > 0 && it < kLoopCap; it++) { R0 *= .8; f0 = fe(R0); }
-        double R1 = 1.2 * Rg1, f1 = fe(R1);
-        for (int it = 0; f1 < 0 && it < kLoopCap; it++) { R1 *= 1.2; f1 = fe(R1); }
-        if (brent_root(fe, R0, R1, d.Rc)) bad = true;
-        // getBestDelta (Delta.cpp:248-294)
-        d.R0 = get_jr0(d);
-        d.N = evolve_orbit(d, d.R0, 1);
-        Ds2dD2F g{&d};
-        double lo = -0.001, hi = 5, D2out = 0;
-        double Dmin = g(lo), Dmax = g(hi);
-        for (int it = 0; Dmin * Dmax > 0 && fabs(Dmax) > 1e-4 && fabs(Dmin) > 1e-4; it++) {
-            if (Dmax < 0) { hi *= 5; Dmax = g(hi); } else { lo -= .1; Dmin = g(lo); }
-            if (it > 1000000) { bad = true; break; }
-        }
-        if (fabs(g(lo)) < 1e-8) D2out = lo;
-        else if (fabs(g(hi)) < 1e-8) D2out = hi;
-        else if (brent_root(g, lo, hi, D2out)) bad = true;
-        Dgrid[nE] = D2out;
-        if (d.bad) bad = true;
-    }
+    for (int nE = 0; nE < ngrid; nE++)
+        Dgrid[nE] = delta_energy(P, base, nE, ngrid, Egrid[nE], fits[0], bad, kDeltaWalkCapHost);
     return bad ? FJ_ERR_ARG : FJ_OK;
+}
+
+// The focal-distance tables of n models on the GPU (fj_delta.cu): views of
+// the models' device potentials and the device tables to fill, uploaded to
+// the context; fixed addresses, so a launch can be captured in a graph.
+namespace {
+struct DeltaDev {
+    const PotView *views;
+    double *const *Eg;
+    double *const *Dg;
+    int *bad;
+    int n;
+};
+
+int delta_prepare(fj_ctx *ctx, int n, const PotView *views, double *const *Eg, double *const *Dg, DeltaDev &dd)
+{
+    const size_t bytes = n * (sizeof(PotView) + 2 * sizeof(double *) + sizeof(int));
+    int rc = ensure(ctx, ctx->delta_ws, bytes);
+    if (rc) return rc;
+    std::vector<char> h(bytes);
+    char *p = h.data();
+    memcpy(p, views, n * sizeof(PotView));
+    memcpy(p + n * sizeof(PotView), Eg, n * sizeof(double *));
+    memcpy(p + n * (sizeof(PotView) + sizeof(double *)), Dg, n * sizeof(double *));
+    memset(p + n * (sizeof(PotView) + 2 * sizeof(double *)), 0, n * sizeof(int));
+    char *d = (char *)ctx->delta_ws.p;
+    FJ_CUDA(cudaMemcpyAsync(d, h.data(), bytes, cudaMemcpyHostToDevice, ctx->stream));
+    FJ_CUDA(cudaStreamSynchronize(ctx->stream));  // h is pageable and goes out of scope
+    dd.views = (const PotView *)d;
+    dd.Eg = (double *const *)(d + n * sizeof(PotView));
+    dd.Dg = (double *const *)(d + n * (sizeof(PotView) + sizeof(double *)));
+    dd.bad = (int *)(d + n * (sizeof(PotView) + 2 * sizeof(double *)));
+    dd.n = n;
+    return FJ_OK;
+}
+
+// n status flags back to the host: 0, or FJ_ERR_ARG where a search hit its cap
+int delta_status(fj_ctx *ctx, const DeltaDev &dd, int *status)
+{
+    std::vector<int> h(dd.n);
+    FJ_CUDA(cudaMemcpyAsync(h.data(), dd.bad, dd.n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    FJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    int any = 0;
+    for (int m = 0; m < dd.n; m++) {
+        if (status) status[m] = h[m] ? FJ_ERR_ARG : FJ_OK;
+        any |= h[m];
+    }
+    return any;
+}
+}  // namespace
+
+extern "C" int fj_tabulate_delta_batch(fj_ctx *ctx, int n, const fj_potential *pots, int ngrid, double *Egrid,
+                                       double *Dgrid, int *status)
+{
+    if (!ctx) return FJ_ERR_ARG;
+    if (n < 1 || !pots || ngrid < 2 || !Egrid || !Dgrid) return fail(ctx, FJ_ERR_ARG, "tabulate_delta_batch: arguments");
+    std::vector<PotView> views(n);
+    std::vector<double *> eg(n), dg(n);
+    for (int m = 0; m < n; m++) {
+        int rc = check_pot(ctx, &pots[m]);
+        if (rc) return rc;
+        if (pots[m].nr < 11) return fail(ctx, FJ_ERR_ARG, "tabulate_delta_batch: nr < 11");
+        views[m] = view(&pots[m]);
+        eg[m] = Egrid + (size_t)m * ngrid;
+        dg[m] = Dgrid + (size_t)m * ngrid;
+    }
+    DeltaDev dd;
+    int rc = delta_prepare(ctx, n, views.data(), eg.data(), dg.data(), dd);
+    if (rc) return rc;
+    FJ_CUDA(launch_tabulate_delta(dd.views, dd.Eg, dd.Dg, n, ngrid, dd.bad, ctx->stream));
+    delta_status(ctx, dd, status);
+    return FJ_OK;
 }
 
 // ------------------------------------------------------ coefficient file
@@ -1003,6 +832,7 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
     const bool ref_order = two && cfg->twocomp_order == FJ_TWOCOMP_REFERENCE;
     auto t0 = std::chrono::steady_clock::now();
     int rc;
+    if (cfg->delta_every < 0) return fail(ctx, FJ_ERR_ARG, "run_model: delta_every must be >= 0");
     const bool resume = cfg->phil_in || cfg->Pr_in || cfg->Pr2_in;
     if (resume && !(cfg->phil_in && cfg->Pr_in && cfg->Pr2_in))
         return fail(ctx, FJ_ERR_ARG, "run_model: a restart needs phil_in, Pr_in and Pr2_in");
@@ -1045,17 +875,37 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
         FJ_CUDA(launch_sum3(nt, potC, potC + nt, potC + 2 * nt, potD, potD + nt, potD + 2 * nt, potA, potA + nt,
                             potA + 2 * nt, s));
     }
-    // focal-distance table from the guess (or restart) potential (fJmodels.cpp:63, 127)
+    // focal-distance table from the guess (or restart) potential (fJmodels.cpp:63, 127);
+    // again from the new potential after every delta_every-th iteration if asked
     std::vector<double> hp(3 * nt);
     FJ_CUDA(cudaMemcpyAsync(hp.data(), potA, 3 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
     FJ_CUDA(cudaStreamSynchronize(s));
-    fj_potential hpot{nr, npl, res->ar, hp.data(), hp.data() + nt, hp.data() + 2 * nt};
+    auto tabulate = [&](const double *dpot) -> int {  // dpot: device tables [3][nt]
+        if (cfg->delta_gpu) {
+            const fj_potential dp{nr, npl, d_ar, dpot, dpot + nt, dpot + 2 * nt};
+            int r2 = fj_tabulate_delta_batch(ctx, 1, &dp, ngrid, d_Eg, d_Dg, nullptr);
+            if (r2) return r2;
+            FJ_CUDA(cudaMemcpyAsync(res->Egrid, d_Eg, ngrid * sizeof(double), cudaMemcpyDeviceToHost, s));
+            FJ_CUDA(cudaMemcpyAsync(res->Dgrid, d_Dg, ngrid * sizeof(double), cudaMemcpyDeviceToHost, s));
+            FJ_CUDA(cudaStreamSynchronize(s));
+            return FJ_OK;
+        }
+        std::vector<double> tp(3 * nt);
+        FJ_CUDA(cudaMemcpyAsync(tp.data(), dpot, 3 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+        FJ_CUDA(cudaStreamSynchronize(s));
+        const fj_potential hpot{nr, npl, res->ar, tp.data(), tp.data() + nt, tp.data() + 2 * nt};
+        fj_tabulate_delta(&hpot, ngrid, res->Egrid, res->Dgrid);
+        FJ_CUDA(cudaMemcpyAsync(d_Eg, res->Egrid, ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+        FJ_CUDA(cudaMemcpyAsync(d_Dg, res->Dgrid, ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+        FJ_CUDA(cudaStreamSynchronize(s));
+        return FJ_OK;
+    };
     if (cfg->Egrid_in && cfg->Dgrid_in) {
         memcpy(res->Egrid, cfg->Egrid_in, ngrid * sizeof(double));
         memcpy(res->Dgrid, cfg->Dgrid_in, ngrid * sizeof(double));
-    } else fj_tabulate_delta(&hpot, ngrid, res->Egrid, res->Dgrid);
-    FJ_CUDA(cudaMemcpyAsync(d_Eg, res->Egrid, ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
-    FJ_CUDA(cudaMemcpyAsync(d_Dg, res->Dgrid, ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+        FJ_CUDA(cudaMemcpyAsync(d_Eg, res->Egrid, ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+        FJ_CUDA(cudaMemcpyAsync(d_Dg, res->Dgrid, ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+    } else if ((rc = tabulate(potA))) return rc;
     fj_delta_table dt{ngrid, d_Eg, d_Dg};
     double *cur = potA, *nxt = potB;
     std::vector<double> old(nt), neu(nt);
@@ -1114,6 +964,9 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
         old.swap(neu);
         std::swap(cur, nxt);
         if (cfg->tol > 0 && maxd < cfg->tol) { k++; break; }
+        if (cfg->delta_every > 0 && (k + 1) % cfg->delta_every == 0 && k + 1 < cfg->itermax &&
+            (rc = tabulate(cur)))
+            return rc;
     }
     res->iterations = k;
     const fj_potential pot{nr, npl, d_ar, cur, cur + nt, cur + 2 * nt};
@@ -1149,6 +1002,9 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
             return fail(ctx, FJ_ERR_ARG, "run_model_batch: bad sizes (one-component models only)");
         if (c.ar_in || c.phil_in || c.Pr_in || c.Pr2_in)
             return fail(ctx, FJ_ERR_ARG, "run_model_batch: restart tables are a fj_run_model option");
+        if (c.delta_every != cfgs[0].delta_every || c.delta_every < 0 || c.delta_every > 1 ||
+            (c.delta_every && !c.delta_gpu))
+            return fail(ctx, FJ_ERR_ARG, "run_model_batch: delta_every is 0 or 1 (with delta_gpu) for all models");
         if (c.rule.nq != rule.nq || c.rule.precision != rule.precision || c.rule.jquad != rule.jquad ||
             memcmp(c.rule.xq, rule.xq, rule.nq * sizeof(double)) || memcmp(c.rule.wq, rule.wq, rule.nq * sizeof(double)))
             return fail(ctx, FJ_ERR_ARG, "run_model_batch: all models must share one velocity rule");
@@ -1175,6 +1031,7 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
     guard.h = hmono;
     struct Dev { double *ar, *rhl, *cur, *nxt, *Eg, *Dg, *grids, *coef, *mono; };
     std::vector<Dev> d(n);
+    std::vector<int> gpu_delta;  // models whose focal-distance table is tabulated on the GPU
     cudaStream_t s = ctx->stream;
     int rc;
     size_t monooff = 0;
@@ -1203,9 +1060,13 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
         if (c.Egrid_in && c.Dgrid_in) {
             memcpy(res[m].Egrid, c.Egrid_in, c.ngrid * sizeof(double));
             memcpy(res[m].Dgrid, c.Dgrid_in, c.ngrid * sizeof(double));
+        } else if (c.delta_gpu) {
+            gpu_delta.push_back(m);  // all together on the GPU below
         } else fj_tabulate_delta(&hpot, c.ngrid, res[m].Egrid, res[m].Dgrid);
-        FJ_CUDA(cudaMemcpyAsync(d[m].Eg, res[m].Egrid, c.ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
-        FJ_CUDA(cudaMemcpyAsync(d[m].Dg, res[m].Dgrid, c.ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+        if (!c.delta_gpu || (c.Egrid_in && c.Dgrid_in)) {
+            FJ_CUDA(cudaMemcpyAsync(d[m].Eg, res[m].Egrid, c.ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+            FJ_CUDA(cudaMemcpyAsync(d[m].Dg, res[m].Dgrid, c.ngrid * sizeof(double), cudaMemcpyHostToDevice, s));
+        }
         res[m].bound = res[m].failures = 0;
         res[m].kernel_ms = 0;
         res[m].last_change = -1;
@@ -1217,6 +1078,36 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
         items[m] = fj_batch_item{fj_potential{c.nr, c.npoly, d[m].ar, d[m].cur, d[m].cur + nt, d[m].cur + 2 * nt},
                                  fj_delta_table{c.ngrid, d[m].Eg, d[m].Dg}, c.df, c.ngauss, d[m].grids};
     }
+    // GPU focal-distance tables in one launch: the models that asked for them now,
+    // and with delta_every = 1 every model again before each later iteration (from
+    // cur, which the iteration refreshes in place, so the launch replays in a graph)
+    const bool retab = cfgs[0].delta_every == 1;
+    std::vector<int> tab_models = gpu_delta;
+    if (retab) {
+        tab_models.resize(n);
+        for (int m = 0; m < n; m++) tab_models[m] = m;
+    }
+    DeltaDev dd{nullptr, nullptr, nullptr, nullptr, 0};
+    const int ngrid0 = tab_models.empty() ? 0 : cfgs[tab_models[0]].ngrid;
+    auto prepare = [&](const std::vector<int> &ms, DeltaDev &out) -> int {
+        std::vector<PotView> views;
+        std::vector<double *> eg, dg;
+        for (int m : ms) {
+            if (cfgs[m].ngrid != ngrid0)
+                return fail(ctx, FJ_ERR_ARG, "run_model_batch: GPU focal-distance tables need one ngrid");
+            const size_t nt = nts[m];
+            views.push_back(PotView{cfgs[m].nr, cfgs[m].npoly, d[m].ar, d[m].cur, d[m].cur + nt, d[m].cur + 2 * nt});
+            eg.push_back(d[m].Eg);
+            dg.push_back(d[m].Dg);
+        }
+        return delta_prepare(ctx, (int)ms.size(), views.data(), eg.data(), dg.data(), out);
+    };
+    if (!gpu_delta.empty()) {  // first tables of the models that asked (the others have theirs)
+        DeltaDev d0;
+        if ((rc = prepare(gpu_delta, d0))) return rc;
+        FJ_CUDA(launch_tabulate_delta(d0.views, d0.Eg, d0.Dg, d0.n, ngrid0, d0.bad, s));
+    }
+    if (retab && (rc = prepare(tab_models, dd))) return rc;  // stream-ordered after the launch above
     FJ_CUDA(cudaStreamSynchronize(s));
     const double setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     std::vector<double> old(ntsum);
@@ -1224,7 +1115,8 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
     // one iteration of every model: batched phase-space launch, then each model's
     // projection and Poisson solve into nxt, nxt copied to cur (fixed addresses, so
     // the sequence can be replayed as a graph) and its multipoles to the host
-    auto iteration = [&](fj_moment_stats *st) -> int {
+    auto iteration = [&](fj_moment_stats *st, bool tab) -> int {
+        if (tab) FJ_CUDA(launch_tabulate_delta(dd.views, dd.Eg, dd.Dg, dd.n, ngrid0, dd.bad, s));
         int r2 = fj_moments_batch(ctx, n, items.data(), &rule, st);
         if (r2) return r2;
         for (int m = 0; m < n; m++) {
@@ -1270,14 +1162,14 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
             FJ_CUDA(cudaStreamSynchronize(s));
         } else {
             fj_moment_stats st;
-            if ((rc = iteration(&st))) return rc;
+            if ((rc = iteration(&st, retab && k > 0))) return rc;
             FJ_CUDA(cudaStreamSynchronize(s));
             kernel_ms += st.kernel_ms;
             bound += st.bound;
             failures += st.failures;
             if (use_graph && k + 1 < itermax) {  // capture the sequence once it has run eagerly
                 FJ_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-                rc = iteration(nullptr);
+                rc = iteration(nullptr, retab);
                 cudaGraph_t g = nullptr;
                 const cudaError_t ce = cudaStreamEndCapture(s, &g);
                 if (rc) { if (g) cudaGraphDestroy(g); return rc; }
@@ -1300,6 +1192,10 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
         if (res[m].grids6)
             FJ_CUDA(cudaMemcpyAsync(res[m].grids6, d[m].grids, 6 * (size_t)c.nr * c.ngauss * sizeof(double),
                                     cudaMemcpyDeviceToHost, s));
+    }
+    for (int m : tab_models) {  // the GPU tables of the last iteration
+        FJ_CUDA(cudaMemcpyAsync(res[m].Egrid, d[m].Eg, cfgs[m].ngrid * sizeof(double), cudaMemcpyDeviceToHost, s));
+        FJ_CUDA(cudaMemcpyAsync(res[m].Dgrid, d[m].Dg, cfgs[m].ngrid * sizeof(double), cudaMemcpyDeviceToHost, s));
     }
     FJ_CUDA(cudaStreamSynchronize(s));
     const double wall = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
@@ -1325,8 +1221,9 @@ extern "C" int fj_run_model_surrogate(fj_ctx *ctx, const fj_model_config *cfg, c
         cfg->rule.precision != FJ_PREC_MIXED || cfg->df.kind != FJ_DF_DPL || sch->exact_first < 1 ||
         sch->exact_last < 0 || sch->audit_stride < 1 || sch->samples < 1 || sch->epochs_first < 1 || sch->epochs < 1)
         return fail(ctx, FJ_ERR_ARG, "run_model_surrogate: needs one DPL component, the mixed rule and a valid schedule");
-    if (cfg->ar_in || cfg->phil_in || cfg->Pr_in || cfg->Pr2_in)
-        return fail(ctx, FJ_ERR_ARG, "run_model_surrogate: restart tables are a fj_run_model option");
+    if (cfg->ar_in || cfg->phil_in || cfg->Pr_in || cfg->Pr2_in || cfg->delta_gpu || cfg->delta_every)
+        return fail(ctx, FJ_ERR_ARG, "run_model_surrogate: restart tables and GPU or repeated Delta tables are "
+                                     "fj_run_model options");
     fj_surrogate_report rp{};
     auto now = [] { return std::chrono::steady_clock::now(); };
     auto ms_since = [](std::chrono::steady_clock::time_point t) {

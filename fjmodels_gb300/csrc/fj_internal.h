@@ -53,6 +53,14 @@ struct LosArgs {
     double x01[kLos01], w01[kLos01];
 };
 cudaError_t launch_los(const LosArgs &a, cudaStream_t s);
+size_t los_local_bytes();
+
+// Focal-distance tables of n models (fj_delta.cu): one thread per (model,
+// energy); pots, Eg, Dg device arrays [n] (tables [ngrid] each), bad device [n]
+// (set to 1 where a bracket or root search hit its cap)
+cudaError_t launch_tabulate_delta(const PotView *pots, double *const *Eg, double *const *Dg, int n, int ngrid,
+                                  int *bad, cudaStream_t s);
+size_t delta_local_bytes();
 
 // Several models' phase-space launches in one grid: model m owns blocks
 // [block_start[m], block_start[m+1]) and grid points [point_start[m],

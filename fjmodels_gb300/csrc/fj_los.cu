@@ -156,6 +156,12 @@ size_t los_smem_bytes(const MomentArgs &m)
     return (m.P.nr + 4 * nt + 2 * m.ngrid + 2 * m.nq + 2 * m.gl.n + kLosBlock / 32) * sizeof(double);
 }
 
+size_t los_local_bytes()
+{
+    cudaFuncAttributes at;
+    return cudaFuncGetAttributes(&at, k_los) == cudaSuccess ? at.localSizeBytes : 0;
+}
+
 cudaError_t launch_los(const LosArgs &a, cudaStream_t s)
 {
     const size_t smem = los_smem_bytes(a.m);

@@ -320,6 +320,15 @@ int fj_guess_rhl(int nr, int ngauss, int npoly, const double *ar, int kind, doub
 /* Focal-distance table tabulateDelta (delta/tabulate.cpp:13-38, delta/Delta.cpp),
    evaluated on the host from HOST potential tables.  Egrid/Dgrid host [ngrid]. */
 int fj_tabulate_delta(const fj_potential *pot_host, int ngrid, double *Egrid, double *Dgrid);
+/* The same tables of n models on the GPU, one thread per (model, energy)
+   running the host's code (no reference counterpart: the reference tabulates
+   one model).  pots host [n] of DEVICE potential tables (nr >= 11); Egrid,
+   Dgrid device [n][ngrid]; status host [n] (may be NULL): FJ_OK, or
+   FJ_ERR_ARG where a bracket or root search hit its cap (the host call's
+   return value).  The tables agree with the host's to the rounding of the
+   device's transcendental functions (root tolerance 1e-8). */
+int fj_tabulate_delta_batch(fj_ctx *ctx, int n, const fj_potential *pots, int ngrid, double *Egrid, double *Dgrid,
+                            int *status);
 
 /* Coefficient file writer _writeOut (io/writeOut.cpp:74-138): byte-identical
    output for identical arrays.  mats9 host [9][nr*npoly] in the file order
@@ -365,6 +374,11 @@ typedef struct fj_model_config {
     const double *phil_in;       /* total potential tables [nr*npoly] to iterate from; */
     const double *Pr_in;         /* the focal-distance table is tabulated from them unless */
     const double *Pr2_in;        /* Egrid_in/Dgrid_in are given                           */
+    /* focal-distance table (no reference counterpart: the reference tabulates
+       once, on the host, from the guess potential) */
+    int delta_gpu;               /* 1: tabulate on the GPU (fj_tabulate_delta_batch) */
+    int delta_every;             /* k > 0: re-tabulate from the new potential after every k-th
+                                    iteration (fj_run_model_batch: 0 or 1, with delta_gpu) */
 } fj_model_config;
 
 /* Two-component iteration order.  SUMMED: both components' moments in the

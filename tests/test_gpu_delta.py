@@ -1,0 +1,98 @@
+"""The focal-distance table on the GPU (fj_tabulate_delta_batch: the host's
+tabulateDelta code, delta/tabulate.cpp:13-38 and delta/Delta.cpp, one thread per
+(model, energy)).  Against the host table: energies to 1e-12, squared focal distances
+to 1e-7 relative (the device's transcendental functions round differently from the
+host's; the roots are searched to 1e-8).  Against the reference's own table of the
+golden fixtures, as the host table is.  In the model loops: a GPU table gives the same
+bits in fj_run_model and fj_run_model_batch (graph or not), and re-tabulating after
+every iteration uses the table of the potential the previous iteration produced."""
+import time
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import fjmodels_gb300 as F  # noqa: E402
+from fjmodels_gb300 import _abi as A  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+from tests.conftest import load_golden  # noqa: E402
+from tests.helpers import rel  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(a):
+    return torch.tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda")
+
+
+def _models(n, seed):
+    """C4-like models: type, grid and sizes drawn from a seeded generator."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        model = ["Hernquist", "Isochrone", "NFW"][rng.integers(3)]
+        nr, npl = int(rng.choice([32, 48, 64])), 5
+        ar = F.log_grid(1e-2, 100.0 if model != "NFW" else 300.0, nr)
+        rhl = F.guess_rhl(ar, 16, npl, model)
+        out.append((ar, *O.compute_phil(ar, rhl)))
+    return out
+
+
+def test_gpu_table_matches_host_table(ctx):
+    tabs = _models(24, 5)
+    pots = [ctx.potential(*[dev(t) for t in tb]) for tb in tabs]
+    t0 = time.perf_counter()
+    E, D, status = ctx.tabulate_delta_batch(pots, 30)
+    torch.cuda.synchronize()
+    t_gpu = time.perf_counter() - t0
+    E, D = E.cpu().numpy(), D.cpu().numpy()
+    t0 = time.perf_counter()
+    host = [F.tabulate_delta(*tb) for tb in tabs]
+    t_host = time.perf_counter() - t0
+    print(f"24 models: GPU {t_gpu * 1e3:.0f} ms, host {t_host * 1e3:.0f} ms")
+    for m, (Eh, Dh, rc) in enumerate(host):
+        assert status[m] == rc, m
+        assert rel(E[m], Eh) < 1e-12, m
+        assert np.max(np.abs(D[m] - Dh) / np.abs(Dh)) < 1e-7, (m, np.max(np.abs(D[m] - Dh) / np.abs(Dh)))
+
+
+@pytest.mark.parametrize("name", ["hern_dpl", "nfw_dpl_rot"])
+def test_gpu_table_matches_reference(ctx, name):
+    g, meta, _ = load_golden(name)
+    nr, npl = meta["nr"], meta["np"]
+    pot = ctx.potential(dev(g["ar"]), dev(g["guess_phil"].reshape(nr, npl)), dev(g["guess_Pr"].reshape(nr, npl)),
+                        dev(g["guess_Pr2"].reshape(nr, npl)))
+    E, D, _ = ctx.tabulate_delta_batch([pot], 30)
+    assert rel(E.cpu().numpy()[0], g["Egrid"]) < 1e-12 and rel(D.cpu().numpy()[0], g["Dgrid"]) < 1e-7
+
+
+MODELS = [dict(nr=32, ngauss=12, npoly=4, rmin=1e-2, rmax=100.0, df=F.DFParams("Hernquist")),
+          dict(nr=40, ngauss=16, npoly=5, rmin=1e-2, rmax=300.0, df=F.DFParams("NFW", chi=1.0, k=0.5))]
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_gpu_tables_in_the_model_loops(ctx, use_graph):
+    rule = F.Rule(*F.tanh_sinh_rule(10), precision=A.FJ_PREC_MIXED)
+    for every in (0, 1):
+        outs = ctx.run_model_batch(MODELS, rule, itermax=3, use_graph=use_graph, delta_gpu=True, delta_every=every)
+        for m, ob in zip(MODELS, outs):
+            o1 = ctx.run_model(m["nr"], m["ngauss"], m["npoly"], m["rmin"], m["rmax"], m["df"], rule, itermax=3,
+                               delta_gpu=True, delta_every=every)
+            for key in ("phil", "Pr", "Pr2", "coef6", "Egrid", "Dgrid"):
+                np.testing.assert_array_equal(ob[key], o1[key], err_msg=f"{key} every={every}")
+
+
+def test_retabulated_table_is_the_previous_potentials(ctx):
+    m = MODELS[1]
+    rule = F.Rule(*F.tanh_sinh_rule(10), precision=A.FJ_PREC_MIXED)
+    args = (m["nr"], m["ngauss"], m["npoly"], m["rmin"], m["rmax"], m["df"], rule)
+    one = ctx.run_model(*args, itermax=1, delta_gpu=True)
+    two = ctx.run_model(*args, itermax=2, delta_gpu=True, delta_every=1)
+    pot = ctx.potential(dev(one["ar"]), dev(one["phil"]), dev(one["Pr"]), dev(one["Pr2"]))
+    E, D, _ = ctx.tabulate_delta_batch([pot], 30)
+    np.testing.assert_array_equal(two["Egrid"], E.cpu().numpy()[0])
+    np.testing.assert_array_equal(two["Dgrid"], D.cpu().numpy()[0])
+    assert not np.array_equal(two["Dgrid"], one["Dgrid"])
+    with pytest.raises(F.FJError):
+        ctx.run_model_batch(MODELS, rule, itermax=2, delta_gpu=False, delta_every=1)
