@@ -12,7 +12,7 @@ FJ_DF_DPL, FJ_DF_QUASIISO = 0, 1
 FJ_PREC_FP64, FJ_PREC_MIXED = 0, 1
 FJ_TWOCOMP_SUMMED, FJ_TWOCOMP_REFERENCE = 0, 1
 FJ_JQUAD_QAGS = 0
-FJ_GUESS = {"Hernquist": 0, "Isochrone": 1, "NFW": 2}
+FJ_GUESS = {"Hernquist": 0, "Isochrone": 1, "NFW": 2, "NFWext": 3}
 
 
 class fj_potential(C.Structure):
@@ -63,7 +63,7 @@ class fj_model_config(C.Structure):
                 ("Egrid_in", DP), ("Dgrid_in", DP), ("ncomp", C.c_int), ("guess2", C.c_int),
                 ("mass2", C.c_double), ("r0_2", C.c_double), ("q2", C.c_double), ("df2", fj_df_params),
                 ("twocomp_order", C.c_int), ("ar_in", DP), ("phil_in", DP), ("Pr_in", DP), ("Pr2_in", DP),
-                ("delta_gpu", C.c_int), ("delta_every", C.c_int)]
+                ("delta_gpu", C.c_int), ("delta_every", C.c_int), ("ext_phil", DP), ("ext_Pr", DP), ("ext_Pr2", DP)]
 
 
 class fj_model_result(C.Structure):

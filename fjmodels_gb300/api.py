@@ -376,19 +376,26 @@ class Context:
     # ---------------------------------------------------------------- whole model
     def run_model(self, nr, ngauss, npoly, rmin, rmax, df, rule, itermax, tol=0.0, ngrid=30, q=1.0,
                   keep_grids=False, delta_table=None, df2=None, q2=1.0, twocomp_order=A.FJ_TWOCOMP_SUMMED,
-                  restart=None, delta_gpu=False, delta_every=0):
+                  restart=None, delta_gpu=False, delta_every=0, ext=None):
         """Self-consistent model (oneComp, fJmodels.cpp:86-144; with df2, the two-component
         loop of fJmodels.cpp:38-84 in `twocomp_order`) with host buffers.
         delta_table = (Egrid, Dgrid) uses a given focal-distance table instead of tabulating one;
         restart = a dict with ar, phil, Pr, Pr2 (readOut, or an earlier result) iterates on from
         those tables instead of the guess density (rmin, rmax are then unused).
         delta_gpu tabulates the focal-distance table on the GPU; delta_every = k > 0 tabulates it
-        again from the new potential after every k-th iteration (the reference: once)."""
+        again from the new potential after every k-th iteration (the reference: once).
+        ext = (phil, Pr, Pr2) of a fixed external potential added after the guess and after every
+        iteration (the reference's external mode, fJmodels.cpp:120-125, 134)."""
         self.use_own_stream()
         din = [None, None] if delta_table is None else [_f64(delta_table[0]), _f64(delta_table[1])]
         cfg = A.fj_model_config(nr, ngauss, npoly, ngrid, rmin, rmax, A.FJ_GUESS.get(df.model, 0), df.mass, df.r0,
                                 q, df.c, rule.c, itermax, tol, *[_dp(d) if d is not None else None for d in din])
         cfg.delta_gpu, cfg.delta_every = int(delta_gpu), int(delta_every)
+        if ext is not None:
+            ex = [_f64(t) for t in ext]
+            if any(t.size != nr * npoly for t in ex):
+                raise FJError("run_model: external potential tables do not match nr, npoly")
+            cfg.ext_phil, cfg.ext_Pr, cfg.ext_Pr2 = (_dp(t) for t in ex)
         if restart is not None:
             rs = {k: _f64(restart[k]) for k in ("ar", "phil", "Pr", "Pr2")}
             if rs["ar"].size != nr or any(rs[k].size != nr * npoly for k in ("phil", "Pr", "Pr2")):

@@ -644,7 +644,7 @@ int fj_gauleg(double x1, double x2, int n, double *x, double *w)
 int fj_guess_rhl(int nr, int ngauss, int npoly, const double *ar, int kind, double mass, double r0, double q,
                  double *rhl)
 {
-    if (nr < 1 || ngauss < 1 || npoly < 1 || npoly > kMaxPoly || !ar || !rhl || kind < 0 || kind > 2)
+    if (nr < 1 || ngauss < 1 || npoly < 1 || npoly > kMaxPoly || !ar || !rhl || kind < 0 || kind > 3)
         return FJ_ERR_ARG;
     const double q2 = q * q;
     auto rho = [&](double R, double z) {  // pot/models.cpp:40-56
@@ -654,6 +654,7 @@ int fj_guess_rhl(int nr, int ngauss, int npoly, const double *ar, int kind, doub
             return mass / kFPI / (q * pow((a + r0) * a, 2) * a) * r0 * (r0 + 2 * a);
         }
         if (kind == FJ_GUESS_NFW) return mass / (m / r0 * pow(r0 + m, 2)) / kFPI;
+        if (kind == FJ_GUESS_NFWEXT) return mass / (m / r0 * pow(r0 + m, 1)) / kFPI;
         return mass / (m / r0 * pow(r0 + m, 3)) / kTPI;
     };
     std::vector<double> ci(ngauss), wi(ngauss), si(ngauss), pol(npoly);
@@ -833,6 +834,9 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
     auto t0 = std::chrono::steady_clock::now();
     int rc;
     if (cfg->delta_every < 0) return fail(ctx, FJ_ERR_ARG, "run_model: delta_every must be >= 0");
+    const bool ext = cfg->ext_phil || cfg->ext_Pr || cfg->ext_Pr2;
+    if (ext && !(cfg->ext_phil && cfg->ext_Pr && cfg->ext_Pr2))
+        return fail(ctx, FJ_ERR_ARG, "run_model: an external potential needs ext_phil, ext_Pr and ext_Pr2");
     const bool resume = cfg->phil_in || cfg->Pr_in || cfg->Pr2_in;
     if (resume && !(cfg->phil_in && cfg->Pr_in && cfg->Pr2_in))
         return fail(ctx, FJ_ERR_ARG, "run_model: a restart needs phil_in, Pr_in and Pr2_in");
@@ -851,18 +855,26 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
             return fail(ctx, rc, "run_model: guess of component 2");
     }
     // device layout: ar | rhl (2) | pot A, B (total, 3 tables each) | pot C, D (components) | Eg | Dg |
-    // grids6 (2) | coef6 (2)
-    const size_t nd = nr + 2 * (size_t)nt + 12 * (size_t)nt + 2 * ngrid + 12 * (size_t)nr * ng + 12 * (size_t)nt;
+    // grids6 (2) | coef6 (2) | external potential (3)
+    const size_t nd =
+        nr + 2 * (size_t)nt + 12 * (size_t)nt + 2 * ngrid + 12 * (size_t)nr * ng + 12 * (size_t)nt + 3 * (size_t)nt;
     double *dbuf = nullptr;
     FJ_CUDA(cudaMalloc(&dbuf, nd * sizeof(double)));
     struct Free { double *p; ~Free() { cudaFree(p); } } guard{dbuf};
     double *d_ar = dbuf, *d_rhl = d_ar + nr, *potA = d_rhl + 2 * nt, *potB = potA + 3 * nt, *potC = potB + 3 * nt,
            *potD = potC + 3 * nt, *d_Eg = potD + 3 * nt, *d_Dg = d_Eg + ngrid, *d_grids = d_Dg + ngrid,
            *d_grids2 = d_grids + 6 * (size_t)nr * ng, *d_coef = d_grids2 + 6 * (size_t)nr * ng,
-           *d_coef2 = d_coef + 6 * (size_t)nt;
+           *d_coef2 = d_coef + 6 * (size_t)nt, *potE = d_coef2 + 6 * (size_t)nt;
     cudaStream_t s = ctx->stream;
     FJ_CUDA(cudaMemcpyAsync(d_ar, res->ar, nr * sizeof(double), cudaMemcpyHostToDevice, s));
     FJ_CUDA(cudaMemcpyAsync(d_rhl, rhl.data(), 2 * nt * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (ext) {
+        FJ_CUDA(cudaMemcpyAsync(potE, cfg->ext_phil, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+        FJ_CUDA(cudaMemcpyAsync(potE + nt, cfg->ext_Pr, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+        FJ_CUDA(cudaMemcpyAsync(potE + 2 * nt, cfg->ext_Pr2, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    // updatePhil with the external potential (potLeg.cpp:21-29): pot += ext, all three tables
+    auto add_ext = [&](double *pot) { return launch_add(3 * nt, pot, potE, pot, s); };
     if (resume) {  // the written total potential (fJmodels.cpp:63 state at the restart iteration)
         FJ_CUDA(cudaMemcpyAsync(potA, cfg->phil_in, nt * sizeof(double), cudaMemcpyHostToDevice, s));
         FJ_CUDA(cudaMemcpyAsync(potA + nt, cfg->Pr_in, nt * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -875,6 +887,7 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
         FJ_CUDA(launch_sum3(nt, potC, potC + nt, potC + 2 * nt, potD, potD + nt, potD + 2 * nt, potA, potA + nt,
                             potA + 2 * nt, s));
     }
+    if (ext && !resume) FJ_CUDA(add_ext(potA));  // fJmodels.cpp:120-125
     // focal-distance table from the guess (or restart) potential (fJmodels.cpp:63, 127);
     // again from the new potential after every delta_every-th iteration if asked
     std::vector<double> hp(3 * nt);
@@ -954,6 +967,7 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
             FJ_CUDA(launch_sum3(nt, potC, potC + nt, potC + 2 * nt, potD, potD + nt, potD + 2 * nt, nxt, nxt + nt,
                                 nxt + 2 * nt, s));
         }
+        if (ext) FJ_CUDA(add_ext(nxt));  // fJmodels.cpp:134
         FJ_CUDA(cudaMemcpyAsync(neu.data(), nxt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
         FJ_CUDA(cudaStreamSynchronize(s));
         double maxd = 0;
@@ -1000,8 +1014,9 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
         if (c.nr < 11 || c.ngauss < 1 || c.npoly < 1 || c.npoly > kMaxPoly || c.ngrid < 2 || c.itermax < 1 ||
             c.ncomp > 1)
             return fail(ctx, FJ_ERR_ARG, "run_model_batch: bad sizes (one-component models only)");
-        if (c.ar_in || c.phil_in || c.Pr_in || c.Pr2_in)
-            return fail(ctx, FJ_ERR_ARG, "run_model_batch: restart tables are a fj_run_model option");
+        if (c.ar_in || c.phil_in || c.Pr_in || c.Pr2_in || c.ext_phil || c.ext_Pr || c.ext_Pr2)
+            return fail(ctx, FJ_ERR_ARG, "run_model_batch: restart tables and external potentials are fj_run_model "
+                                         "options");
         if (c.delta_every != cfgs[0].delta_every || c.delta_every < 0 || c.delta_every > 1 ||
             (c.delta_every && !c.delta_gpu))
             return fail(ctx, FJ_ERR_ARG, "run_model_batch: delta_every is 0 or 1 (with delta_gpu) for all models");
@@ -1221,7 +1236,8 @@ extern "C" int fj_run_model_surrogate(fj_ctx *ctx, const fj_model_config *cfg, c
         cfg->rule.precision != FJ_PREC_MIXED || cfg->df.kind != FJ_DF_DPL || sch->exact_first < 1 ||
         sch->exact_last < 0 || sch->audit_stride < 1 || sch->samples < 1 || sch->epochs_first < 1 || sch->epochs < 1)
         return fail(ctx, FJ_ERR_ARG, "run_model_surrogate: needs one DPL component, the mixed rule and a valid schedule");
-    if (cfg->ar_in || cfg->phil_in || cfg->Pr_in || cfg->Pr2_in || cfg->delta_gpu || cfg->delta_every)
+    if (cfg->ar_in || cfg->phil_in || cfg->Pr_in || cfg->Pr2_in || cfg->delta_gpu || cfg->delta_every ||
+        cfg->ext_phil || cfg->ext_Pr || cfg->ext_Pr2)
         return fail(ctx, FJ_ERR_ARG, "run_model_surrogate: restart tables and GPU or repeated Delta tables are "
                                      "fj_run_model options");
     fj_surrogate_report rp{};

@@ -1,9 +1,17 @@
 // fj_delta.cu -- the focal-distance tables of many models at once: one thread
 // per (model, energy) runs delta_energy (fj_delta.cuh), the same code as the
-// host's fj_tabulate_delta.  Each thread integrates its orbits alone (FP64,
-// serial Bulirsch-Stoer steps), so the kernel is latency-bound and pays off
-// with many models (or a table per iteration), not for one.  Built without
-// FMA contraction, like the host restatement it shares its arithmetic with.
+// host's fj_tabulate_delta.  The energies' searches take very different paths
+// and lengths (bracket walks of one to thousands of steps, adaptive orbit
+// steps), so each thread runs alone in its block -- lanes of one warp would
+// serialise each other's paths -- and the SMs interleave the single-thread
+// blocks.  Built without FMA contraction, like the host code.
+//
+// The fit of the focal distance to an orbit is not a continuous function of
+// rounding: a change of one unit in the last place of the orbit equations
+// moves some entries of the table by tens of per cent (the host code itself,
+// with pow(y, 3) written as y*y*y, does the same).  The device's libm rounds
+// differently from the host's, so the GPU table is another table of the same
+// algorithm, not the host's bits; the energies agree to rounding.
 #include "fj_internal.h"
 #include "fj_delta.cuh"
 
@@ -11,12 +19,10 @@ namespace fj {
 
 namespace {
 
-constexpr int kDeltaBlock = 32;
-
-__global__ void __launch_bounds__(kDeltaBlock) k_tabulate_delta(const PotView *pots, double *const *Eg,
+__global__ void __launch_bounds__(1) k_tabulate_delta(const PotView *pots, double *const *Eg,
                                                                double *const *Dg, int n, int ngrid, int *bad)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x;
     if (t >= n * ngrid) return;
     const int m = t / ngrid, nE = t % ngrid;
     const PotView P = pots[m];
@@ -36,7 +42,7 @@ cudaError_t launch_tabulate_delta(const PotView *pots, double *const *Eg, double
                                   int *bad, cudaStream_t s)
 {
     const int nt = n * ngrid;
-    k_tabulate_delta<<<(nt + kDeltaBlock - 1) / kDeltaBlock, kDeltaBlock, 0, s>>>(pots, Eg, Dg, n, ngrid, bad);
+    k_tabulate_delta<<<nt, 1, 0, s>>>(pots, Eg, Dg, n, ngrid, bad);
     return cudaGetLastError();
 }
 

@@ -49,10 +49,13 @@ extern "C" {
    (include/Utils.h:173-185); n > 0 = fixed n-point Gauss-Legendre */
 #define FJ_JQUAD_QAGS 0
 
-/* guess densities (pot/models.cpp:40-56) */
+/* guess densities (pot/models.cpp:40-56), and the density of the external
+   halo (rhoNFWext, pot/models.cpp:61-65: GM / (m/a (a + m)) / 4 pi, the
+   reference's a = 25, GM = 0.01 passed as r0 and mass) */
 #define FJ_GUESS_HERNQUIST 0
 #define FJ_GUESS_ISOCHRONE 1
 #define FJ_GUESS_NFW 2
+#define FJ_GUESS_NFWEXT 3
 
 typedef struct fj_ctx fj_ctx;
 
@@ -379,6 +382,11 @@ typedef struct fj_model_config {
     int delta_gpu;               /* 1: tabulate on the GPU (fj_tabulate_delta_batch) */
     int delta_every;             /* k > 0: re-tabulate from the new potential after every k-th
                                     iteration (fj_run_model_batch: 0 or 1, with delta_gpu) */
+    /* a fixed external potential added to the model's own (the reference's
+       commented-out external mode, fJmodels.cpp:120-125, 134: updatePhil after
+       the guess and after every iteration); host [nr*npoly] tables, NULL = none.
+       A restart's tables are taken as the total.  fj_run_model only. */
+    const double *ext_phil, *ext_Pr, *ext_Pr2;
 } fj_model_config;
 
 /* Two-component iteration order.  SUMMED: both components' moments in the
