@@ -4,7 +4,8 @@ first run's focal-distance table, which the file does not hold) give the bits of
 of k + m iterations.  From the reference's 6-digit file the restart lands within the
 printed precision (relative 1e-4 per shell; the loop is contracting, so the rounding of
 the restart point does not grow).  Both for one component and for the reference's
-two-component order.  Restart tables of the wrong shape are argument errors."""
+two-component order.  Restart tables of the wrong shape are argument errors.  Also the
+external-potential mode, which adds a fixed potential to every iteration's."""
 import numpy as np
 import pytest
 
@@ -54,3 +55,38 @@ def test_restart_arguments(ctx):
     bad["Pr2"] = np.zeros((NR, NPL))  # right shapes, but ar not increasing
     with pytest.raises(F.FJError):
         ctx.run_model(NR, NG, NPL, 0, 0, df, _rule(), itermax=1, restart=bad)
+
+
+def test_external_potential_mode(ctx):
+    """The reference's external mode (fJmodels.cpp:120-125, 134; the NFW halo of
+    pot/models.cpp:61-65 with a = 25, GM = 0.01): the iterations start from guess + ext and
+    every new potential is the model's own plus ext.  One iteration equals the explicit
+    sequence Poisson(guess) + ext -> focal-distance table -> moments -> projection ->
+    Poisson -> + ext, bit for bit."""
+    rule = _rule()
+    df = F.DFParams("Hernquist")
+    ar = F.log_grid(RMIN, RMAX, NR)
+    f64 = dict(dtype=torch.float64, device="cuda")
+    d_ar = torch.tensor(ar, **f64)
+
+    def poisson(rhl):
+        t = [torch.zeros((NR, NPL), **f64) for _ in range(3)]
+        ctx.computePhil(d_ar, torch.tensor(rhl, **f64), *t)
+        return t
+
+    ext = poisson(F.guess_rhl(ar, NG, NPL, "NFWext", mass=0.01, r0=25.0))
+    ext_h = [t.cpu().numpy() for t in ext]
+    out = ctx.run_model(NR, NG, NPL, RMIN, RMAX, df, rule, itermax=1, ext=ext_h)
+    tot = [a + b for a, b in zip(poisson(F.guess_rhl(ar, NG, NPL, "Hernquist")), ext)]
+    tot_h = [t.cpu().numpy() for t in tot]
+    E, D, _ = F.tabulate_delta(ar, *tot_h)
+    assert np.array_equal(out["Egrid"], E) and np.array_equal(out["Dgrid"], D)
+    pot, delta = ctx.potential(d_ar, *tot), ctx.delta(torch.tensor(E, **f64), torch.tensor(D, **f64))
+    new = [torch.zeros((NR, NPL), **f64) for _ in range(3)]
+    grids, coef = torch.zeros((6, NR, NG), **f64), torch.zeros((6, NR, NPL), **f64)
+    ctx.computeNewPhi(pot, delta, df, rule, NG, grids, coef, *new)
+    torch.cuda.synchronize()
+    for k, a, b in zip(("phil", "Pr", "Pr2"), new, ext):
+        assert np.array_equal(out[k], (a + b).cpu().numpy()), k
+    with pytest.raises(F.FJError):
+        ctx.run_model(NR, NG, NPL, RMIN, RMAX, df, rule, itermax=1, ext=[e[:-1] for e in ext_h])
