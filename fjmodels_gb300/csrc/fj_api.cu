@@ -155,7 +155,8 @@ int poly_table(fj_ctx *ctx, int ngauss, int npoly, const double **dptr)
 
 int gl_rule(fj_ctx *ctx, int n, GLRule *out)
 {
-    if (n <= 0) { *out = GLRule{0, nullptr, nullptr}; return FJ_OK; }
+    memset(out, 0, sizeof *out);
+    if (n <= 0) return FJ_OK;
     auto it = ctx->gl_rules.find(n);
     if (it == ctx->gl_rules.end()) {
         std::vector<double> h(2 * n);
@@ -167,7 +168,9 @@ int gl_rule(fj_ctx *ctx, int n, GLRule *out)
         it = ctx->gl_rules.emplace(n, b).first;
     }
     const double *p = (const double *)it->second.p;
-    *out = GLRule{n, p, p + n};
+    out->n = n;
+    out->x01 = p;
+    out->w01 = p + n;
     return FJ_OK;
 }
 
@@ -187,9 +190,12 @@ int upload_rule(fj_ctx *ctx, const fj_quad_rule *r, const double **xq, const dou
     return FJ_OK;
 }
 
+// Descriptors reach the device as bytes and fj_moments_batch compares them
+// with the last upload (a graph capture must not upload): padding is zeroed.
 DFDev df_dev(const fj_df_params *d)
 {
     DFDev o;
+    memset(&o, 0, sizeof o);
     o.kind = d->kind;
     o.alpha = d->alpha; o.beta = d->beta; o.J0 = d->J0;
     o.norm = d->mass / pow(d->J0, 3);
@@ -214,6 +220,7 @@ int build_args(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta
                const fj_quad_rule *rule, int ngauss, const double *Rz, int npts, double *out6, MomentArgs &a,
                bool &mixed)
 {
+    memset(&a, 0, sizeof a);  // padding too (the batch descriptors are compared as bytes)
     int rc = check_pot(ctx, pot);
     if (rc) return rc;
     if (!delta || delta->ngrid < 2 || !delta->Egrid || !delta->Dgrid) return fail(ctx, FJ_ERR_ARG, "delta table");
