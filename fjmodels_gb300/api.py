@@ -215,7 +215,8 @@ class Context:
     def run_model_batch(self, models, rule, itermax, tol=0.0, ngrid=30, use_graph=True, delta_gpu=False,
                         delta_every=0):
         """Several one-component models iterated together (fj_run_model_batch).  models = list of
-        dicts with nr, ngauss, npoly, rmin, rmax, df (DFParams) and optional q, delta_table.
+        dicts with nr, ngauss, npoly, rmin, rmax, df (DFParams) and optional q, delta_table, and
+        df2 (+ q2) for a second component (summed order, as run_model's FJ_TWOCOMP_SUMMED).
         delta_gpu: focal-distance tables on the GPU, all models in one launch; delta_every = 1
         tabulates them again before every later iteration."""
         self.use_own_stream()
@@ -232,16 +233,26 @@ class Context:
                                         df.r0, m.get("q", 1.0), df.c, rule.c, itermax, tol,
                                         *[_dp(d) if d is not None else None for d in din])
             cfgs[i].delta_gpu, cfgs[i].delta_every = int(delta_gpu), int(delta_every)
+            df2 = m.get("df2")
+            if df2 is not None:
+                c = cfgs[i]
+                c.ncomp, c.guess2, c.mass2, c.r0_2, c.q2 = 2, A.FJ_GUESS.get(df2.model, 0), df2.mass, df2.r0, m.get("q2", 1.0)
+                c.df2, c.twocomp_order = df2.c, A.FJ_TWOCOMP_SUMMED
             out = {"ar": np.zeros(nr), "coef6": np.zeros((6, nr, npl)), "phil": np.zeros((nr, npl)),
                    "Pr": np.zeros((nr, npl)), "Pr2": np.zeros((nr, npl)), "Egrid": np.zeros(ngrid),
                    "Dgrid": np.zeros(ngrid)}
             outs.append(out)
             ress[i] = A.fj_model_result(*[_dp(out[k]) for k in ("ar", "coef6", "phil", "Pr", "Pr2", "Egrid",
                                                                   "Dgrid")], None)
+            if df2 is not None:
+                out["coef6_2"] = np.zeros((6, nr, npl))
+                ress[i].coef6_2 = _dp(out["coef6_2"])
         self._check(self.lib.fj_run_model_batch(self.h, n, cfgs, ress, 1 if use_graph else 0), "fj_run_model_batch")
         for out, r in zip(outs, ress):
             out.update(vir7=np.array(r.vir7[:]), iterations=r.iterations, last_change=r.last_change, bound=r.bound,
                        failures=r.failures, wall_ms=r.wall_ms, kernel_ms=r.kernel_ms, setup_ms=r.setup_ms)
+            if "coef6_2" in out:
+                out["vir7_2"] = np.array(r.vir7_2[:])
         return outs
 
     def tabulate_delta_batch(self, pots, ngrid=30):

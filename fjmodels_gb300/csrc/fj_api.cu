@@ -1019,8 +1019,11 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
         if (!r.ar || !r.coef6 || !r.phil || !r.Pr || !r.Pr2 || !r.Egrid || !r.Dgrid)
             return fail(ctx, FJ_ERR_ARG, "run_model_batch: missing result buffers");
         if (c.nr < 11 || c.ngauss < 1 || c.npoly < 1 || c.npoly > kMaxPoly || c.ngrid < 2 || c.itermax < 1 ||
-            c.ncomp > 1)
-            return fail(ctx, FJ_ERR_ARG, "run_model_batch: bad sizes (one-component models only)");
+            c.ncomp < 0 || c.ncomp > 2)
+            return fail(ctx, FJ_ERR_ARG, "run_model_batch: bad sizes or component count");
+        if (c.ncomp == 2 && c.twocomp_order != FJ_TWOCOMP_SUMMED)
+            return fail(ctx, FJ_ERR_ARG, "run_model_batch: two components in the summed order (the reference's "
+                                         "order is a fj_run_model option)");
         if (c.ar_in || c.phil_in || c.Pr_in || c.Pr2_in || c.ext_phil || c.ext_Pr || c.ext_Pr2)
             return fail(ctx, FJ_ERR_ARG, "run_model_batch: restart tables and external potentials are fj_run_model "
                                          "options");
@@ -1033,13 +1036,14 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
         itermax = c.itermax > itermax ? c.itermax : itermax;
     }
     auto t0 = std::chrono::steady_clock::now();
-    // per-model device block: ar | rhl | cur (3 tables) | nxt (3) | Eg | Dg | grids6 | coef6
+    // per-model device block: ar | rhl | cur (3 tables) | nxt (3) | Eg | Dg | grids6 | coef6, and for a
+    // second component (summed order, fj_run_model's FJ_TWOCOMP_SUMMED): | grids6 | coef6
     std::vector<size_t> off(n + 1, 0), nts(n);
     for (int m = 0; m < n; m++) {
         const fj_model_config &c = cfgs[m];
-        const size_t nt = (size_t)c.nr * c.npoly;
+        const size_t nt = (size_t)c.nr * c.npoly, g6 = 6 * (size_t)c.nr * c.ngauss;
         nts[m] = nt;
-        off[m + 1] = off[m] + c.nr + nt + 6 * nt + 2 * c.ngrid + 6 * (size_t)c.nr * c.ngauss + 6 * nt;
+        off[m + 1] = off[m] + c.nr + nt + 6 * nt + 2 * c.ngrid + g6 + 6 * nt + (c.ncomp == 2 ? g6 + 6 * nt : 0);
     }
     double *dbuf = nullptr, *hmono = nullptr;
     FJ_CUDA(cudaMalloc(&dbuf, off[n] * sizeof(double)));
@@ -1051,7 +1055,7 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
     for (int m = 0; m < n; m++) ntsum += nts[m];
     FJ_CUDA(cudaMallocHost(&hmono, ntsum * sizeof(double)));
     guard.h = hmono;
-    struct Dev { double *ar, *rhl, *cur, *nxt, *Eg, *Dg, *grids, *coef, *mono; };
+    struct Dev { double *ar, *rhl, *cur, *nxt, *Eg, *Dg, *grids, *coef, *mono, *grids2, *coef2; };
     std::vector<Dev> d(n);
     std::vector<int> gpu_delta;  // models whose focal-distance table is tabulated on the GPU
     cudaStream_t s = ctx->stream;
@@ -1061,19 +1065,31 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
         const fj_model_config &c = cfgs[m];
         const size_t nt = nts[m];
         double *b = dbuf + off[m];
+        const size_t g6 = 6 * (size_t)c.nr * c.ngauss;
+        double *coef = b + c.nr + 7 * nt + 2 * c.ngrid + g6;
         d[m] = Dev{b, b + c.nr, b + c.nr + nt, b + c.nr + 4 * nt, b + c.nr + 7 * nt, b + c.nr + 7 * nt + c.ngrid,
-                   b + c.nr + 7 * nt + 2 * c.ngrid, b + c.nr + 7 * nt + 2 * c.ngrid + 6 * (size_t)c.nr * c.ngauss,
-                   hmono + monooff};
+                   b + c.nr + 7 * nt + 2 * c.ngrid, coef, hmono + monooff, nullptr, nullptr};
+        if (c.ncomp == 2) { d[m].grids2 = coef + 6 * nt; d[m].coef2 = d[m].grids2 + g6; }
         monooff += nt;
         if ((rc = fj_log_grid(c.rmin, c.rmax, c.nr, res[m].ar))) return fail(ctx, rc, "run_model_batch: grid");
-        std::vector<double> rhl(nt);
+        std::vector<double> rhl(2 * nt);
         if ((rc = fj_guess_rhl(c.nr, c.ngauss, c.npoly, res[m].ar, c.guess, c.mass, c.r0, c.q, rhl.data())))
             return fail(ctx, rc, "run_model_batch: guess");
+        if (c.ncomp == 2 &&
+            (rc = fj_guess_rhl(c.nr, c.ngauss, c.npoly, res[m].ar, c.guess2, c.mass2, c.r0_2, c.q2, rhl.data() + nt)))
+            return fail(ctx, rc, "run_model_batch: guess of component 2");
         FJ_CUDA(cudaMemcpyAsync(d[m].ar, res[m].ar, c.nr * sizeof(double), cudaMemcpyHostToDevice, s));
         FJ_CUDA(cudaMemcpyAsync(d[m].rhl, rhl.data(), nt * sizeof(double), cudaMemcpyHostToDevice, s));
+        if (c.ncomp == 2)  // component 2's guess multipoles in nxt for its Poisson solve (fJmodels.cpp:49-59)
+            FJ_CUDA(cudaMemcpyAsync(d[m].nxt + 2 * nt, rhl.data() + nt, nt * sizeof(double), cudaMemcpyHostToDevice, s));
         FJ_CUDA(cudaStreamSynchronize(s));
         if ((rc = fj_poisson(ctx, c.nr, c.npoly, d[m].ar, d[m].rhl, d[m].cur, d[m].cur + nt, d[m].cur + 2 * nt)))
             return rc;
+        if (c.ncomp == 2) {  // each component's guess potential, total = their sum
+            double *pD = d[m].coef;  // scratch: 3 tables of component 2 (coef is written by the iterations)
+            if ((rc = fj_poisson(ctx, c.nr, c.npoly, d[m].ar, d[m].nxt + 2 * nt, pD, pD + nt, pD + 2 * nt))) return rc;
+            FJ_CUDA(launch_add(3 * (int)nt, d[m].cur, pD, d[m].cur, s));
+        }
         std::vector<double> hp(3 * nt);
         FJ_CUDA(cudaMemcpyAsync(hp.data(), d[m].cur, 3 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
         FJ_CUDA(cudaStreamSynchronize(s));
@@ -1093,12 +1109,14 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
         res[m].kernel_ms = 0;
         res[m].last_change = -1;
     }
-    std::vector<fj_batch_item> items(n);
+    std::vector<fj_batch_item> items;  // one per component: both components of a model in its total potential
     for (int m = 0; m < n; m++) {
         const fj_model_config &c = cfgs[m];
         const size_t nt = nts[m];
-        items[m] = fj_batch_item{fj_potential{c.nr, c.npoly, d[m].ar, d[m].cur, d[m].cur + nt, d[m].cur + 2 * nt},
-                                 fj_delta_table{c.ngrid, d[m].Eg, d[m].Dg}, c.df, c.ngauss, d[m].grids};
+        const fj_potential pot{c.nr, c.npoly, d[m].ar, d[m].cur, d[m].cur + nt, d[m].cur + 2 * nt};
+        items.push_back(fj_batch_item{pot, fj_delta_table{c.ngrid, d[m].Eg, d[m].Dg}, c.df, c.ngauss, d[m].grids});
+        if (c.ncomp == 2)
+            items.push_back(fj_batch_item{pot, fj_delta_table{c.ngrid, d[m].Eg, d[m].Dg}, c.df2, c.ngauss, d[m].grids2});
     }
     // GPU focal-distance tables in one launch: the models that asked for them now,
     // and with delta_every = 1 every model again before each later iteration (from
@@ -1139,13 +1157,20 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
     // the sequence can be replayed as a graph) and its multipoles to the host
     auto iteration = [&](fj_moment_stats *st, bool tab) -> int {
         if (tab) FJ_CUDA(launch_tabulate_delta(dd.views, dd.Eg, dd.Dg, dd.n, ngrid0, dd.bad, s));
-        int r2 = fj_moments_batch(ctx, n, items.data(), &rule, st);
+        int r2 = fj_moments_batch(ctx, (int)items.size(), items.data(), &rule, st);
         if (r2) return r2;
         for (int m = 0; m < n; m++) {
             const fj_model_config &c = cfgs[m];
             const size_t nt = nts[m];
             if ((r2 = fj_legendre_project(ctx, c.nr, c.ngauss, c.npoly, d[m].ar, d[m].grids, d[m].coef))) return r2;
-            if ((r2 = fj_poisson(ctx, c.nr, c.npoly, d[m].ar, d[m].coef, d[m].nxt, d[m].nxt + nt, d[m].nxt + 2 * nt)))
+            const double *dens = d[m].coef;
+            if (c.ncomp == 2) {  // one solve of the summed density multipoles
+                if ((r2 = fj_legendre_project(ctx, c.nr, c.ngauss, c.npoly, d[m].ar, d[m].grids2, d[m].coef2)))
+                    return r2;
+                FJ_CUDA(launch_add((int)nt, d[m].coef, d[m].coef2, d[m].rhl, s));
+                dens = d[m].rhl;
+            }
+            if ((r2 = fj_poisson(ctx, c.nr, c.npoly, d[m].ar, dens, d[m].nxt, d[m].nxt + nt, d[m].nxt + 2 * nt)))
                 return r2;
             FJ_CUDA(cudaMemcpyAsync(d[m].cur, d[m].nxt, 3 * nt * sizeof(double), cudaMemcpyDeviceToDevice, s));
             FJ_CUDA(cudaMemcpyAsync(d[m].mono, d[m].nxt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1208,6 +1233,11 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
         const fj_potential pot{c.nr, c.npoly, d[m].ar, d[m].cur, d[m].cur + nt, d[m].cur + 2 * nt};
         if ((rc = fj_vir2(ctx, &pot, c.ngauss, d[m].coef, res[m].vir7))) return rc;
         FJ_CUDA(cudaMemcpyAsync(res[m].coef6, d[m].coef, 6 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+        if (c.ncomp == 2) {
+            if ((rc = fj_vir2(ctx, &pot, c.ngauss, d[m].coef2, res[m].vir7_2))) return rc;
+            if (res[m].coef6_2)
+                FJ_CUDA(cudaMemcpyAsync(res[m].coef6_2, d[m].coef2, 6 * nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
         FJ_CUDA(cudaMemcpyAsync(res[m].phil, d[m].cur, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
         FJ_CUDA(cudaMemcpyAsync(res[m].Pr, d[m].cur + nt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
         FJ_CUDA(cudaMemcpyAsync(res[m].Pr2, d[m].cur + 2 * nt, nt * sizeof(double), cudaMemcpyDeviceToHost, s));

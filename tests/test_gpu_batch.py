@@ -91,3 +91,18 @@ def test_batch_arguments(ctx):
                                         r.c, 1, 0.0, None, None)
             ress[i] = A.fj_model_result(*[b_.ctypes.data_as(A.DP) for b_ in b], None)
         ctx._check(ctx.lib.fj_run_model_batch(ctx.h, n, cfgs, ress, 0), "fj_run_model_batch")
+
+
+def test_run_model_batch_mixes_component_counts(ctx):
+    """One- and two-component models (summed order) in one batch: each gives the bits of its
+    own fj_run_model, component 2's coefficients and virial sums included."""
+    rule = F.Rule(*F.tanh_sinh_rule(10), precision=A.FJ_PREC_MIXED)
+    halo = F.DFParams("NFW", dphi_h=0.5, dz_h=0.8, dphi_g=1.0, dz_g=1.2, mass=1.0, r0=10.0)
+    models = [MODELS[0], dict(MODELS[1], df=F.DFParams("Hernquist", mass=0.1, r0=1.0), df2=halo)]
+    for use_graph in (False, True):
+        outs = ctx.run_model_batch(models, rule, itermax=2, use_graph=use_graph)
+        for m, ob in zip(models, outs):
+            kw = dict(df2=m["df2"], twocomp_order=A.FJ_TWOCOMP_SUMMED) if "df2" in m else {}
+            o1 = ctx.run_model(m["nr"], m["ngauss"], m["npoly"], m["rmin"], m["rmax"], m["df"], rule, itermax=2, **kw)
+            for key in ("phil", "Pr", "Pr2", "coef6", "vir7") + (("coef6_2", "vir7_2") if kw else ()):
+                np.testing.assert_array_equal(ob[key], o1[key], err_msg=f"{key} graph={use_graph}")
