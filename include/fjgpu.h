@@ -415,8 +415,10 @@ typedef struct fj_model_result {
 
 int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_result *res);
 
-/* n one-component models iterated together (no reference counterpart): per
-   iteration one fj_moments_batch launch over every model's grid, then each
+/* n models iterated together (no reference counterpart): one- and
+   two-component models (the latter in the summed order, FJ_TWOCOMP_SUMMED:
+   both components' grids in the one launch), per iteration one
+   fj_moments_batch launch over every model's grid, then each
    model's projection and Poisson solve; with use_graph the iteration is
    captured once as a CUDA graph after running eagerly and replayed.  All
    models share cfgs[0].rule; each runs max(itermax) iterations or until every
