@@ -197,12 +197,12 @@ def run_ours(args, rank, world):
     if args.form == "mixed" and args.mixed_config:
         ctx.set_mixed_config(*[int(v) for v in args.mixed_config.split(",")])
         tuned = {"variant": ctx.mixed_config()[0], "nodes_per_block": ctx.mixed_config()[1], "source": "given"}
-    elif args.form == "mixed":  # pick the kernel configuration on every 7th grid point (untimed)
+    elif args.form == "mixed":  # pick the kernel configuration on every 4th grid point (untimed)
         ci, _ = F.gauleg(0, 1, ng)
         allp = np.array([[ar[n] * np.sqrt(1 - c * c), ar[n] * c] for n in range(nr) for c in ci])
-        v, c, ms = ctx.autotune_mixed(ctx.potential(d_ar, *tabs), delta, df, rule, torch.tensor(allp[::7], **f64))
-        tuned = {"variant": v, "nodes_per_block": c, "sample_kernel_ms": ms, "sample_points": len(allp[::7]),
-                 "table_ms": np.round(ctx.autotune_table, 2).tolist()}
+        v, c, ms = ctx.autotune_mixed(ctx.potential(d_ar, *tabs), delta, df, rule, torch.tensor(allp[::4], **f64))
+        tuned = {"variant": v, "nodes_per_block": c, "sample_kernel_ms": ms, "sample_points": len(allp[::4]),
+                 "table_ms": np.round(ctx.autotune_table, 2).tolist(), "table_nodes_per_block": [1024, 2048, 4096]}
     state = {"cur": tabs, "nxt": nxt}
     kernel_ms, changes = [], []
 

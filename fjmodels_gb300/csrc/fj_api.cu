@@ -486,14 +486,18 @@ int fj_autotune_mixed(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table
     int bv = v0, bc = c0;
     double best = -1;
     for (int v = 0; v < kMixedVariants; v++)
-        for (int c : chunks) {
+        for (int ci = 0; ci < 3; ci++) {
             ctx->mixed_variant = v;
-            ctx->mixed_chunk = c;
-            fj_moment_stats st;
-            int rc = run_moments(ctx, pot, delta, df, rule, 0, Rz, npts, out6, &st);
-            if (rc) { ctx->mixed_variant = v0; ctx->mixed_chunk = c0; return rc; }
-            if (all_ms) all_ms[v * 3 + (c == 2048 ? 0 : c == 4096 ? 1 : 2)] = st.kernel_ms;
-            if (best < 0 || st.kernel_ms < best) { best = st.kernel_ms; bv = v; bc = c; }
+            ctx->mixed_chunk = chunks[ci];
+            double ms = -1;
+            for (int rep = 0; rep < 2; rep++) {  // the faster of two launches (the first may pay one-time costs)
+                fj_moment_stats st;
+                int rc = run_moments(ctx, pot, delta, df, rule, 0, Rz, npts, out6, &st);
+                if (rc) { ctx->mixed_variant = v0; ctx->mixed_chunk = c0; return rc; }
+                if (ms < 0 || st.kernel_ms < ms) ms = st.kernel_ms;
+            }
+            if (all_ms) all_ms[v * 3 + ci] = ms;
+            if (best < 0 || ms < best) { best = ms; bv = v; bc = chunks[ci]; }
         }
     ctx->mixed_variant = bv;
     ctx->mixed_chunk = bc;
