@@ -49,10 +49,10 @@ FP64_FLOPS_PER_EVAL = {"plain": 1.23e5, "gl": None}
 # (profiles/moments_mixed_nfw_80x40.md)
 FP32_FLOPS_PER_EVAL = {"mixed": 4.68e4}
 # DRAM bytes (read + write) per phase-space evaluation from the same captures:
-# 418.6 MB over 2,555,520 evaluations (mixed; local-memory and partial-sum
-# traffic, the inputs are < 16 KB), 53.4 MB over 255,552 (plain FP64); a launch's
-# traffic scales with its evaluations
-DRAM_BYTES_PER_EVAL = {"mixed": 418.6e6 / 2555520, "plain": 53.4e6 / 255552}
+# 1027.2 MB over 2,555,520 evaluations (mixed, the 80-register build the autotuner
+# keeps; local-memory and partial-sum traffic, the inputs are < 16 KB), 53.4 MB over
+# 255,552 (plain FP64); a launch's traffic scales with its evaluations
+DRAM_BYTES_PER_EVAL = {"mixed": 1027.2e6 / 2555520, "plain": 53.4e6 / 255552}
 
 
 def parse():
