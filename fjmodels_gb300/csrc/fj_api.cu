@@ -246,7 +246,7 @@ int build_args(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta
     const long long nq3 = (long long)rule->nq * rule->nq * rule->nq;
     a.mixed_chunk = ctx->mixed_chunk;
     a.blocks_per_point =
-        mixed ? mixed_blocks_per_point(nq3, a.mixed_chunk) : (int)((nq3 + kMomentBlock - 1) / kMomentBlock);
+        mixed ? mixed_blocks_per_point(nq3, a.mixed_chunk) : (int)((nq3 + kPlainChunk - 1) / kPlainChunk);
     a.out6 = out6;
     a.jout = nullptr;
     return FJ_OK;

@@ -12,6 +12,7 @@ struct fj_quad_rule;
 namespace fj {
 
 constexpr int kMomentBlock = 128;  // threads per block of the phase-space kernel
+constexpr int kPlainChunk = 1024;  // velocity nodes of one point per block (FP64 form)
 // per-thread stack the kernels need: the QAGS interval list (kQagsCap entries
 // of four doubles and an int), the epsilon table and the call frames
 constexpr size_t kStackBytes = 8192;

@@ -5,10 +5,16 @@
 //
 // Work unit: node q = (i, j, k) of the nq^3 tensor rule (integ/GaussQuad.cpp:
 // 160-180), velocity V = 1e-6 + Ve*(x_i, x_j, x_k) (integ/Integ.cpp:46-62).
-// Blocks of kMomentBlock threads cover consecutive nodes of one point; the
-// per-block sums go to a scratch array and a second kernel adds them in a
-// fixed order, so results are deterministic run to run.
+// A block takes kPlainChunk consecutive nodes of one point, compacts the bound
+// ones (H < 0) into a shared list, orders it by the cost proxy of fj_order.cuh
+// and its threads take the entries as they free up; each node's DF goes to a
+// shared array, and after the list thread t sums the moments of entries t,
+// t + 128, .. in order.  The per-block sums go to a scratch array and a second
+// kernel adds them in a fixed order, so results are deterministic run to run.
+#include <cstdint>
+
 #include "fj_internal.h"
+#include "fj_order.cuh"
 
 namespace fj {
 
@@ -22,7 +28,9 @@ __device__ __forceinline__ double warp_sum(double v)
 size_t moment_smem_bytes(const MomentArgs &a)
 {
     const size_t nd = a.P.nr + 3 * (size_t)a.P.nr * a.P.npoly + 2 * a.ngrid + 2 * a.nq + 2 * a.gl.n;
-    return nd * sizeof(double) + 6 * (kMomentBlock / 32) * sizeof(double);
+    return nd * sizeof(double) + 6 * (kMomentBlock / 32) * sizeof(double) + 4 * sizeof(double) +
+           kPlainChunk * (sizeof(double) + sizeof(float) + sizeof(unsigned short)) + (kMomentBlock / 32 + 1) * sizeof(int) +
+           16;
 }
 
 __global__ void __launch_bounds__(kMomentBlock) k_moments(MomentArgs a0, MomentBatch batch)
@@ -39,6 +47,10 @@ __global__ void __launch_bounds__(kMomentBlock) k_moments(MomentArgs a0, MomentB
     double *s_ar = sm, *s_phil = s_ar + nr, *s_Pr = s_phil + nt, *s_Pr2 = s_Pr + nt;
     double *s_Eg = s_Pr2 + nt, *s_Dg = s_Eg + a.ngrid, *s_xq = s_Dg + a.ngrid, *s_wq = s_xq + a.nq;
     double *s_glx = s_wq + a.nq, *s_glw = s_glx + a.gl.n, *s_red = s_glw + a.gl.n;
+    double *s_pt = s_red + 6 * (kMomentBlock / 32), *s_df = s_pt + 4;
+    float *s_key = (float *)(s_df + kPlainChunk);
+    unsigned short *s_list = (unsigned short *)(s_key + kPlainChunk);
+    int *s_wc = (int *)(((uintptr_t)(s_list + kPlainChunk) + 15) & ~(uintptr_t)15), *s_next = s_wc + kMomentBlock / 32;
     for (int i = threadIdx.x; i < nr; i += blockDim.x) s_ar[i] = a.P.ar[i];
     for (int i = threadIdx.x; i < nt; i += blockDim.x) {
         s_phil[i] = a.P.phil[i]; s_Pr[i] = a.P.Pr[i]; s_Pr2[i] = a.P.Pr2[i];
@@ -52,55 +64,92 @@ __global__ void __launch_bounds__(kMomentBlock) k_moments(MomentArgs a0, MomentB
     const GLRule gl{a.gl.n, s_glx, s_glw};
     const int B = a.blocks_per_point;
     const int p = bid / B, chunk = bid % B;
-    const int nq = a.nq, nq3 = nq * nq * nq;
-    const int node = chunk * kMomentBlock + threadIdx.x;
-
-    double R, z;
-    if (a.Rz) { R = a.Rz[2 * p]; z = a.Rz[2 * p + 1]; }
-    else {
-        const int n = p / a.ngauss, g = p % a.ngauss;
-        const double c = a.ci[g], si = sqrt(1 - c * c);
-        R = s_ar[n] * si; z = s_ar[n] * c;
-    }
-
-    double m[6] = {0, 0, 0, 0, 0, 0};
-    unsigned bound = 0, failed = 0;
-    if (node < nq3) {
-        const int i = node / (nq * nq), j = (node / nq) % nq, k = node % nq;
-        const double Phi_h = pot_phi(P, R, z);
-        const double rmax = s_ar[nr - 1];
-        const double Ve = sqrt(-2 * (Phi_h - pot_phi(P, 10 * rmax, 10 * rmax)));
-        const double V0 = 1e-6 + Ve * s_xq[i], V1 = 1e-6 + Ve * s_xq[j], V2 = 1e-6 + Ve * s_xq[k];
-        const double jacob = Ve * Ve * Ve;
-        const double H = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h;
-        double DF = 0.;
-        if (H < 0) {
-            bound = 1;
-            unsigned fail = 0;
-            double Jr, Jz;
-            const double Delta = deltafn(s_Eg, s_Dg, a.ngrid, H);
-            fudge_actions(P, Delta, R, z, Phi_h, V0, V1, V2, gl, Jr, Jz, fail);
-            DF = df_value(a.df, P, R, Jr, Jz, R * V1, fail);
-            if (fail & (kFailBracket | kFailRoot)) DF = 0.;
-            failed = fail ? 1u : 0u;
+    const int nq = a.nq, nq2 = nq * nq, nq3 = nq2 * nq;
+    const int n0 = chunk * kPlainChunk, n1 = min(n0 + kPlainChunk, nq3);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {  // the point (integ/Integ.cpp:150-151)
+        double R, z;
+        if (a.Rz) { R = a.Rz[2 * p]; z = a.Rz[2 * p + 1]; }
+        else {
+            const int n = p / a.ngauss, g = p % a.ngauss;
+            const double c = a.ci[g], si = sqrt(1 - c * c);
+            R = s_ar[n] * si; z = s_ar[n] * c;
         }
-        const double w = s_wq[i] * s_wq[j] * s_wq[k];
-        const double jd = jacob * DF;
-        m[0] = w * jd;
-        m[1] = w * (jd * V1);
-        m[2] = w * (jd * V0 * V0);
-        m[3] = w * (jd * V1 * V1);
-        m[4] = w * (jd * V2 * V2);
-        m[5] = w * (jd * V0 * V2);
+        const double Phi_h = pot_phi(P, R, z), rmax = s_ar[nr - 1];
+        s_pt[0] = R; s_pt[1] = z; s_pt[2] = Phi_h;
+        s_pt[3] = sqrt(-2 * (Phi_h - pot_phi(P, 10 * rmax, 10 * rmax)));
+        *s_next = kMomentBlock;
+    }
+    __syncthreads();
+    const double R = s_pt[0], z = s_pt[1], Phi_h = s_pt[2], Ve = s_pt[3];
+    auto velocity = [&](int node, double &V0, double &V1, double &V2) {
+        V0 = 1e-6 + Ve * s_xq[node / nq2]; V1 = 1e-6 + Ve * s_xq[(node / nq) % nq]; V2 = 1e-6 + Ve * s_xq[node % nq];
+    };
+    // bound nodes of [n0, n1) in node order
+    int nbound = 0;
+    for (int base = n0; base < n1; base += kMomentBlock) {
+        const int node = base + threadIdx.x;
+        bool b = false;
+        if (node < n1) {
+            double V0, V1, V2;
+            velocity(node, V0, V1, V2);
+            b = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h < 0;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, b);
+        if (lane == 0) s_wc[warp] = __popc(bal);
+        __syncthreads();
+        int off = nbound, tot = 0;
+        for (int w = 0; w < kMomentBlock / 32; w++) {
+            if (w < warp) off += s_wc[w];
+            tot += s_wc[w];
+        }
+        if (b) s_list[off + __popc(bal & ((1u << lane) - 1u))] = (unsigned short)(node - n0);
+        __syncthreads();
+        nbound += tot;
+    }
+    for (int q = threadIdx.x; q < nbound; q += kMomentBlock) {
+        const int node = n0 + s_list[q];
+        s_key[q] = node_cost_key((float)s_xq[node / nq2], (float)s_xq[(node / nq) % nq], (float)s_xq[node % nq]);
+    }
+    sort_list(s_list, s_key, nbound);
+    // the solves, nodes taken as threads free up
+    unsigned failed = 0;
+    for (int q = threadIdx.x; q < nbound;) {
+        const int node = n0 + s_list[q];
+        double V0, V1, V2;
+        velocity(node, V0, V1, V2);
+        const double H = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h;
+        unsigned fail = 0;
+        double Jr, Jz;
+        fudge_actions(P, deltafn(s_Eg, s_Dg, a.ngrid, H), R, z, Phi_h, V0, V1, V2, gl, Jr, Jz, fail);
+        double DF = df_value(a.df, P, R, Jr, Jz, R * V1, fail);
+        if (fail & (kFailBracket | kFailRoot)) DF = 0.;
+        failed += fail ? 1u : 0u;
+        s_df[q] = DF;
+        q = atomicAdd(s_next, 1);
+    }
+    __syncthreads();
+    double m[6] = {0, 0, 0, 0, 0, 0};
+    const double jacob = Ve * Ve * Ve;
+    for (int q = threadIdx.x; q < nbound; q += kMomentBlock) {
+        const int node = n0 + s_list[q];
+        double V0, V1, V2;
+        velocity(node, V0, V1, V2);
+        const double w = s_wq[node / nq2] * s_wq[(node / nq) % nq] * s_wq[node % nq];
+        const double jd = jacob * s_df[q];
+        m[0] += w * jd;
+        m[1] += w * (jd * V1);
+        m[2] += w * (jd * V0 * V0);
+        m[3] += w * (jd * V1 * V1);
+        m[4] += w * (jd * V2 * V2);
+        m[5] += w * (jd * V0 * V2);
     }
     // block reduction in a fixed order
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int q = 0; q < 6; q++) {
         const double v = warp_sum(m[q]);
         if (lane == 0) s_red[warp * 6 + q] = v;
     }
-    const unsigned nb = __syncthreads_count(bound);
     const unsigned nf = __syncthreads_count(failed);
     if (threadIdx.x < 6) {
         double s = 0;
@@ -108,7 +157,7 @@ __global__ void __launch_bounds__(kMomentBlock) k_moments(MomentArgs a0, MomentB
         a.partial[((size_t)p * B + chunk) * 6 + threadIdx.x] = s;
     }
     if (threadIdx.x == 0) {
-        if (nb) atomicAdd(&a.counters[0], (unsigned long long)nb);
+        if (nbound) atomicAdd(&a.counters[0], (unsigned long long)nbound);
         if (nf) atomicAdd(&a.counters[1], (unsigned long long)nf);
     }
 }
