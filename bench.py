@@ -70,6 +70,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-points", type=int, default=0,
                     help="profiling case: one phase-space launch over this many grid points, no bench line")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"],
+                    help="c2: the bench line (NFW 80x40); c3: a two-component model (64x32, 15 iterations); "
+                         "c4: a batched sweep of seeded models (extra measurements, not the bench line)")
+    ap.add_argument("--models", type=int, default=256, help="c4: number of models")
     return ap.parse_args()
 
 
@@ -403,10 +407,66 @@ def profile_case(args):
                       "kernel_ms": st.kernel_ms, "failures": st.failures}))
 
 
+def workload_c3(args):
+    """Two-component model: Hernquist bulge (M = 0.1, r0 = 1) + NFW halo (M = 1, r0 = 10), each
+    component's h/g coefficients drawn from U[0.4, 1.0] with a fixed seed; 64 x 32 grid, l <= 10,
+    22^3 tanh-sinh nodes, the summed density in one Poisson solve, 15 iterations, mixed form."""
+    import fjmodels_gb300 as F
+    from fjmodels_gb300 import _abi as A
+    rng = np.random.default_rng(2024)
+    d1, d2 = rng.uniform(0.4, 1.0, 4), rng.uniform(0.4, 1.0, 4)
+    bulge = F.DFParams("Hernquist", *d1, mass=0.1, r0=1.0)
+    halo = F.DFParams("NFW", *d2, mass=1.0, r0=10.0)
+    ctx = F.Context(0)
+    rule = F.Rule(*velocity_rule(), precision=A.FJ_PREC_MIXED)
+    nr, ng, npl, it = 64, 32, 6, 15
+    out = ctx.run_model(nr, ng, npl, 1e-3, 300.0, bulge, rule, itermax=it, df2=halo,
+                        twocomp_order=A.FJ_TWOCOMP_SUMMED)
+    evals = 2 * nr * ng * CFG["nq"] ** 3 * it
+    ctx.close()
+    return {"workload": "c3", "metric": "wall-s per two-component model (64x32, l<=10, 15 iterations, mixed form)",
+            "value": out["wall_ms"] / 1e3, "unit": "s/model", "setup_s": out["setup_ms"] / 1e3,
+            "kernel_s": out["kernel_ms"] / 1e3, "phase_space_evals_per_s": evals / (out["wall_ms"] / 1e3),
+            "iterations": out["iterations"], "dfs": {"bulge": d1.round(4).tolist(), "halo": d2.round(4).tolist()},
+            "data": "synthetic (seeded DF draw, analytic guess densities)"}
+
+
+def workload_c4(args):
+    """Batched sweep: seeded models -- type from {Hernquist, Isochrone, NFW}, h/g coefficients
+    ~ U[0.3, 1.2], chi ~ U[0, 2], radii in {32, 48, 64, 96} x angles in {16, 24, 32}, l <= 8 --
+    iterated together (one phase-space launch per iteration, the iteration captured as a CUDA
+    graph, the focal-distance tables on the GPU), mixed form; 2 iterations timed whole."""
+    import fjmodels_gb300 as F
+    from fjmodels_gb300 import _abi as A
+    rng = np.random.default_rng(256)
+    models = []
+    for _ in range(args.models):
+        kind = ["Hernquist", "Isochrone", "NFW"][rng.integers(3)]
+        dh = rng.uniform(0.3, 1.2, 4)
+        df = F.DFParams(kind, *dh, chi=float(rng.uniform(0, 2)), k=0.5)
+        models.append(dict(nr=int(rng.choice([32, 48, 64, 96])), ngauss=int(rng.choice([16, 24, 32])), npoly=5,
+                           rmin=1e-3, rmax=300.0 if kind == "NFW" else 100.0, df=df))
+    ctx = F.Context(0)
+    rule = F.Rule(*velocity_rule(), precision=A.FJ_PREC_MIXED)
+    it = 2
+    outs = ctx.run_model_batch(models, rule, itermax=it, use_graph=True, delta_gpu=True)
+    o = outs[0]
+    evals = sum(m["nr"] * m["ngauss"] for m in models) * CFG["nq"] ** 3 * it
+    ctx.close()
+    return {"workload": "c4", "metric": f"wall-s per batched iteration of {len(models)} models (mixed form)",
+            "value": (o["wall_ms"] - o["setup_ms"]) / 1e3 / it, "unit": "s/iteration", "setup_s": o["setup_ms"] / 1e3,
+            "models": len(models), "grid_points": sum(m["nr"] * m["ngauss"] for m in models),
+            "phase_space_evals_per_s": evals / ((o["wall_ms"] - o["setup_ms"]) / 1e3),
+            "data": "synthetic (seeded model draw, analytic guess densities)"}
+
+
 def main():
     args = parse()
     if args.profile_points:
         profile_case(args)
+        return
+    if args.workload != "c2":
+        print(json.dumps(workload_c3(args) if args.workload == "c3" else workload_c4(args)))
         return
     rank, world = dist_init()
     if args.impl == "reference":
