@@ -65,7 +65,9 @@ def parse():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison step")
     ap.add_argument("--mixed-config", default=None,
                     help="variant,nodes_per_block of the mixed kernel (default: autotuned before warm-up)")
-    ap.add_argument("--cpu-sample", type=int, default=os.cpu_count(), help="grid points timed for the CPU baseline")
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="grid points timed for the CPU baseline (default: 10 per host thread for the cpu_baseline "
+                         "key, about 10 s; 2 per host thread for each step of --impl reference)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--profile-points", type=int, default=0,
@@ -474,10 +476,10 @@ def main():
             return
         res = []
         for _ in range(args.warmup):
-            cpu_sample(args, sample=min(args.cpu_sample, 4))
+            cpu_sample(args, sample=4)
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            res.append(cpu_sample(args, sample=args.cpu_sample))
+            res.append(cpu_sample(args, sample=args.cpu_sample or 2 * os.cpu_count()))
         wall = time.perf_counter() - t0
         v = float(np.mean([r["value"] for r in res]))
         cb = dict(res[-1], value=v)
@@ -494,7 +496,7 @@ def main():
         if not args.no_e2e:
             out["e2e"] = e2e_ours(args, out.get("mixed_kernel_config"))
         if not args.no_cpu and world == 1:
-            out["cpu_baseline"] = cpu_sample(args, sample=args.cpu_sample)
+            out["cpu_baseline"] = cpu_sample(args, sample=args.cpu_sample or 10 * os.cpu_count())
         print(json.dumps(out))
 
 
