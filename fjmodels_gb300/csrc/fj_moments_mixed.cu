@@ -34,6 +34,12 @@ namespace fj {
 //    Its sums are those of the static form term by term, so both give the
 //    same bits.
 // Which one, and the chunk size, is a per-context setting (fj_autotune_mixed).
+// Shared memory holds only what the node solves read: the FP32 tables, the
+// radii, the focal-distance table, the velocity rule and the node list.  The
+// FP64 potential tables are read from global memory (the point setup, the
+// FP32 table build and the rare FP64 turning-point path): kept out of shared
+// memory they leave L1 to the threads' local memory (QAGS lists, call
+// frames), which took the 80x40 launch from ~347 to ~311 ms.
 int mixed_blocks_per_point(long long nq3, int chunk) { return (int)((nq3 + chunk - 1) / chunk); }
 
 // capacity of a block's node list: the next power of two >= the node range (the sort pads to it)
@@ -47,7 +53,7 @@ __host__ __device__ static int mixed_list_cap(int chunk)
 size_t moment_mixed_smem_bytes(const MomentArgs &a)
 {
     const size_t nt = (size_t)a.P.nr * a.P.npoly;
-    return (a.P.nr + 3 * nt + 2 * a.ngrid + 2 * a.nq + 6 * (kMixedBlock / 32) + 4) * sizeof(double) +
+    return (a.P.nr + 2 * a.ngrid + 2 * a.nq + 6 * (kMixedBlock / 32) + 4) * sizeof(double) +
            (2 * a.P.nr + 2 * nt + 4 * kQuadIntervals + a.P.npoly) * sizeof(float) + sizeof(GK21f) + 16 +
            (kMixedBlock / 32) * sizeof(int) + (size_t)mixed_list_cap(a.mixed_chunk) * sizeof(unsigned short) + 16 +
            (size_t)mixed_list_cap(a.mixed_chunk) * sizeof(float) + sizeof(int);
@@ -66,8 +72,8 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
         bid -= batch.block_start[m];
     }
     const int nr = a.P.nr, npoly = a.P.npoly, nt = nr * npoly;
-    double *s_ar = sm, *s_phil = s_ar + nr, *s_Pr = s_phil + nt, *s_Pr2 = s_Pr + nt;
-    double *s_Eg = s_Pr2 + nt, *s_Dg = s_Eg + a.ngrid, *s_xq = s_Dg + a.ngrid, *s_wq = s_xq + a.nq;
+    double *s_ar = sm;
+    double *s_Eg = s_ar + nr, *s_Dg = s_Eg + a.ngrid, *s_xq = s_Dg + a.ngrid, *s_wq = s_xq + a.nq;
     double *s_red = s_wq + a.nq, *s_pt = s_red + 6 * (kMixedBlock / 32);
     float *f_ar = (float *)(s_pt + 4), *f_phil = f_ar + nr, *f_Pr = f_phil + nt, *f_ih = f_Pr + nt;
     float *f_qc = f_ih + nr, *f_pyl = f_qc + 4 * kQuadIntervals;
@@ -78,9 +84,6 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
     float *s_df = (float *)(((uintptr_t)(s_list + cap) + 15) & ~(uintptr_t)15);
     int *s_next = (int *)(s_df + cap);
     for (int i = threadIdx.x; i < nr; i += blockDim.x) s_ar[i] = a.P.ar[i];
-    for (int i = threadIdx.x; i < nt; i += blockDim.x) {
-        s_phil[i] = a.P.phil[i]; s_Pr[i] = a.P.Pr[i]; s_Pr2[i] = a.P.Pr2[i];
-    }
     for (int i = threadIdx.x; i < a.ngrid; i += blockDim.x) { s_Eg[i] = a.Eg[i]; s_Dg[i] = a.Dg[i]; }
     for (int i = threadIdx.x; i < a.nq; i += blockDim.x) { s_xq[i] = a.xq[i]; s_wq[i] = a.wq[i]; }
     if (threadIdx.x < 11) {
@@ -88,7 +91,7 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
         sK->wgk[threadIdx.x] = (float)fj_wgk21_d[threadIdx.x];
         if (threadIdx.x < 5) sK->wg[threadIdx.x] = (float)fj_wg10_d[threadIdx.x];
     }
-    const PotView P{nr, npoly, s_ar, s_phil, s_Pr, s_Pr2};
+    const PotView P{nr, npoly, s_ar, a.P.phil, a.P.Pr, a.P.Pr2};
     const int B = a.blocks_per_point;
     const int p = bid / B, chunk = bid % B;
     __syncthreads();
@@ -107,7 +110,7 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
     }
     __syncthreads();
     const double R = s_pt[0], z = s_pt[1], Phi_h = s_pt[2], Ve = s_pt[3];
-    mixed_tables_f(nr, npoly, s_ar, s_phil, s_Pr, Phi_h, R, z, f_ar, f_phil, f_Pr, f_ih, f_qc, f_pyl, threadIdx.x,
+    mixed_tables_f(nr, npoly, s_ar, a.P.phil, a.P.Pr, Phi_h, R, z, f_ar, f_phil, f_Pr, f_ih, f_qc, f_pyl, threadIdx.x,
                    blockDim.x);
     const int nq = a.nq, nq2 = nq * nq;
     const long long nq3 = (long long)nq2 * nq;
@@ -141,7 +144,7 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
         s_df[q] = node_cost_key((float)s_xq[node / nq2], (float)s_xq[(node / nq) % nq], (float)s_xq[node % nq]);
     }
     sort_list(s_list, s_df, nbound);
-    const PotViewF PF = mixed_view_f(nr, npoly, s_ar, s_phil, Phi_h, R, z, f_ar, f_phil, f_Pr, f_ih, f_qc, f_pyl);
+    const PotViewF PF = mixed_view_f(nr, npoly, s_ar, a.P.phil, Phi_h, R, z, f_ar, f_phil, f_Pr, f_ih, f_qc, f_pyl);
     const double jacob = Ve * Ve * Ve;
 
     double m[6] = {0, 0, 0, 0, 0, 0};
