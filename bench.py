@@ -43,16 +43,16 @@ UNIT = "s/model"
 # FP64 operations per phase-space evaluation executed by active threads of the
 # phase-space kernel (dadd + dmul + 2*dfma from ncu on the nfw_80x40 workload,
 # profiles/moments_fp64_nfw_80x40.md); the algorithmic work unit of the roofline.
-FP64_FLOPS_PER_EVAL = {"plain": 1.23e5, "gl": None}
+FP64_FLOPS_PER_EVAL = {"plain": 1.21e5, "gl": None}
 # FP32 operations (fadd + fmul + 2*ffma) executed by active lanes per phase-space
 # evaluation of the mixed form, from ncu on a 240-point spread of the same workload
 # (profiles/moments_mixed_nfw_80x40.md)
 FP32_FLOPS_PER_EVAL = {"mixed": 4.68e4}
 # DRAM bytes (read + write) per phase-space evaluation from the same captures:
-# 1027.2 MB over 2,555,520 evaluations (mixed, the 80-register build the autotuner
-# keeps; local-memory and partial-sum traffic, the inputs are < 16 KB), 53.4 MB over
+# 1678.2 MB over 2,555,520 evaluations (mixed, the 64-register build with 8 blocks
+# per SM; local-memory and partial-sum traffic, the inputs are < 16 KB), 7.58 MB over
 # 255,552 (plain FP64); a launch's traffic scales with its evaluations
-DRAM_BYTES_PER_EVAL = {"mixed": 1027.2e6 / 2555520, "plain": 53.4e6 / 255552}
+DRAM_BYTES_PER_EVAL = {"mixed": 1678.2e6 / 2555520, "plain": 7.58e6 / 255552}
 
 
 def parse():
