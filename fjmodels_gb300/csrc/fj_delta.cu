@@ -2,9 +2,13 @@
 // per (model, energy) runs delta_energy (fj_delta.cuh), the same code as the
 // host's fj_tabulate_delta.  The energies' searches take very different paths
 // and lengths (bracket walks of one to thousands of steps, adaptive orbit
-// steps), so each thread runs alone in its block -- lanes of one warp would
-// serialise each other's paths -- and the SMs interleave the single-thread
-// blocks.  Built without FMA contraction, like the host code.
+// steps), and the launch lasts as long as its slowest fit, so what counts is
+// that every fit starts at once: 32 threads per block keep all of them
+// resident (256 models x 30 energies: 13.0 s, against 22.3 s with one thread
+// per block, where the SMs' 32-block limit made two waves).  A warp per fit,
+// its lanes sharing the sums over the orbit points, was not faster (23.5 s):
+// the sums are not where the slow fits spend their time.  Built without FMA
+// contraction, like the host code.
 //
 // The fit of the focal distance to an orbit is not a continuous function of
 // rounding: a change of one unit in the last place of the orbit equations
@@ -19,10 +23,10 @@ namespace fj {
 
 namespace {
 
-__global__ void __launch_bounds__(1) k_tabulate_delta(const PotView *pots, double *const *Eg,
+__global__ void __launch_bounds__(32) k_tabulate_delta(const PotView *pots, double *const *Eg,
                                                                double *const *Dg, int n, int ngrid, int *bad)
 {
-    const int t = blockIdx.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n * ngrid) return;
     const int m = t / ngrid, nE = t % ngrid;
     const PotView P = pots[m];
@@ -42,7 +46,7 @@ cudaError_t launch_tabulate_delta(const PotView *pots, double *const *Eg, double
                                   int *bad, cudaStream_t s)
 {
     const int nt = n * ngrid;
-    k_tabulate_delta<<<nt, 1, 0, s>>>(pots, Eg, Dg, n, ngrid, bad);
+    k_tabulate_delta<<<(nt + 31) / 32, 32, 0, s>>>(pots, Eg, Dg, n, ngrid, bad);
     return cudaGetLastError();
 }
 

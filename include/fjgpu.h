@@ -328,8 +328,10 @@ int fj_tabulate_delta(const fj_potential *pot_host, int ngrid, double *Egrid, do
    one model).  pots host [n] of DEVICE potential tables (nr >= 11); Egrid,
    Dgrid device [n][ngrid]; status host [n] (may be NULL): FJ_OK, or
    FJ_ERR_ARG where a bracket or root search hit its cap (the host call's
-   return value).  The tables agree with the host's to the rounding of the
-   device's transcendental functions (root tolerance 1e-8). */
+   return value).  The energies agree with the host's to rounding; the focal
+   distances are another draw of the same fit (the fit is not continuous in
+   the rounding of the device's transcendental functions: entries move by
+   ~10-20 %, the densities they give by a few per cent). */
 int fj_tabulate_delta_batch(fj_ctx *ctx, int n, const fj_potential *pots, int ngrid, double *Egrid, double *Dgrid,
                             int *status);
 
