@@ -27,7 +27,7 @@ SOURCES = {"fj_moments.cu": ["--fmad=false"], "fj_multipole.cu": ["--fmad=false"
            "fj_los.cu": ["--fmad=false"], "fj_delta.cu": ["--fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-         "-Xcompiler", "-Wall,-Wno-unused-function,-ffp-contract=off"]
+         "-Xcompiler", "-Wall,-Wno-unused-function,-Wno-unknown-pragmas,-ffp-contract=off"]
 
 
 def nvcc():
