@@ -1,14 +1,15 @@
 // fj_delta.cu -- the focal-distance tables of many models at once: one thread
 // per (model, energy) runs delta_energy (fj_delta.cuh), the same code as the
 // host's fj_tabulate_delta.  The energies' searches take very different paths
-// and lengths (bracket walks of one to thousands of steps, adaptive orbit
-// steps), and the launch lasts as long as its slowest fit, so what counts is
-// that every fit starts at once: 32 threads per block keep all of them
-// resident (256 models x 30 energies: 13.0 s, against 22.3 s with one thread
-// per block, where the SMs' 32-block limit made two waves).  A warp per fit,
-// its lanes sharing the sums over the orbit points, was not faster (23.5 s):
-// the sums are not where the slow fits spend their time.  Built without FMA
-// contraction, like the host code.
+// and lengths (most of a fit is the search for its Jr = 0 orbit: repeated
+// adaptive orbit integrations), and the launch lasts as long as its slowest
+// fits, so every fit starts at once and the fits are spread evenly over the
+// SMs: small blocks of kDeltaThreads.  256 models x 30 energies on the GB300:
+// 10.7 s with 8 threads per block, 11.0 s with 16, 11.8 s with 32 or 64, and
+// 22.3 s with one thread per block (the SMs' 32-block limit made two waves).
+// A warp per fit, its lanes sharing the sums over the orbit points of the
+// focal-distance walk, was not faster: those sums are a small part of a fit.
+// Built without FMA contraction, like the host code.
 //
 // The fit of the focal distance to an orbit is not a continuous function of
 // rounding: a change of one unit in the last place of the orbit equations
@@ -23,7 +24,9 @@ namespace fj {
 
 namespace {
 
-__global__ void __launch_bounds__(32) k_tabulate_delta(const PotView *pots, double *const *Eg,
+constexpr int kDeltaThreads = 8;  // fits per block
+
+__global__ void __launch_bounds__(kDeltaThreads) k_tabulate_delta(const PotView *pots, double *const *Eg,
                                                                double *const *Dg, int n, int ngrid, int *bad)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -46,7 +49,7 @@ cudaError_t launch_tabulate_delta(const PotView *pots, double *const *Eg, double
                                   int *bad, cudaStream_t s)
 {
     const int nt = n * ngrid;
-    k_tabulate_delta<<<(nt + 31) / 32, 32, 0, s>>>(pots, Eg, Dg, n, ngrid, bad);
+    k_tabulate_delta<<<(nt + kDeltaThreads - 1) / kDeltaThreads, kDeltaThreads, 0, s>>>(pots, Eg, Dg, n, ngrid, bad);
     return cudaGetLastError();
 }
 

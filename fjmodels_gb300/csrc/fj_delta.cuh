@@ -14,7 +14,7 @@ constexpr int kOrbSize = 200;
 
 struct DeltaFit {
     PotView P;
-    double E, Lz, Rc, R0, D2, sqDR, v0, cv, sv, Ri, zi;
+    double E, Lz, Lz2, Rc, R0, D2, sqDR, v0, cv, sv, Ri, zi;  // Lz2 = pow(Lz, 2.0), once per fit
     double R[kOrbSize], z[kOrbSize];
     int N;
     bool bad;
@@ -26,20 +26,20 @@ FJ_HD void orbit_rhs(const DeltaFit &d, const double *y, double *f)
     pot_grad(d.P, y[0], y[1], phi, dR, dz);
     f[0] = y[2];
     f[1] = y[3];
-    f[2] = -dR + pow(d.Lz, 2.0) / pow(y[0], 3.0);
+    f[2] = -dR + d.Lz2 / pow(y[0], 3.0);  // Delta.cpp's pow(Lz, 2.0), taken once per fit
     f[3] = -dz;
 }
 
 FJ_HDNI void gbs_step(const DeltaFit &d, double h, const double *y0, double *y1, double *yerr)
 {
     constexpr int K = 6;
-    double T[K][4], prev[4] = {0, 0, 0, 0};
+    double T[K][4], prev[4] = {0, 0, 0, 0}, dy0[4];
+    orbit_rhs(d, y0, dy0);  // the same first derivative for every sequence
     for (int k = 0; k < K; k++) {
         const int ns = 2 * (k + 1);
         const double hs = h / ns;
         double zm[4], zc[4], dy[4];
-        orbit_rhs(d, y0, dy);
-        for (int i = 0; i < 4; i++) { zm[i] = y0[i]; zc[i] = y0[i] + hs * dy[i]; }
+        for (int i = 0; i < 4; i++) { zm[i] = y0[i]; zc[i] = y0[i] + hs * dy0[i]; }
         for (int s = 1; s < ns; s++) {
             orbit_rhs(d, zc, dy);
             for (int i = 0; i < 4; i++) { const double zn = zm[i] + 2 * hs * dy[i]; zm[i] = zc[i]; zc[i] = zn; }
@@ -256,6 +256,7 @@ FJ_HDNI double delta_energy(const PotView &P, const DeltaBase &b, int nE, int ng
     d.P = P;
     d.E = E;
     d.Lz = .25 * b.Lz1;
+    d.Lz2 = pow(d.Lz, 2.0);
     // RcE (include/Utils.h:220-236)
     RcEF fe{P, d.E};
     double R0 = .8 * b.Rg1, f0 = fe(R0);

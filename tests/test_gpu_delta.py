@@ -1,6 +1,6 @@
 """The focal-distance table on the GPU (fj_tabulate_delta_batch: the host's
 tabulateDelta code, delta/tabulate.cpp:13-38 and delta/Delta.cpp, one thread per
-(model, energy), 32 per block).  The focal-distance fit is not continuous in rounding (one unit in
+(model, energy), 8 per block).  The focal-distance fit is not continuous in rounding (one unit in
 the last place of the orbit equations moves entries by tens of per cent; the host code
 does the same), so the GPU table is checked for what is stable: the energies against
 the host's and the reference's to 1e-12, run-to-run identity, and the density moments a
