@@ -160,6 +160,8 @@ FORM_TEXT = {"mixed": "mixed precision (FP32 turning points, QAGS momentum integ
                       "limit turning points and accumulation)",
              "plain": "plain FP64, QAGS momentum integrals",
              "gl": "FP64, 16-point Gauss-Legendre momentum integrals"}
+WORKLOAD = (f"NFW rotating (chi=1,k=0.5) {CFG['nr']}x{CFG['ngauss']} grid, l<=12, 22^3 tanh-sinh nodes, "
+            f"{CFG['iters_per_model']} iterations/model")
 
 
 def velocity_rule():
@@ -254,8 +256,7 @@ def run_ours(args, rank, world):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64" if fp32 else "f64",
         "data": "synthetic (analytic NFW guess density, seeded by construction)",
-        "config": {"workload": f"NFW rotating (chi=1,k=0.5) {nr}x{ng} grid, l<=12, 22^3 tanh-sinh nodes, "
-                               f"{CFG['iters_per_model']} iterations/model",
+        "config": {"workload": WORKLOAD,
                    "form": FORM_TEXT[args.form],
                    "phase_space_evals_per_step": nodes, "bound_evals_per_step": last.bound,
                    "l2": "256 MiB buffer written between steps", "parallelism": f"replicas{world}"},
@@ -486,8 +487,9 @@ def main():
         print(json.dumps({"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
                           "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
                           "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                          "data": "synthetic", "config": {"workload": "NFW rotating 80x40, l<=12, 22^3 tanh-sinh",
-                                                          "form": args.form},
+                          "data": "synthetic", "config": {"workload": WORKLOAD,
+                                                          "form": "the reference's FP64 algorithm on the host "
+                                                                  "(the oracle's C restatement)"},
                           "cpu_baseline": cb,
                           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
