@@ -550,7 +550,7 @@ FJ_HDNI float qags_f(F &f, const GK21f &K, float a, float b, float epsabs, float
     if ((err0 <= tol && err0 != resasc0) || err0 == 0.0f) return res0;
 
     float alist[kQagsCapF], blist[kQagsCapF], rlist[kQagsCapF], elist[kQagsCapF];
-    int iord[kQagsCapF];
+    unsigned char iord[kQagsCapF];  // interval indices < kQagsCapF
     float rlist2[52], res3la[3];
     int nres = 0, numrl2 = 1;
     alist[0] = a; blist[0] = b; rlist[0] = res0; elist[0] = err0; iord[0] = 0;
