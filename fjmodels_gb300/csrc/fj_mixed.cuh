@@ -536,6 +536,7 @@ FJ_HD void qelg_f(float *tab, int &n_io, float *res3, int &nres, float &result, 
 }
 
 constexpr int kQagsCapF = 64;
+static_assert(kQagsCapF <= 256, "qags_f keeps interval indices as bytes");
 
 // QAGS (DQAGSE) in FP32 on [a,b] with the reference's tolerances; interval
 // list of kQagsCapF entries on the thread's stack.
