@@ -1,6 +1,6 @@
 // fj_peak.cu -- FMA-throughput micro-benchmark: the FP64 / FP32 peaks the
-// phase-space kernel's roofline is quoted against (the measured peaks
-// cover HBM and BF16 tensor throughput only).
+// phase-space kernels' rooflines are quoted against (a copy-bandwidth or BF16
+// GEMM measurement says nothing about these pipes).
 #include <cuda_runtime.h>
 
 #include "../../include/fjgpu.h"
