@@ -73,7 +73,7 @@ def build(verbose=False, force=False):
         for _, log in results:
             sys.stderr.write(log)
     tmp = LIB + ".tmp"
-    r = subprocess.run([cc, *ARCH, "-shared", "-o", tmp, *[o for o, _ in results], "-lcudart"],
+    r = subprocess.run([cc, *ARCH, "-shared", "-o", tmp, *[o for o, _ in results], "-lcudart", "-lpthread"],
                        capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stderr)

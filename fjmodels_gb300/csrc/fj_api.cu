@@ -4,6 +4,7 @@
 // file writer) plus the one-component self-consistent loop.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -11,6 +12,7 @@
 #include <fstream>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/fjgpu.h"
@@ -689,20 +691,32 @@ int fj_guess_rhl(int nr, int ngauss, int npoly, const double *ar, int kind, doub
 }  // extern "C"
 
 // --------------------------------------------------- focal-distance table
-// tabulateDelta (delta/tabulate.cpp:13-38) on the host, one energy after the
-// other (fj_delta.cuh); fj_tabulate_delta_batch runs the same code per
-// (model, energy) on the GPU.
+// tabulateDelta (delta/tabulate.cpp:13-38) on the host (fj_delta.cuh); the
+// energies are independent, so host threads take them in turn (each entry is
+// the same computation whichever thread runs it: the same bits as one thread).
+// fj_tabulate_delta_batch runs the same code per (model, energy) on the GPU.
 extern "C" int fj_tabulate_delta(const fj_potential *pot, int ngrid, double *Egrid, double *Dgrid)
 {
     if (!pot || pot->nr < 11 || pot->npoly < 1 || pot->npoly > kMaxPoly || ngrid < 2 || !Egrid || !Dgrid)
         return FJ_ERR_ARG;
     const PotView P = view(pot);
     const DeltaBase base = delta_base(P);
-    bool bad = base.bad;
-    std::vector<DeltaFit> fits(1);
-    for (int nE = 0; nE < ngrid; nE++)
-        Dgrid[nE] = delta_energy(P, base, nE, ngrid, Egrid[nE], fits[0], bad, kDeltaWalkCapHost);
-    return bad ? FJ_ERR_ARG : FJ_OK;
+    const int nthreads = (int)std::max(1u, std::min((unsigned)ngrid, std::thread::hardware_concurrency()));
+    std::vector<DeltaFit> fits(nthreads);
+    std::vector<char> bad(nthreads, base.bad ? 1 : 0);
+    auto work = [&](int t) {
+        bool b = false;
+        for (int nE = t; nE < ngrid; nE += nthreads)
+            Dgrid[nE] = delta_energy(P, base, nE, ngrid, Egrid[nE], fits[t], b, kDeltaWalkCapHost);
+        if (b) bad[t] = 1;
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nthreads; t++) pool.emplace_back(work, t);
+    work(0);
+    for (auto &th : pool) th.join();
+    for (char b : bad)
+        if (b) return FJ_ERR_ARG;
+    return FJ_OK;
 }
 
 // The focal-distance tables of n models on the GPU (fj_delta.cu): views of
