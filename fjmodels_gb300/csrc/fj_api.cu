@@ -625,6 +625,10 @@ int fj_los(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, co
     a.m.counters = (unsigned long long *)ctx->counters.p;
     a.rhl = rhl; a.kind = kind; a.Rzv = Rzv; a.n = n; a.out = out;
     fj_tanh_sinh01(a.x01, a.w01);
+    a.blocks_per_item = los_blocks_per_item(kind, rule->nq);
+    if ((long long)n * a.blocks_per_item > 0x7fffffffLL) return fail(ctx, FJ_ERR_ARG, "los: too many values");
+    if ((rc = ensure(ctx, ctx->partial, (size_t)n * a.blocks_per_item * sizeof(double)))) return rc;
+    a.partial = (double *)ctx->partial.p;
     FJ_CUDA(cudaMemsetAsync(ctx->counters.p, 0, 4 * sizeof(unsigned long long), ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     FJ_CUDA(launch_los(a, ctx->stream));

@@ -52,8 +52,12 @@ struct LosArgs {
     int n;
     double *out;        // [n]
     double x01[kLos01], w01[kLos01];
+    int blocks_per_item;  // blocks sharing one value's nodes (kLosChunk nodes each)
+    double *partial;      // [n][blocks_per_item] block sums, added in order by k_los_finalize
 };
+constexpr int kLosChunk = 1024;  // nodes of one value per block
 cudaError_t launch_los(const LosArgs &a, cudaStream_t s);
+int los_blocks_per_item(int kind, int nq);
 size_t los_local_bytes();
 
 // Focal-distance tables of n models (fj_delta.cu): one thread per (model,

@@ -3,9 +3,12 @@
 // the phase-space kernel's node body (Staeckel-fudge actions + DF, plain FP64)
 // under 3-D and 2-D tensor rules.
 //
-// One block per requested value.  Its threads take the rule's nodes
-// round-robin and each sums its nodes in node order; the block adds the
-// thread sums in a fixed order, so a value is the same run to run.
+// A value's nodes are split into ranges of kLosChunk nodes, one block each
+// (a line profile's 22^3 nodes: 11 blocks), so a few hundred values fill the
+// GPU.  A block's threads take its nodes round-robin and each sums its nodes
+// in node order; the block adds the thread sums in a fixed order and
+// k_los_finalize adds the blocks' sums in order, so a value is the same run
+// to run.
 //   SIGMA  SigmaDF(R, z) = 2 sum_i w01_i (rmax - R) rho(R + x01_i (rmax - R), z),
 //          rho from the density multipoles (ev_dens, UtilsLeg.h:285-298, 323-334)
 //   LINE   line_profile(R, z, vx): [-1,1]^3 rule over (vy, x, vz), the DF at the
@@ -82,7 +85,7 @@ __global__ void __launch_bounds__(kLosBlock) k_los(LosArgs a)
     __syncthreads();
     const PotView P{nr, npoly, s_ar, s_phil, s_Pr, s_Pr2};
     const GLRule gl{m.gl.n, s_glx, s_glw};
-    const int item = blockIdx.x;
+    const int B = a.blocks_per_item, item = blockIdx.x / B, chunk = blockIdx.x % B;
     const double R = a.Rzv[3 * item], z = a.Rzv[3 * item + 1], v = a.Rzv[3 * item + 2];
     if (a.kind == FJ_LOS_SIGMA) {
         if (threadIdx.x == 0) a.out[item] = sigma_df(P, s_rhl, a, R, z);
@@ -92,9 +95,10 @@ __global__ void __launch_bounds__(kLosBlock) k_los(LosArgs a)
     const double Phi = pot_phi(P, R, z), Ve = sqrt(-2 * (Phi - pot_phi(P, 10 * rmax, 10 * rmax)));
     const int nq = m.nq;
     const int nnodes = a.kind == FJ_LOS_LINE ? nq * nq * nq : (a.kind == FJ_LOS_PVPHI ? kLos01 * kLos01 : kLos01 * nq);
+    const int n0 = (int)((long long)chunk * nnodes / B), n1 = (int)((long long)(chunk + 1) * nnodes / B);
     double sum = 0;
     unsigned failed = 0, bound = 0;
-    for (int node = threadIdx.x; node < nnodes; node += kLosBlock) {
+    for (int node = n0 + threadIdx.x; node < n1; node += kLosBlock) {
         double V[3], w, jacob;
         if (a.kind == FJ_LOS_LINE) {  // lineProfile(vy, x, vz), Integ.cpp:63-92
             const int i = node / (nq * nq), j = (node / nq) % nq, k = node % nq;
@@ -139,8 +143,7 @@ __global__ void __launch_bounds__(kLosBlock) k_los(LosArgs a)
     if (threadIdx.x == 0) {
         double s = 0;
         for (int q = 0; q < kLosBlock / 32; q++) s += s_red[q];
-        if (a.kind == FJ_LOS_LINE) s /= sigma_df(P, s_rhl, a, R, z);
-        a.out[item] = s;
+        a.partial[blockIdx.x] = s;
         if (a.m.counters) {
             if (nb) atomicAdd(&a.m.counters[0], (unsigned long long)nb);
             if (nf) atomicAdd(&a.m.counters[1], (unsigned long long)nf);
@@ -148,7 +151,27 @@ __global__ void __launch_bounds__(kLosBlock) k_los(LosArgs a)
     }
 }
 
+// a value's block sums in order; a line profile is divided by SigmaDF at the
+// point (Integ.cpp:92), from the tables in global memory
+__global__ void k_los_finalize(LosArgs a)
+{
+    const int item = blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= a.n || a.kind == FJ_LOS_SIGMA) return;
+    const int B = a.blocks_per_item;
+    double s = 0;
+    for (int c = 0; c < B; c++) s += a.partial[(size_t)item * B + c];
+    if (a.kind == FJ_LOS_LINE) s /= sigma_df(a.m.P, a.rhl, a, a.Rzv[3 * item], a.Rzv[3 * item + 1]);
+    a.out[item] = s;
+}
+
 }  // namespace
+
+int los_blocks_per_item(int kind, int nq)
+{
+    const long long nnodes = kind == FJ_LOS_LINE ? (long long)nq * nq * nq
+                             : kind == FJ_LOS_PVPHI ? (long long)kLos01 * kLos01 : (long long)kLos01 * nq;
+    return kind == FJ_LOS_SIGMA ? 1 : (int)((nnodes + kLosChunk - 1) / kLosChunk);
+}
 
 size_t los_smem_bytes(const MomentArgs &m)
 {
@@ -169,7 +192,10 @@ cudaError_t launch_los(const LosArgs &a, cudaStream_t s)
         const cudaError_t e = cudaFuncSetAttribute(k_los, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    k_los<<<a.n, kLosBlock, smem, s>>>(a);
+    k_los<<<(unsigned)((long long)a.n * a.blocks_per_item), kLosBlock, smem, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || a.kind == FJ_LOS_SIGMA) return e;
+    k_los_finalize<<<(a.n + 127) / 128, 128, 0, s>>>(a);
     return cudaGetLastError();
 }
 
