@@ -146,7 +146,7 @@ int fj_moments_points(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table
    The [-1,1] axes take `rule` (host arrays; precision FJ_PREC_FP64; jquad as
    for the moments), the [0,1] axes the reference's 22-point tanh-sinh table
    (fj_tanh_sinh01).  rhl device [nr*npoly] (may be NULL for PVPHI, PVZ,
-   PVR); out device [n].  Plain FP64, one thread block per value. */
+   PVR); out device [n].  Plain FP64; a value's nodes in blocks of 1024, summed in a fixed order. */
 #define FJ_LOS_SIGMA 0
 #define FJ_LOS_LINE 1
 #define FJ_LOS_PVPHI 2
