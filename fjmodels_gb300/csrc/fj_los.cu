@@ -5,10 +5,12 @@
 //
 // A value's nodes are split into ranges of kLosChunk nodes, one block each
 // (a line profile's 22^3 nodes: 11 blocks), so a few hundred values fill the
-// GPU.  A block's threads take its nodes round-robin and each sums its nodes
-// in node order; the block adds the thread sums in a fixed order and
-// k_los_finalize adds the blocks' sums in order, so a value is the same run
-// to run.
+// GPU.  As in the phase-space kernels, a block compacts its bound nodes,
+// orders them by the cost proxy of fj_order.cuh and hands them to threads as
+// they free up, storing each node's DF; thread t then sums list entries t,
+// t + kLosBlock, .. from the stored DFs, the block adds the thread sums in a
+// fixed order and k_los_finalize adds the blocks' sums in order, so a value
+// is the same run to run.
 //   SIGMA  SigmaDF(R, z) = 2 sum_i w01_i (rmax - R) rho(R + x01_i (rmax - R), z),
 //          rho from the density multipoles (ev_dens, UtilsLeg.h:285-298, 323-334)
 //   LINE   line_profile(R, z, vx): [-1,1]^3 rule over (vy, x, vz), the DF at the
@@ -21,6 +23,7 @@
 // arithmetic with.
 #include "../../include/fjgpu.h"
 #include "fj_internal.h"
+#include "fj_order.cuh"
 
 namespace fj {
 
@@ -74,6 +77,10 @@ __global__ void __launch_bounds__(kLosBlock) k_los(LosArgs a)
     double *s_ar = sm, *s_phil = s_ar + nr, *s_Pr = s_phil + nt, *s_Pr2 = s_Pr + nt;
     double *s_Eg = s_Pr2 + nt, *s_Dg = s_Eg + m.ngrid, *s_xq = s_Dg + m.ngrid, *s_wq = s_xq + m.nq;
     double *s_glx = s_wq + m.nq, *s_glw = s_glx + m.gl.n, *s_rhl = s_glw + m.gl.n, *s_red = s_rhl + nt;
+    double *s_df = s_red + kLosBlock / 32;                          // [kLosChunk] DF of the list entries
+    float *s_key = (float *)(s_df + kLosChunk);                       // [kLosChunk] cost keys
+    unsigned short *s_list = (unsigned short *)(s_key + kLosChunk);   // [kLosChunk] bound nodes
+    int *s_wc = (int *)(s_list + kLosChunk), *s_next = s_wc + kLosBlock / 32;
     for (int i = threadIdx.x; i < nr; i += blockDim.x) s_ar[i] = m.P.ar[i];
     for (int i = threadIdx.x; i < nt; i += blockDim.x) {
         s_phil[i] = m.P.phil[i]; s_Pr[i] = m.P.Pr[i]; s_Pr2[i] = m.P.Pr2[i];
@@ -96,10 +103,8 @@ __global__ void __launch_bounds__(kLosBlock) k_los(LosArgs a)
     const int nq = m.nq;
     const int nnodes = a.kind == FJ_LOS_LINE ? nq * nq * nq : (a.kind == FJ_LOS_PVPHI ? kLos01 * kLos01 : kLos01 * nq);
     const int n0 = (int)((long long)chunk * nnodes / B), n1 = (int)((long long)(chunk + 1) * nnodes / B);
-    double sum = 0;
-    unsigned failed = 0, bound = 0;
-    for (int node = n0 + threadIdx.x; node < n1; node += kLosBlock) {
-        double V[3], w, jacob;
+    // a node's velocity, weight and Jacobian
+    auto node_vel = [&](int node, double *V, double &w, double &jacob) {
         if (a.kind == FJ_LOS_LINE) {  // lineProfile(vy, x, vz), Integ.cpp:63-92
             const int i = node / (nq * nq), j = (node / nq) % nq, k = node % nq;
             const double vy = s_xq[i], x = s_xq[j], vz = s_xq[k];
@@ -122,30 +127,74 @@ __global__ void __launch_bounds__(kLosBlock) k_los(LosArgs a)
             jacob = Ve * Ve;
             w = a.w01[i] * s_wq[j];
         }
-        const double H = .5 * (V[0] * V[0] + V[1] * V[1] + V[2] * V[2]) + Phi;
-        double DF = 0.;
-        if (H < 0) {  // df(), DF.cpp:78-124
-            unsigned fail = 0;
-            double Jr, Jz;
-            fudge_actions(P, deltafn(s_Eg, s_Dg, m.ngrid, H), R, z, Phi, V[0], V[1], V[2], gl, Jr, Jz, fail);
-            DF = df_value(m.df, P, R, Jr, Jz, R * V[1], fail);
-            if (fail & (kFailBracket | kFailRoot)) DF = 0.;
-            failed += fail ? 1u : 0u;
-            bound++;
-        }
-        sum += w * (jacob * DF);
-    }
+    };
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // bound nodes of [n0, n1) in node order, then ordered by the cost proxy of
+    // the phase-space kernels (most expensive first), taken as threads free up
+    int nbound = 0;
+    for (int base = n0; base < n1; base += kLosBlock) {
+        const int node = base + threadIdx.x;
+        bool b = false;
+        if (node < n1) {
+            double V[3], w, jacob;
+            node_vel(node, V, w, jacob);
+            b = .5 * (V[0] * V[0] + V[1] * V[1] + V[2] * V[2]) + Phi < 0;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, b);
+        if (lane == 0) s_wc[warp] = __popc(bal);
+        __syncthreads();
+        int off = nbound, tot = 0;
+        for (int q = 0; q < kLosBlock / 32; q++) {
+            if (q < warp) off += s_wc[q];
+            tot += s_wc[q];
+        }
+        if (b) s_list[off + __popc(bal & ((1u << lane) - 1u))] = (unsigned short)(node - n0);
+        __syncthreads();
+        nbound += tot;
+    }
+    const double iVe = 1. / Ve;
+    for (int q = threadIdx.x; q < nbound; q += kLosBlock) {
+        double V[3], w, jacob;
+        node_vel(n0 + s_list[q], V, w, jacob);
+        s_key[q] = node_cost_key((float)(V[0] * iVe), (float)(V[1] * iVe), (float)(V[2] * iVe));
+    }
+    sort_list(s_list, s_key, nbound);
+    if (threadIdx.x == 0) *s_next = kLosBlock;
+    __syncthreads();
+    unsigned failed = 0;
+    for (int q = threadIdx.x; q < nbound;) {  // df(), DF.cpp:78-124
+        double V[3], w, jacob;
+        node_vel(n0 + s_list[q], V, w, jacob);
+        const double H = .5 * (V[0] * V[0] + V[1] * V[1] + V[2] * V[2]) + Phi;
+        unsigned fail = 0;
+        double Jr, Jz;
+        fudge_actions(P, deltafn(s_Eg, s_Dg, m.ngrid, H), R, z, Phi, V[0], V[1], V[2], gl, Jr, Jz, fail);
+        double DF = df_value(m.df, P, R, Jr, Jz, R * V[1], fail);
+        if (fail & (kFailBracket | kFailRoot)) DF = 0.;
+        failed += fail ? 1u : 0u;
+        s_df[q] = DF;
+        q = atomicAdd(s_next, 1);
+    }
+    __syncthreads();
+    double sum = 0;  // fixed order: thread t adds list entries t, t + kLosBlock, ..
+    for (int q = threadIdx.x; q < nbound; q += kLosBlock) {
+        double V[3], w, jacob;
+        node_vel(n0 + s_list[q], V, w, jacob);
+        sum += w * (jacob * s_df[q]);
+    }
     const double ws = los_warp_sum(sum);
-    if (lane == 0) s_red[warp] = ws;
-    const int nb = __syncthreads_count(bound);
-    const int nf = __syncthreads_count(failed);
+    unsigned nfw = failed;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nfw += __shfl_xor_sync(0xffffffffu, nfw, o);
+    if (lane == 0) { s_red[warp] = ws; s_wc[warp] = (int)nfw; }
+    __syncthreads();
     if (threadIdx.x == 0) {
         double s = 0;
-        for (int q = 0; q < kLosBlock / 32; q++) s += s_red[q];
+        unsigned nf = 0;
+        for (int q = 0; q < kLosBlock / 32; q++) { s += s_red[q]; nf += (unsigned)s_wc[q]; }
         a.partial[blockIdx.x] = s;
         if (a.m.counters) {
-            if (nb) atomicAdd(&a.m.counters[0], (unsigned long long)nb);
+            if (nbound) atomicAdd(&a.m.counters[0], (unsigned long long)nbound);
             if (nf) atomicAdd(&a.m.counters[1], (unsigned long long)nf);
         }
     }
@@ -176,7 +225,8 @@ int los_blocks_per_item(int kind, int nq)
 size_t los_smem_bytes(const MomentArgs &m)
 {
     const size_t nt = (size_t)m.P.nr * m.P.npoly;
-    return (m.P.nr + 4 * nt + 2 * m.ngrid + 2 * m.nq + 2 * m.gl.n + kLosBlock / 32) * sizeof(double);
+    return (m.P.nr + 4 * nt + 2 * m.ngrid + 2 * m.nq + 2 * m.gl.n + kLosBlock / 32 + kLosChunk) * sizeof(double) +
+           kLosChunk * (sizeof(float) + sizeof(unsigned short)) + (kLosBlock / 32 + 1) * sizeof(int);
 }
 
 size_t los_local_bytes()
