@@ -12,6 +12,7 @@ FJ_DF_DPL, FJ_DF_QUASIISO = 0, 1
 FJ_PREC_FP64, FJ_PREC_MIXED = 0, 1
 FJ_TWOCOMP_SUMMED, FJ_TWOCOMP_REFERENCE = 0, 1
 FJ_JQUAD_QAGS = 0
+FJ_POISSON_QAGS, FJ_POISSON_CUMULATIVE = 0, 1
 FJ_GUESS = {"Hernquist": 0, "Isochrone": 1, "NFW": 2, "NFWext": 3}
 
 
@@ -35,7 +36,8 @@ class fj_quad_rule(C.Structure):
 
 class fj_moment_stats(C.Structure):
     _fields_ = [("nodes", C.c_longlong), ("bound", C.c_longlong), ("failures", C.c_longlong),
-                ("kernel_ms", C.c_double), ("escalated", C.c_longlong)]
+                ("kernel_ms", C.c_double), ("escalated", C.c_longlong), ("fail_quad", C.c_longlong),
+                ("fail_bracket", C.c_longlong), ("fail_root", C.c_longlong), ("resolved64", C.c_longlong)]
 
 
 class fj_batch_item(C.Structure):
@@ -113,6 +115,9 @@ SIGNATURES = {
     "fj_legendre_project": ([CTX, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "fj_poisson": ([CTX, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "fj_poisson_noalloc": ([C.c_int, C.c_int] + [C.c_void_p] * 6, C.c_int),
+    "fj_set_poisson": ([CTX, C.c_int], C.c_int),
+    "fj_get_poisson": ([CTX, P(C.c_int)], C.c_int),
+    "fj_poisson_noalloc_stack": ([P(C.c_size_t), P(C.c_size_t)], C.c_int),
     "fj_sum_potentials": ([CTX, C.c_int] + [C.c_void_p] * 9, C.c_int),
     "fj_compute_new_phi": ([CTX, P(fj_potential), P(fj_delta_table), P(fj_df_params), P(fj_quad_rule), C.c_int,
                             C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, P(fj_moment_stats)], C.c_int),

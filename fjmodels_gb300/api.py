@@ -282,6 +282,17 @@ class Context:
     def set_mixed_config(self, variant, nodes_per_block):
         self._check(self.lib.fj_set_mixed_config(self.h, variant, nodes_per_block), "fj_set_mixed_config")
 
+    def set_poisson(self, mode):
+        """Radial integrals of every Poisson solve on this context: A.FJ_POISSON_QAGS (the
+        reference's adaptive quadrature, the default) or A.FJ_POISSON_CUMULATIVE (exact
+        interval integrals of the same integrands, prefix-summed)."""
+        self._check(self.lib.fj_set_poisson(self.h, mode), "fj_set_poisson")
+
+    def poisson(self):
+        m = C.c_int()
+        self._check(self.lib.fj_get_poisson(self.h, C.byref(m)), "fj_get_poisson")
+        return m.value
+
     def mixed_config(self):
         v, c = C.c_int(), C.c_int()
         self._check(self.lib.fj_get_mixed_config(self.h, C.byref(v), C.byref(c)), "fj_get_mixed_config")

@@ -41,6 +41,7 @@ struct fj_ctx {
     std::vector<double> rule_host;                     // last uploaded velocity rule
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int mixed_variant = 0, mixed_chunk = kMixedMaxNodes;  // mixed kernel configuration (fj_autotune_mixed)
+    int poisson = FJ_POISSON_QAGS;                     // radial integrals of fj_poisson (fj_set_poisson)
     float *jout = nullptr;                             // mixed form: actions of every bound node (fj_set_action_output)
     DevBuf batch;                                      // batched launch: MomentArgs[n] | block_start | point_start
     std::vector<char> batch_host;                      // what `batch` holds (re-uploaded only when it changes)
@@ -256,16 +257,20 @@ int build_args(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta
 
 int read_stats(fj_ctx *ctx, long long nodes, fj_moment_stats *stats)
 {
-    unsigned long long h[4];
+    unsigned long long h[kNumCounters];
     FJ_CUDA(cudaMemcpyAsync(h, ctx->counters.p, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
     FJ_CUDA(cudaStreamSynchronize(ctx->stream));
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     stats->nodes = nodes;
-    stats->bound = (long long)h[0];
-    stats->failures = (long long)h[1];
+    stats->bound = (long long)h[kCntBound];
+    stats->failures = (long long)h[kCntFailed];
     stats->kernel_ms = ms;
-    stats->escalated = (long long)h[3];
+    stats->escalated = (long long)h[kCntEscalated];
+    stats->fail_quad = (long long)h[kCntFailQuad];
+    stats->fail_bracket = (long long)h[kCntFailBracket];
+    stats->fail_root = (long long)h[kCntFailRoot];
+    stats->resolved64 = (long long)h[kCntResolved64];
     return FJ_OK;
 }
 
@@ -278,7 +283,7 @@ int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delt
     int rc = build_args(ctx, pot, delta, df, rule, ngauss, Rz, npts, out6, a, mixed);
     if (rc) return rc;
     if ((rc = ensure(ctx, ctx->partial, (size_t)npts * a.blocks_per_point * 6 * sizeof(double)))) return rc;
-    if ((rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long)))) return rc;
+    if ((rc = ensure(ctx, ctx->counters, kNumCounters * sizeof(unsigned long long)))) return rc;
     a.partial = (double *)ctx->partial.p;
     a.counters = (unsigned long long *)ctx->counters.p;
     const long long nq3 = (long long)rule->nq * rule->nq * rule->nq;
@@ -286,7 +291,7 @@ int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delt
         a.jout = ctx->jout;
         FJ_CUDA(cudaMemsetAsync(a.jout, 0xFF, (size_t)npts * nq3 * 2 * sizeof(float), ctx->stream));
     }
-    FJ_CUDA(cudaMemsetAsync(a.counters, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    FJ_CUDA(cudaMemsetAsync(a.counters, 0, kNumCounters * sizeof(unsigned long long), ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     FJ_CUDA(mixed ? launch_moments_mixed(a, ctx->mixed_variant, ctx->stream) : launch_moments(a, ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
@@ -431,7 +436,7 @@ int fj_moments_batch(fj_ctx *ctx, int n, const fj_batch_item *items, const fj_qu
     }
     int rc;
     if ((rc = ensure(ctx, ctx->partial, partial * sizeof(double)))) return rc;
-    if ((rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long)))) return rc;
+    if ((rc = ensure(ctx, ctx->counters, kNumCounters * sizeof(unsigned long long)))) return rc;
     for (int m = 0; m < n; m++) {
         args[m].partial = (double *)ctx->partial.p + reinterpret_cast<size_t>(args[m].partial);
         args[m].counters = (unsigned long long *)ctx->counters.p;
@@ -451,7 +456,7 @@ int fj_moments_batch(fj_ctx *ctx, int n, const fj_batch_item *items, const fj_qu
     const char *db = (const char *)ctx->batch.p;
     const MomentBatch b{(const MomentArgs *)db, (const int *)(db + n * sizeof(MomentArgs)),
                         (const int *)(db + n * sizeof(MomentArgs) + (n + 1) * sizeof(int)), n};
-    FJ_CUDA(cudaMemsetAsync(ctx->counters.p, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    FJ_CUDA(cudaMemsetAsync(ctx->counters.p, 0, kNumCounters * sizeof(unsigned long long), ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     FJ_CUDA(launch_moments_batch(args[0], b, bs[n], smem, mixed, ctx->mixed_variant, ctx->stream));
     FJ_CUDA(launch_moments_finalize_batch(b, ps[n], ctx->stream));
@@ -524,9 +529,29 @@ int fj_poisson(fj_ctx *ctx, int nr, int npoly, const double *ar, const double *r
 {
     if (!ctx || nr < 2 || npoly < 1 || npoly > kMaxPoly || !ar || !rhl || !phil || !Pr || !Pr2)
         return fail(ctx, FJ_ERR_ARG, "poisson: bad arguments");
-    int rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long));
+    if (ctx->poisson == FJ_POISSON_CUMULATIVE) {
+        if (nr > kPoissonCumulativeMaxNr) return fail(ctx, FJ_ERR_ARG, "poisson: too many radii");
+        FJ_CUDA(launch_poisson_cumulative(nr, npoly, ar, rhl, phil, Pr, Pr2, ctx->stream));
+        return FJ_OK;
+    }
+    int rc = ensure(ctx, ctx->counters, kNumCounters * sizeof(unsigned long long));
     if (rc) return rc;
     FJ_CUDA(launch_poisson(nr, npoly, ar, rhl, phil, Pr, Pr2, (unsigned long long *)ctx->counters.p, ctx->stream));
+    return FJ_OK;
+}
+
+int fj_set_poisson(fj_ctx *ctx, int mode)
+{
+    if (!ctx || (mode != FJ_POISSON_QAGS && mode != FJ_POISSON_CUMULATIVE))
+        return fail(ctx, FJ_ERR_ARG, "set_poisson: unknown mode");
+    ctx->poisson = mode;
+    return FJ_OK;
+}
+
+int fj_get_poisson(fj_ctx *ctx, int *mode)
+{
+    if (!ctx || !mode) return FJ_ERR_ARG;
+    *mode = ctx->poisson;
     return FJ_OK;
 }
 
@@ -621,7 +646,7 @@ int fj_los(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, co
     bool mixed = false;
     int rc = build_args(ctx, pot, delta, df, rule, 0, Rzv, n, out, a.m, mixed);
     if (rc) return rc;
-    if ((rc = ensure(ctx, ctx->counters, 4 * sizeof(unsigned long long)))) return rc;
+    if ((rc = ensure(ctx, ctx->counters, kNumCounters * sizeof(unsigned long long)))) return rc;
     a.m.counters = (unsigned long long *)ctx->counters.p;
     a.rhl = rhl; a.kind = kind; a.Rzv = Rzv; a.n = n; a.out = out;
     fj_tanh_sinh01(a.x01, a.w01);
@@ -629,7 +654,7 @@ int fj_los(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delta, co
     if ((long long)n * a.blocks_per_item > 0x7fffffffLL) return fail(ctx, FJ_ERR_ARG, "los: too many values");
     if ((rc = ensure(ctx, ctx->partial, (size_t)n * a.blocks_per_item * sizeof(double)))) return rc;
     a.partial = (double *)ctx->partial.p;
-    FJ_CUDA(cudaMemsetAsync(ctx->counters.p, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    FJ_CUDA(cudaMemsetAsync(ctx->counters.p, 0, kNumCounters * sizeof(unsigned long long), ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     FJ_CUDA(launch_los(a, ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
@@ -714,9 +739,16 @@ extern "C" int fj_tabulate_delta(const fj_potential *pot, int ngrid, double *Egr
             Dgrid[nE] = delta_energy(P, base, nE, ngrid, Egrid[nE], fits[t], b, kDeltaWalkCapHost);
         if (b) bad[t] = 1;
     };
+    // a share whose thread cannot be started runs on the calling thread (no
+    // exception crosses the C ABI)
     std::vector<std::thread> pool;
-    for (int t = 1; t < nthreads; t++) pool.emplace_back(work, t);
+    int started = 1;
+    try {
+        for (; started < nthreads; started++) pool.emplace_back(work, started);
+    } catch (...) {
+    }
     work(0);
+    for (int t = started; t < nthreads; t++) work(t);
     for (auto &th : pool) th.join();
     for (char b : bad)
         if (b) return FJ_ERR_ARG;

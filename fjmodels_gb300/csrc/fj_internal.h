@@ -12,6 +12,15 @@ struct fj_quad_rule;
 namespace fj {
 
 constexpr int kMomentBlock = 128;  // threads per block of the phase-space kernel
+// Device counters of one call (fj_moment_stats): nodes with H < 0, nodes whose
+// action solve still hit a cap (any kind), Poisson integrals that hit theirs,
+// nodes whose turning points ran in FP64 (mixed form), the final failures by
+// kind (a node can count in several), and mixed-form nodes re-solved by the
+// plain FP64 solve because their FP32 solve hit a cap.
+enum : int {
+    kCntBound = 0, kCntFailed = 1, kCntPoisson = 2, kCntEscalated = 3,
+    kCntFailQuad = 4, kCntFailBracket = 5, kCntFailRoot = 6, kCntResolved64 = 7, kNumCounters = 8
+};
 constexpr int kPlainChunk = 1024;  // velocity nodes of one point per block (FP64 form)
 // per-thread stack the kernels need: the QAGS interval list (kQagsCap entries
 // of four doubles and an int), the epsilon table and the call frames
@@ -36,7 +45,7 @@ struct MomentArgs {
     int mixed_chunk;         // mixed form: nodes per block (<= kMixedMaxNodes)
     float *jout;             // mixed form, optional: (Jr, Jz) of every bound node [npts][nq^3][2]
     double *partial;         // [npts][blocks_per_point][6]
-    unsigned long long *counters;  // [0] bound nodes, [1] failed nodes, [3] FP64 escalations
+    unsigned long long *counters;  // [kNumCounters], the slots below
     double *out6;            // [6][npts]
 };
 
@@ -76,6 +85,35 @@ struct MomentBatch {
     const int *block_start, *point_start;
     int n;
 };
+
+// per-node status tallies of one thread: nodes with any cap, and by kind
+struct FailTally {
+    unsigned any = 0, quad = 0, bracket = 0, root = 0;
+    __device__ __forceinline__ void add(unsigned fail)
+    {
+        any += fail ? 1u : 0u;
+        quad += (fail & kFailQuad) ? 1u : 0u;
+        bracket += (fail & kFailBracket) ? 1u : 0u;
+        root += (fail & kFailRoot) ? 1u : 0u;
+    }
+};
+
+// adds a warp's values of v to *ctr (one atomic per warp, none for a zero sum);
+// every lane of the warp must call it
+__device__ __forceinline__ void warp_count(unsigned long long *ctr, unsigned v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(ctr, (unsigned long long)v);
+}
+
+__device__ __forceinline__ void warp_count_fails(unsigned long long *counters, const FailTally &t)
+{
+    warp_count(&counters[kCntFailed], t.any);
+    warp_count(&counters[kCntFailQuad], t.quad);
+    warp_count(&counters[kCntFailBracket], t.bracket);
+    warp_count(&counters[kCntFailRoot], t.root);
+}
 
 // the model of block (or point) `i` of a batch: largest m with start[m] <= i
 __device__ __forceinline__ int batch_model(const int *start, int n, int i)
@@ -119,6 +157,11 @@ cudaError_t launch_project(int nr, int ngauss, int npoly, const double *ar, cons
 constexpr int kPoissonCap = 256;
 cudaError_t launch_poisson(int nr, int npoly, const double *ar, const double *rhl, double *phil,
                            double *Pr, double *Pr2, unsigned long long *counters, cudaStream_t s);
+// Poisson with the radial integrals taken exactly over the linear interpolation
+// of the density multipoles (prefix sums, no adaptive quadrature): one block per l
+constexpr int kPoissonCumulativeMaxNr = 4096;
+cudaError_t launch_poisson_cumulative(int nr, int npoly, const double *ar, const double *rhl, double *phil,
+                                      double *Pr, double *Pr2, cudaStream_t s);
 cudaError_t launch_sum3(int n, const double *a0, const double *a1, const double *a2, const double *b0,
                         const double *b1, const double *b2, double *o0, double *o1, double *o2, cudaStream_t s);
 // o = a + b elementwise (summed component densities)
@@ -141,5 +184,6 @@ cudaError_t launch_gemm_tc(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 
 size_t moments_local_bytes();
 size_t moments_mixed_local_bytes();
 size_t multipole_local_bytes();
+size_t poisson_local_bytes();  // per-thread local memory (stack) of the Poisson kernel
 
 }  // namespace fj

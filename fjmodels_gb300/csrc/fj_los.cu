@@ -194,8 +194,8 @@ __global__ void __launch_bounds__(kLosBlock) k_los(LosArgs a)
         for (int q = 0; q < kLosBlock / 32; q++) { s += s_red[q]; nf += (unsigned)s_wc[q]; }
         a.partial[blockIdx.x] = s;
         if (a.m.counters) {
-            if (nbound) atomicAdd(&a.m.counters[0], (unsigned long long)nbound);
-            if (nf) atomicAdd(&a.m.counters[1], (unsigned long long)nf);
+            if (nbound) atomicAdd(&a.m.counters[kCntBound], (unsigned long long)nbound);
+            if (nf) atomicAdd(&a.m.counters[kCntFailed], (unsigned long long)nf);
         }
     }
 }

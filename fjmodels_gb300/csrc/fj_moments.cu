@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(kMomentBlock) k_moments(MomentArgs a0, MomentB
     }
     sort_list(s_list, s_key, nbound);
     // the solves, nodes taken as threads free up
-    unsigned failed = 0;
+    FailTally tally;
     for (int q = threadIdx.x; q < nbound;) {
         const int node = n0 + s_list[q];
         double V0, V1, V2;
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(kMomentBlock) k_moments(MomentArgs a0, MomentB
         fudge_actions(P, deltafn(s_Eg, s_Dg, a.ngrid, H), R, z, Phi_h, V0, V1, V2, gl, Jr, Jz, fail);
         double DF = df_value(a.df, P, R, Jr, Jz, R * V1, fail);
         if (fail & (kFailBracket | kFailRoot)) DF = 0.;
-        failed += fail ? 1u : 0u;
+        tally.add(fail);
         s_df[q] = DF;
         q = atomicAdd(s_next, 1);
     }
@@ -150,16 +150,14 @@ __global__ void __launch_bounds__(kMomentBlock) k_moments(MomentArgs a0, MomentB
         const double v = warp_sum(m[q]);
         if (lane == 0) s_red[warp * 6 + q] = v;
     }
-    const unsigned nf = __syncthreads_count(failed);
+    warp_count_fails(a.counters, tally);
+    __syncthreads();
     if (threadIdx.x < 6) {
         double s = 0;
         for (int w = 0; w < kMomentBlock / 32; w++) s += s_red[w * 6 + threadIdx.x];
         a.partial[((size_t)p * B + chunk) * 6 + threadIdx.x] = s;
     }
-    if (threadIdx.x == 0) {
-        if (nbound) atomicAdd(&a.counters[0], (unsigned long long)nbound);
-        if (nf) atomicAdd(&a.counters[1], (unsigned long long)nf);
-    }
+    if (threadIdx.x == 0 && nbound) atomicAdd(&a.counters[kCntBound], (unsigned long long)nbound);
 }
 
 // sums the per-block partials of each point and normalises as rhofDF does

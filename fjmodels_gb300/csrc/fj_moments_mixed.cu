@@ -148,8 +148,14 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
     const double jacob = Ve * Ve * Ve;
 
     double m[6] = {0, 0, 0, 0, 0, 0};
-    unsigned failed = 0, esc = 0;
-    // one node's solve; returns the DF that enters the moments
+    unsigned esc = 0, resolved = 0;
+    FailTally tally;
+    // one node's solve; returns the DF that enters the moments.  A node whose
+    // FP32 solve hits a cap (a full QAGS list, a bracket walk or Brent at its
+    // step limit) is solved again by the plain form's FP64 solve (QAGS lists of
+    // kQagsCap intervals); only what that solve still caps is counted as a
+    // failure, with the plain form's policy (a capped bracket or root: DF 0; a
+    // full QAGS list: the estimate so far, as QUADPACK returns it).
     auto solve = [&](int q) {
         const int node = n0 + s_list[q];
         const int i = node / nq2, j = (node / nq) % nq, k = node % nq;
@@ -158,14 +164,21 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
         unsigned fail = 0, e = 0;
         const double Delta = deltafn(s_Eg, s_Dg, a.ngrid, H);
         double J[2];
-        const double f = mixed_node_df(P, PF, *sK, a.df, Delta, R, z, Phi_h, V0, V1, V2, fail, e, J);
+        double f = mixed_node_df(P, PF, *sK, a.df, Delta, R, z, Phi_h, V0, V1, V2, fail, e, J);
+        if (fail) {
+            fail = 0;
+            const GLRule qags{0, nullptr, nullptr};
+            fudge_actions(P, Delta, R, z, Phi_h, V0, V1, V2, qags, J[0], J[1], fail);
+            f = df_value(a.df, P, R, J[0], J[1], R * V1, fail);
+            resolved++;
+        }
         if (a.jout) {
             float *jo = a.jout + ((size_t)p * nq3 + node) * 2;
             jo[0] = (float)J[0];
             jo[1] = (float)J[1];
         }
         esc += e;
-        failed += fail ? 1u : 0u;
+        tally.add(fail);
         return (fail & (kFailBracket | kFailRoot)) ? 0. : f;
     };
     auto accumulate = [&](int q, double DF) {
@@ -199,26 +212,16 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
         for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
         if (lane == 0) s_red[warp * 6 + q] = v;
     }
-    unsigned nf = failed, ne = esc;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        nf += __shfl_xor_sync(0xffffffffu, nf, off);
-        ne += __shfl_xor_sync(0xffffffffu, ne, off);
-    }
-    if (lane == 0) s_wc[warp] = (int)nf;
+    warp_count_fails(a.counters, tally);
+    warp_count(&a.counters[kCntEscalated], esc);
+    warp_count(&a.counters[kCntResolved64], resolved);
     __syncthreads();
     if (threadIdx.x < 6) {
         double s = 0;
         for (int w = 0; w < kMixedBlock / 32; w++) s += s_red[w * 6 + threadIdx.x];
         a.partial[((size_t)p * B + chunk) * 6 + threadIdx.x] = s;
     }
-    if (threadIdx.x == 0) {
-        unsigned nfb = 0;
-        for (int w = 0; w < kMixedBlock / 32; w++) nfb += (unsigned)s_wc[w];
-        if (nbound) atomicAdd(&a.counters[0], (unsigned long long)nbound);
-        if (nfb) atomicAdd(&a.counters[1], (unsigned long long)nfb);
-    }
-    if (lane == 0 && ne) atomicAdd(&a.counters[3], (unsigned long long)ne);
+    if (threadIdx.x == 0 && nbound) atomicAdd(&a.counters[kCntBound], (unsigned long long)nbound);
 }
 
 namespace {

@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(32 * kPoissonWarps) k_poisson(int nr, int npol
         epsabs *= 2; epsrel *= 2; tries++;
     }
     if (lane != 0) return;
-    if (fail && counters) atomicAdd(&counters[2], 1ull);
+    if (fail && counters) atomicAdd(&counters[kCntPoisson], 1ull);
     const double r = ar[n];
     const double G = 1;
     phil[t] = -kTPI * G * (Iint / pow(r, l + 1) + Iext * pow(r, l));
@@ -161,6 +161,79 @@ cudaError_t launch_poisson(int nr, int npoly, const double *ar, const double *rh
     const int nt = nr * npoly;
     k_poisson<<<(nt + kPoissonWarps - 1) / kPoissonWarps, 32 * kPoissonWarps, 0, s>>>(nr, npoly, ar, rhl, phil, Pr,
                                                                                       Pr2, counters);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------- exact cumulative Poisson solve
+// The integrals of computeInts (pot/Potential.cpp:82-155) taken exactly: the
+// integrands are x^(l+2) rho_l(x) and rho_l(x) x^(1-l) with rho_l the linear
+// interpolation of the density multipoles (linterp, include/Utils.h:122-128:
+// constant below ar[0]) and rho_l(x) = max(0, rho_l[nr-1] (ar[nr-1]/x)^4)
+// beyond the grid (Potential.cpp:90-99), so each grid interval contributes a
+// closed form and the integrals are prefix sums over the intervals, added in
+// a fixed order.  No adaptive decisions: the potential is a smooth function of
+// the density, where the reference's QAGS (epsabs 1e-4, epsrel 1e-3) moves it
+// by up to ~1e-3 when a small change of the density flips a subdivision.
+// One block per multipole l, a thread per interval, then one thread per radius.
+
+// int_a^b x^m (c0 + c1 x) dx
+__device__ __forceinline__ double seg_power_integral(double a, double b, int m, double c0, double c1)
+{
+    const double t0 = m == -1 ? log(b / a) : (pow(b, m + 1) - pow(a, m + 1)) / (m + 1);
+    const double t1 = m == -2 ? log(b / a) : (pow(b, m + 2) - pow(a, m + 2)) / (m + 2);
+    return c0 * t0 + c1 * t1;
+}
+
+__global__ void k_poisson_cumulative(int nr, int npoly, const double *ar, const double *rhl, double *phil,
+                                     double *Pr, double *Pr2)
+{
+    extern __shared__ double sh[];
+    double *s_in = sh, *s_ex = sh + nr;  // interval i = [ar[i], ar[i+1]] (s_in[nr-1]: [0, ar[0]]; s_ex[nr-1]: tail)
+    const int np = blockIdx.x, l = 2 * np;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+        if (i < nr - 1) {
+            const double a = ar[i], b = ar[i + 1], ya = rhl[i * npoly + np], yb = rhl[(i + 1) * npoly + np];
+            const double s = (yb - ya) / (b - a), c0 = ya - s * a;
+            s_in[i] = seg_power_integral(a, b, l + 2, c0, s);
+            s_ex[i] = seg_power_integral(a, b, 1 - l, c0, s);
+        } else {
+            const double a0 = ar[0], R = ar[nr - 1], yN = rhl[(nr - 1) * npoly + np];
+            s_in[i] = rhl[np] * pow(a0, l + 3) / (l + 3);
+            s_ex[i] = (yN > 0 ? yN : 0.) * pow(R, 2 - l) / (l + 2);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {  // prefix sums in place: s_in[n] = I_int(ar[n]), s_ex[n] = I_ext(ar[n])
+        double acc = s_in[nr - 1], seg = s_in[0];
+        s_in[0] = acc;
+        for (int n = 1; n < nr; n++) {
+            acc += seg;
+            seg = s_in[n];
+            s_in[n] = acc;
+        }
+        acc = s_ex[nr - 1];
+        for (int n = nr - 1; n >= 0; n--) {
+            const double cur = n < nr - 1 ? s_ex[n] : 0.;
+            if (n < nr - 1) acc += cur;
+            s_ex[n] = acc;
+        }
+    }
+    __syncthreads();
+    for (int n = threadIdx.x; n < nr; n += blockDim.x) {  // computePhil (Potential.cpp:163-200)
+        const double r = ar[n], Ii = s_in[n], Ie = s_ex[n], G = 1;
+        const int t = n * npoly + np;
+        phil[t] = -kTPI * G * (Ii / pow(r, l + 1) + Ie * pow(r, l));
+        Pr[t] = -kTPI * G * (-(l + 1) * Ii / pow(r, l + 2) + l * Ie * pow(r, l - 1));
+        Pr2[t] = -kTPI * G * ((l + 2) * (l + 1) * Ii / pow(r, l + 3) + (l - 1) * l * Ie * pow(r, l - 2) -
+                              (2 * l + 1) * rhl[t]);
+    }
+}
+
+cudaError_t launch_poisson_cumulative(int nr, int npoly, const double *ar, const double *rhl, double *phil,
+                                      double *Pr, double *Pr2, cudaStream_t s)
+{
+    if (nr < 2 || nr > kPoissonCumulativeMaxNr) return cudaErrorInvalidValue;
+    k_poisson_cumulative<<<npoly, 128, 2 * nr * sizeof(double), s>>>(nr, npoly, ar, rhl, phil, Pr, Pr2);
     return cudaGetLastError();
 }
 
@@ -290,6 +363,12 @@ cudaError_t launch_vir2(PotView P, int ngauss, const double *ci, const double *w
 {
     k_vir2<<<1, kVirBlock, 0, s>>>(P, ngauss, ci, wi, coef6, out7);
     return cudaGetLastError();
+}
+
+size_t poisson_local_bytes()
+{
+    cudaFuncAttributes at;
+    return cudaFuncGetAttributes(&at, k_poisson) == cudaSuccess ? at.localSizeBytes : 0;
 }
 
 size_t multipole_local_bytes()

@@ -7,8 +7,8 @@
  *     stores coefficient l=2*np at radius ar[n] in t[n*npoly+np]; a
  *     [nr][ngauss] meridional grid stores point (ar[n], cos theta_g) in
  *     g[n*ngauss+g].  The reference keeps the same matrices as row-pointer
- *     double** (include/Utils.h:71-75); fj_rows_to_flat / fj_flat_to_rows in
- *     INTEGRATION.md adapt them.
+ *     double** (include/Utils.h:71-75); a row-pointer matrix is adapted by
+ *     copying its rows into (or out of) one contiguous buffer.
  *   - "device" pointers are CUDA global-memory pointers on the context's
  *     device; "host" pointers are ordinary memory.  Every call is ordered on
  *     the context's stream and returns after its work is queued unless the
@@ -16,8 +16,9 @@
  *   - Return value: FJ_OK (0) or an FJ_ERR_* code; the reference's exit(n)
  *     paths become error codes (fj_last_error gives the text).  Per-node
  *     numerical failures (a capped bracket, Brent or QAGS limit) never abort:
- *     the node's DF contributes 0, as the reference's NaN guard does
- *     (df/DF.cpp:105), and the count is reported in fj_moment_stats.
+ *     a capped bracket or root makes the node's DF contribute 0, as the
+ *     reference's NaN guard does (df/DF.cpp:105); a full QAGS list keeps the
+ *     integral's estimate so far; the counts are reported in fj_moment_stats.
  *   - One context per host thread; calls on one context are not re-entrant.
  */
 #ifndef FJGPU_H
@@ -97,9 +98,15 @@ typedef struct fj_quad_rule {
 typedef struct fj_moment_stats {
     long long nodes;     /* phase-space evaluations (grid points x nq^3) */
     long long bound;     /* nodes with H < 0 */
-    long long failures;  /* nodes whose action solve hit a cap */
+    long long failures;  /* nodes whose action solve hit a cap (after any FP64 re-solve) */
     double kernel_ms;    /* device time of the phase-space kernel (CUDA events) */
     long long escalated; /* FJ_PREC_MIXED: nodes whose turning points were solved in FP64 */
+    /* failures by kind (a node can count in more than one): a momentum
+       integral's QAGS list full (its estimate so far is kept, as QUADPACK
+       returns it), a bracket walk or Brent at its step cap (the DF counts 0) */
+    long long fail_quad, fail_bracket, fail_root;
+    long long resolved64; /* FJ_PREC_MIXED: nodes whose FP32 solve hit a cap and were
+                             solved again by the plain FP64 solve */
 } fj_moment_stats;
 
 /* ---------------------------------------------------------------- context */
@@ -268,12 +275,34 @@ int fj_poisson(fj_ctx *ctx, int nr, int npoly, const double *ar, const double *r
    latency-bound loop).  The quadrature workspace lives in the kernel's
    shared memory.  Inputs and outputs are device pointers on the current
    device, work is queued on `stream` (a cudaStream_t; NULL = legacy default
-   stream); calls on different streams are independent.
-   FJ_POISSON_NOALLOC_MAX_COEFS is kept for source compatibility: any
-   nr*npoly that fj_poisson accepts is accepted. */
-#define FJ_POISSON_NOALLOC_MAX_COEFS 1024
+   stream); calls on different streams are independent.  Any nr >= 2 and
+   1 <= npoly <= 24 is accepted.  The kernel's per-thread stack must fit the
+   device's current stack limit (CUDA's default 1024 bytes does): otherwise
+   the call returns FJ_ERR_NOMEM without launching, since the launch would
+   make the driver enlarge the local-memory reservation. */
 int fj_poisson_noalloc(int nr, int npoly, const double *ar, const double *rhl, double *phil,
                        double *Pr, double *Pr2, void *stream);
+/* The per-thread stack (bytes) fj_poisson_noalloc's kernel needs, and the
+   current device's per-thread stack limit (cudaLimitStackSize); either
+   pointer may be NULL.  No counterpart in the reference. */
+int fj_poisson_noalloc_stack(size_t *need, size_t *limit);
+
+/* How fj_poisson (and every call that solves the Poisson equation on the
+   context: fj_compute_new_phi, the model loops) takes the radial integrals:
+     FJ_POISSON_QAGS        the reference's adaptive QAGS / QAGIU with its
+                            tolerances and retry rule (the default; parity);
+     FJ_POISSON_CUMULATIVE  the same integrands (the linear interpolation of
+                            the density multipoles, the r^-4 tail beyond the
+                            grid) integrated exactly, interval by interval,
+                            as prefix sums in a fixed order (nr <= 4096).
+   The adaptive form's answer moves by up to ~1e-3 of the potential when a
+   small change of the density flips one of its subdivision decisions; the
+   cumulative form is a smooth function of the density, so a self-consistent
+   loop can converge below that level.  No counterpart in the reference. */
+#define FJ_POISSON_QAGS 0
+#define FJ_POISSON_CUMULATIVE 1
+int fj_set_poisson(fj_ctx *ctx, int mode);
+int fj_get_poisson(fj_ctx *ctx, int *mode);
 
 /* updatePhil (pot/potLeg.cpp:21-29): out = a + b element-wise on the three
    tables (device [nr*npoly] each). */

@@ -75,6 +75,10 @@ void orc_project6(int nr, int ngauss, int npoly, const double *ar, double *grids
 /* Poisson solve (Potential.cpp:110-200): rhl -> phil, Pr, Pr2 */
 void orc_compute_phil(int nr, int npoly, const double *ar, const double *rhl, double *phil,
                       double *Pr, double *Pr2);
+/* the same solve with the radial integrals taken without adaptive
+   quadrature (Gauss-Legendre per grid interval, running sums) */
+void orc_compute_phil_cumulative(int nr, int npoly, const double *ar, const double *rhl, double *phil,
+                                 double *Pr, double *Pr2);
 /* guess density multipoles (Potential.cpp:63-80): kind 0 Hernquist, 1 Isochrone, 2 NFW */
 void orc_guess_rhl(int nr, int ngauss, int npoly, const double *ar, int kind, double mass,
                    double r0, double q, double *rhl);

@@ -88,6 +88,7 @@ def lib():
         L.orc_moment_grid.argtypes = [M, C.c_int, C.c_int, DP, C.c_int, S]
         L.orc_project6.argtypes = [C.c_int, C.c_int, C.c_int, DP, DP, DP]
         L.orc_compute_phil.argtypes = [C.c_int, C.c_int, DP, DP, DP, DP, DP]
+        L.orc_compute_phil_cumulative.argtypes = [C.c_int, C.c_int, DP, DP, DP, DP, DP]
         L.orc_guess_rhl.argtypes = [C.c_int, C.c_int, C.c_int, DP, C.c_int, C.c_double, C.c_double,
                                     C.c_double, DP]
         L.orc_vir2.argtypes = [M, DP, DP]
@@ -250,12 +251,15 @@ def project6(ar, ngauss, npoly, grids6):
     return coef, g
 
 
-def compute_phil(ar, rhl):
+def compute_phil(ar, rhl, cumulative=False):
+    """Poisson solve: the reference's adaptive QAGS/QAGIU, or (cumulative=True) the same
+    integrands integrated interval by interval without adaptivity."""
     ar = _f64(ar)
     rhl = _f64(rhl)
     nr, npoly = rhl.shape
     phil, Pr, Pr2 = np.zeros((nr, npoly)), np.zeros((nr, npoly)), np.zeros((nr, npoly))
-    lib().orc_compute_phil(nr, npoly, _p(ar), _p(rhl), _p(phil), _p(Pr), _p(Pr2))
+    fn = lib().orc_compute_phil_cumulative if cumulative else lib().orc_compute_phil
+    fn(nr, npoly, _p(ar), _p(rhl), _p(phil), _p(Pr), _p(Pr2))
     return phil, Pr, Pr2
 
 

@@ -737,6 +737,64 @@ void orc_compute_phil(int nr, int npoly, const double *ar, const double *rhl, do
     free(rhl_h);
 }
 
+/* The same integrands as computeInts (pot/Potential.cpp:82-155: x^(l+2)
+   linterp(rho_l) inside, linterp(rho_l) / x^(l-1) outside with the
+   max(0, rho_N (R/x)^4) tail) integrated without adaptivity: each grid
+   interval by a 24-point Gauss-Legendre rule (exact for the polynomial
+   integrands inside; to rounding for the negative powers outside, whose
+   intervals span a small ratio of radii), [0, ar[0]] the same way with
+   rho = rhl[0] (linterp's clamp), the tail in closed form; running sums
+   from the centre (internal) and from the tail (external). */
+void orc_compute_phil_cumulative(int nr, int npoly, const double *ar, const double *rhl, double *phil,
+                                 double *Pr, double *Pr2)
+{
+    enum { NGL = 24 };
+    double xg[NGL], wg[NGL];
+    orc_gauleg(0, 1, NGL, xg, wg);
+    double *Iint = malloc(sizeof(double) * nr), *Iext = malloc(sizeof(double) * nr);
+    for (int np = 0; np < npoly; np++) {
+        const int l = 2 * np;
+        double acc = 0;
+        for (int k = 0; k < NGL; k++) {
+            const double x = ar[0] * xg[k];
+            acc += ar[0] * wg[k] * pow(x, l + 2) * rhl[np];
+        }
+        Iint[0] = acc;
+        for (int n = 1; n < nr; n++) {
+            const double a = ar[n - 1], b = ar[n], ya = rhl[(n - 1) * npoly + np], yb = rhl[n * npoly + np];
+            double seg = 0;
+            for (int k = 0; k < NGL; k++) {
+                const double x = a + (b - a) * xg[k];
+                seg += (b - a) * wg[k] * pow(x, l + 2) * (ya + (x - a) / (b - a) * (yb - ya));
+            }
+            acc += seg;
+            Iint[n] = acc;
+        }
+        const double R = ar[nr - 1], yN = rhl[(nr - 1) * npoly + np];
+        acc = MAX(0., yN) * pow(R, 2 - l) / (l + 2);
+        Iext[nr - 1] = acc;
+        for (int n = nr - 2; n >= 0; n--) {
+            const double a = ar[n], b = ar[n + 1], ya = rhl[n * npoly + np], yb = rhl[(n + 1) * npoly + np];
+            double seg = 0;
+            for (int k = 0; k < NGL; k++) {
+                const double x = a + (b - a) * xg[k];
+                seg += (b - a) * wg[k] * (ya + (x - a) / (b - a) * (yb - ya)) / pow(x, l - 1);
+            }
+            acc += seg;
+            Iext[n] = acc;
+        }
+        for (int n = 0; n < nr; n++) {
+            const double r = ar[n], G = 1;
+            phil[n * npoly + np] = -TPI * G * (Iint[n] / pow(r, l + 1) + Iext[n] * pow(r, l));
+            Pr[n * npoly + np] = -TPI * G * (-(l + 1) * Iint[n] / pow(r, l + 2) + l * Iext[n] * pow(r, l - 1));
+            Pr2[n * npoly + np] = -TPI * G * ((l + 2) * (l + 1) * Iint[n] / pow(r, l + 3) +
+                                              (l - 1) * l * Iext[n] * pow(r, l - 2) - (2 * l + 1) * rhl[n * npoly + np]);
+        }
+    }
+    free(Iint);
+    free(Iext);
+}
+
 /* ---------------- guess densities (pot/models.cpp:40-56; Potential.cpp:63-80) ---------------- */
 static double guess_rho(int kind, double mass, double r0, double q, double R, double z)
 {

@@ -90,3 +90,57 @@ def test_fudge_actions_in_the_isochrone_potential():
         Jr, Jz = m.actions(R, z, vR, vp, vz, Delta=0.01)
         assert abs(Jr - Jr_an) < 1e-3 * (Jr_an + L), (R, z, vR, vp, vz, Jr, Jr_an)
         assert abs(Jz + abs(R * vp) - L) < 1e-3 * (Jr_an + L), (R, z, vR, vp, vz, Jz, L)
+
+
+def test_cumulative_poisson_second_order_to_analytic_hernquist():
+    """The cumulative solve integrates the interpolated density exactly, so its error
+    against Phi = -M/(r + r0) is the interpolation's: it falls ~4x per doubling of the
+    grid, where the adaptive solve stalls near its tolerance (epsabs 1e-4, epsrel 1e-3)."""
+    errs, errs_qags = [], []
+    for nr in (200, 400, 800):
+        ar = O.log_grid(1e-3, 1000.0, nr)
+        rhl = O.guess_rhl(ar, 8, 1, "Hernquist")
+        an = -1 / (ar + 1)
+        m = ar > 0.01
+        cum = O.compute_phil(ar, rhl, cumulative=True)[0][:, 0]
+        qg = O.compute_phil(ar, rhl)[0][:, 0]
+        errs.append(np.max(np.abs(cum[m] - an[m]) / np.abs(an[m])))
+        errs_qags.append(np.max(np.abs(qg[m] - an[m]) / np.abs(an[m])))
+    assert 3.5 < errs[0] / errs[1] < 4.5 and 3.5 < errs[1] / errs[2] < 4.5, errs
+    assert errs[2] < 4e-4 and errs_qags[2] > 1.5 * errs[2], (errs, errs_qags)
+
+
+def test_cumulative_poisson_agrees_with_adaptive_to_its_tolerance():
+    ar = O.log_grid(1e-3, 300.0, 80)
+    for model in ("Hernquist", "NFW"):
+        rhl = O.guess_rhl(ar, 40, 7, model)
+        a = O.compute_phil(ar, rhl)[0]
+        b = O.compute_phil(ar, rhl, cumulative=True)[0]
+        d = np.max(np.abs(a - b) / np.abs(b[:, :1]))
+        assert 1e-5 < d < 5e-3, (model, d)
+
+
+def _header_numbers(path):
+    import re
+    txt = open(path).read()
+    body = txt[txt.index("{"):]
+    return np.array([float(x) for x in re.findall(r"-?\d+\.\d+(?:e-?\d+)?", body)])
+
+
+def test_rk8pd_tableau_order_conditions_and_tables():
+    """The Prince & Dormand RK8(7) tableau (the reference's orbit stepper, delta/Delta.cpp:
+    59-60): row sums and every Butcher order condition (200 trees to order 8 for the
+    8th-order weights, to order 7 for the embedded ones) hold to the rounding of its
+    published rationals; the oracle's table and the library's table agree exactly."""
+    import importlib.util
+    import os
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("rk8pd_tableau", os.path.join(root, "oracle", "rk8pd_tableau.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    rows, d8, d7, d78 = mod.check()
+    assert rows < 1e-16 and d8 < 1e-15 and d7 < 1e-15 and d78 > 1e-6
+    a = _header_numbers(os.path.join(root, "oracle", "orc_rk8pd.h"))
+    b = _header_numbers(os.path.join(root, "fjmodels_gb300", "csrc", "fj_rk8pd.h"))
+    assert a.shape == b.shape == (13 + 13 * 12 + 13 + 13,) and np.array_equal(a, b)
+
