@@ -1,12 +1,14 @@
 // fj_delta.cuh -- the focal-distance table: tabulateDelta (delta/tabulate.cpp:
 // 13-38) and the Delta class (delta/Delta.cpp), as host and device code.
-// Orbits use an extrapolated modified-midpoint step (Bulirsch-Stoer) under
-// the y-error step control of the reference's integrator setup (abs 1e-10,
-// rel 1e-9, Delta.cpp:59-69).  One energy of the table is independent of the
+// Orbits use the reference's stepper, the Runge-Kutta 8(7) pair of Prince &
+// Dormand (gsl_odeiv2_step_rk8pd, Delta.cpp:59-60; fj_rk8pd.h), under the
+// y-error step control of its integrator setup (abs 1e-10, rel 1e-9,
+// Delta.cpp:59-69).  One energy of the table is independent of the
 // others (delta_energy): the host loops over them, the batched kernel gives
 // each (model, energy) pair a thread.
 #pragma once
 #include "fj_device.cuh"
+#include "fj_rk8pd.h"
 
 namespace fj {
 
@@ -30,29 +32,37 @@ FJ_HD void orbit_rhs(const DeltaFit &d, const double *y, double *f)
     f[3] = -dz;
 }
 
-FJ_HDNI void gbs_step(const DeltaFit &d, double h, const double *y0, double *y1, double *yerr)
+FJ_HD const RK8PDTab &rk8pd_tab()
 {
-    constexpr int K = 6;
-    double T[K][4], prev[4] = {0, 0, 0, 0}, dy0[4];
-    orbit_rhs(d, y0, dy0);  // the same first derivative for every sequence
-    for (int k = 0; k < K; k++) {
-        const int ns = 2 * (k + 1);
-        const double hs = h / ns;
-        double zm[4], zc[4], dy[4];
-        for (int i = 0; i < 4; i++) { zm[i] = y0[i]; zc[i] = y0[i] + hs * dy0[i]; }
-        for (int s = 1; s < ns; s++) {
-            orbit_rhs(d, zc, dy);
-            for (int i = 0; i < 4; i++) { const double zn = zm[i] + 2 * hs * dy[i]; zm[i] = zc[i]; zc[i] = zn; }
+#ifdef __CUDA_ARCH__
+    return kRK8PD_d;
+#else
+    return kRK8PD_h;
+#endif
+}
+
+// One RK8(7) step: y1 from the 8th-order weights, yerr = h sum (b8 - b7) k
+FJ_HDNI void rk8pd_step(const DeltaFit &d, double h, const double *y0, double *y1, double *yerr)
+{
+    const RK8PDTab &T = rk8pd_tab();
+    double k[13][4], ys[4];
+    for (int st = 0; st < 13; st++) {
+        for (int i = 0; i < 4; i++) {
+            double acc = 0;
+            for (int j = 0; j < st; j++) acc += T.a[st][j] * k[j][i];
+            ys[i] = y0[i] + h * acc;
         }
-        orbit_rhs(d, zc, dy);
-        for (int i = 0; i < 4; i++) T[k][i] = 0.5 * (zm[i] + zc[i] + hs * dy[i]);
-        for (int j = k - 1; j >= 0; j--) {
-            const double r = (double)(k + 1) / (double)(j + 1), fac = r * r - 1.0;
-            for (int i = 0; i < 4; i++) T[j][i] = T[j + 1][i] + (T[j + 1][i] - T[j][i]) / fac;
-        }
-        if (k == K - 2) for (int i = 0; i < 4; i++) prev[i] = T[0][i];
+        orbit_rhs(d, ys, k[st]);
     }
-    for (int i = 0; i < 4; i++) { y1[i] = T[0][i]; yerr[i] = T[0][i] - prev[i]; }
+    for (int i = 0; i < 4; i++) {
+        double s8 = 0, se = 0;
+        for (int st = 0; st < 13; st++) {
+            s8 += T.b8[st] * k[st][i];
+            se += (T.b8[st] - T.b7[st]) * k[st][i];
+        }
+        y1[i] = y0[i] + h * s8;
+        yerr[i] = h * se;
+    }
 }
 
 FJ_HDNI bool evolve_step(const DeltaFit &d, double &t, double t1, double &h, double *y)
@@ -63,7 +73,7 @@ FJ_HDNI bool evolve_step(const DeltaFit &d, double &t, double t1, double &h, dou
     if (h0 > t1 - t) { h0 = t1 - t; final = true; }
     double y1[4], yerr[4];
     for (int tries = 0; tries < 200; tries++) {
-        gbs_step(d, h0, y, y1, yerr);
+        rk8pd_step(d, h0, y, y1, yerr);
         double rmax = 0;
         for (int i = 0; i < 4; i++) {
             const double D0 = epsrel * fabs(y1[i]) + epsabs;

@@ -14,8 +14,9 @@
  *   - Piessens, de Doncker-Kapenga, Ueberhuber, Kahaner, "QUADPACK" (1983):
  *     DQAGSE with DQK21, DQPSRT and DQELG; QAGIU as DQAGSE applied to
  *     f(a+(1-t)/t)/t^2 on (0,1] with the 15-point Kronrod rule;
- *   - Bulirsch & Stoer (1966) extrapolated modified-midpoint step with the
- *     y-error step-size controller described in the GSL manual (odeiv2).
+ *   - the Runge-Kutta 8(7) pair of Prince & Dormand (1981), RK8(7)13M (the
+ *     stepper the reference names, gsl_odeiv2_step_rk8pd), with the y-error
+ *     step-size controller described in the GSL manual (odeiv2).
  */
 #include <float.h>
 #include <math.h>
@@ -25,6 +26,7 @@
 #include "fjoracle.h"
 #include "orc_internal.h"
 #include "orc_kronrod.h"
+#include "orc_rk8pd.h"
 
 /* Gauss-Legendre nodes on [x1,x2] (UtilsLeg.h:18-39, NGAUSS replaced by n). */
 void orc_gauleg(double x1, double x2, int n, double *x, double *w)
@@ -491,39 +493,33 @@ int orc_qagiu(orc_fn f, void *p, double a, double epsabs, double epsrel, int lim
 }
 
 /* ------------------------------------------------------------------------
- * Orbit integrator for the focal-distance tabulation.
- * One "step" is a Bulirsch-Stoer extrapolated modified-midpoint step with
- * substep counts 2,4,...,2*ORC_GBS_K; the error estimate is the difference of
- * the last two diagonal extrapolants.  The controller follows the GSL manual's
- * standard y-error control with the step order of an 8th-order method.
+ * Orbit integrator for the focal-distance tabulation (delta/Delta.cpp:53-90).
+ * One step is the 13-stage RK8(7) pair of Prince & Dormand (orc_rk8pd.h,
+ * generated from the published tableau by rk8pd_tableau.py, which checks its
+ * order conditions): y1 from the 8th-order weights, the error estimate from
+ * the difference of the 8th- and 7th-order weights.  The controller follows
+ * the GSL manual's standard y-error control with the method's order 8.
  * ---------------------------------------------------------------------- */
-#define ORC_GBS_K 6
-
-static void gbs_step(orc_rhs rhs, void *p, double t, double h, const double *y0, double *y1,
-                     double *yerr)
+static void rk8pd_step(orc_rhs rhs, void *p, double t, double h, const double *y0, double *y1, double *yerr)
 {
-    double T[ORC_GBS_K][4];
-    for (int k = 0; k < ORC_GBS_K; k++) {
-        int ns = 2 * (k + 1);
-        double hs = h / ns, zm[4], zc[4], zn[4], dy[4];
-        rhs(t, y0, dy, p);
-        for (int i = 0; i < 4; i++) { zm[i] = y0[i]; zc[i] = y0[i] + hs * dy[i]; }
-        for (int s = 1; s < ns; s++) {
-            rhs(t + s * hs, zc, dy, p);
-            for (int i = 0; i < 4; i++) { zn[i] = zm[i] + 2 * hs * dy[i]; zm[i] = zc[i]; zc[i] = zn[i]; }
+    double k[RK8PD_STAGES][4], ys[4];
+    for (int st = 0; st < RK8PD_STAGES; st++) {
+        for (int i = 0; i < 4; i++) {
+            double acc = 0;
+            for (int j = 0; j < st; j++) acc += rk8pd_a[st][j] * k[j][i];
+            ys[i] = y0[i] + h * acc;
         }
-        rhs(t + h, zc, dy, p);
-        for (int i = 0; i < 4; i++) T[k][i] = 0.5 * (zm[i] + zc[i] + hs * dy[i]);
-        /* Aitken-Neville in h^2 */
-        for (int j = k - 1; j >= 0; j--) {
-            double r = (double)(k + 1) / (double)(j + 1);
-            double fac = r * r - 1.0;
-            for (int i = 0; i < 4; i++) T[j][i] = T[j + 1][i] + (T[j + 1][i] - T[j][i]) / fac;
-        }
-        if (k == ORC_GBS_K - 2)
-            for (int i = 0; i < 4; i++) yerr[i] = T[0][i];
+        rhs(t + rk8pd_c[st] * h, ys, k[st], p);
     }
-    for (int i = 0; i < 4; i++) { y1[i] = T[0][i]; yerr[i] = T[0][i] - yerr[i]; }
+    for (int i = 0; i < 4; i++) {
+        double s8 = 0, se = 0;
+        for (int st = 0; st < RK8PD_STAGES; st++) {
+            s8 += rk8pd_b8[st] * k[st][i];
+            se += (rk8pd_b8[st] - rk8pd_b7[st]) * k[st][i];
+        }
+        y1[i] = y0[i] + h * s8;
+        yerr[i] = h * se;
+    }
 }
 
 int orc_evolve_apply(orc_rhs rhs, void *p, double *t, double t1, double *h, double *y,
@@ -535,7 +531,7 @@ int orc_evolve_apply(orc_rhs rhs, void *p, double *t, double t1, double *h, doub
     if (h0 > dt) { h0 = dt; final = 1; }
     double y1[4], yerr[4];
     for (int tries = 0; tries < 200; tries++) {
-        gbs_step(rhs, p, *t, h0, y, y1, yerr);
+        rk8pd_step(rhs, p, *t, h0, y, y1, yerr);
         double rmax = 0;
         for (int i = 0; i < 4; i++) {
             double D0 = epsrel * fabs(y1[i]) + epsabs;

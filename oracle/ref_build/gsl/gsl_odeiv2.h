@@ -1,5 +1,5 @@
 /* GSL stand-in (test infrastructure): adaptive ODE evolution interface.  The
-   "rk8pd" stepper is a stand-in extrapolation stepper (see gsl_standin.c). */
+   "rk8pd" stepper is the RK8(7) pair of Prince & Dormand (see gsl_standin.c). */
 #ifndef FJREF_GSL_ODEIV2_H
 #define FJREF_GSL_ODEIV2_H
 #include <stddef.h>

@@ -3,8 +3,9 @@
  * calls (GSL itself is absent from this machine).  TEST INFRASTRUCTURE ONLY:
  * it lets the reference's own sources compile, unmodified, into oracle/_ref.
  * The algorithms are the oracle's restatements of the published methods
- * (orc_numerics.c): Brent steps, QUADPACK QAGS/QAGIU and an extrapolated
- * modified-midpoint stepper under GSL's documented y-error step control.
+ * (orc_numerics.c): Brent steps, QUADPACK QAGS/QAGIU and the RK8(7) pair of
+ * Prince & Dormand (the method gsl_odeiv2_step_rk8pd names) under GSL's
+ * documented y-error step control.
  */
 #include <stdlib.h>
 #include "gsl/gsl_errno.h"

@@ -15,6 +15,12 @@
  * guess density multipoles.
  * FJREF_DELTA_FILE, when set, names a file with a focal-distance table
  * (Egrid then Dgrid) used instead of tabulateDelta.
+ *
+ * A parameter file with a second component runs the reference's two-component
+ * loop instead (twoComp, fJmodels.cpp:38-81, in its own order: component 1's
+ * moments in the total potential, whose own new potential then replaces the
+ * total, component 2's in that, total = the sum) and dumps each component's
+ * matrices and the total potential per iteration; the points file is unused.
  */
 #include <cstdio>
 #include <cstdlib>
@@ -44,6 +50,7 @@ double ** __restrict phil, ** __restrict Pr, ** __restrict Pr2,
 FILE * __restrict f_lz;
 
 static FILE *out;
+extern unsigned components;  // io/readParam.cpp:16
 static void dumpv(const char *name, const double *v, int n)
 {
     fprintf(out, "%s %d\n", name, n);
@@ -54,6 +61,59 @@ static void dumpm(const char *name, double **m, int nx, int ny)
     fprintf(out, "%s %d\n", name, nx * ny);
     for (int i = 0; i < nx; i++)
         for (int j = 0; j < ny; j++) fprintf(out, "%.17g\n", m[i][j]);
+}
+
+static int two_components(struct fJParams fJP)
+{
+    double **rhl2 = mat<double>(NR, NPOLY), **vrotl2 = mat<double>(NR, NPOLY), **sigRl2 = mat<double>(NR, NPOLY),
+           **sigpl2 = mat<double>(NR, NPOLY), **sigzl2 = mat<double>(NR, NPOLY), **sigRzl2 = mat<double>(NR, NPOLY);
+    SetModel(fJP, 1);
+    Potential p(1);
+    p.selectGuessRho(fJP.modName != "null" ? fJP.modName : "Hernquist");
+    p.computeGuessRhl();
+    p.computePhil(p.rhlP);
+    SetModel(fJP, 2);
+    Potential p2(2);
+    p2.selectGuessRho(fJP.modName2 != "null" ? fJP.modName2 : "Hernquist");
+    p2.computeGuessRhl();
+    p2.computePhil(p2.rhlP);
+    updatePhil(&p, &p2);
+    dumpm("c1_guess_rhl", p.rhlP, NR, NPOLY);
+    dumpm("c2_guess_rhl", p2.rhlP, NR, NPOLY);
+    dumpm("guess_phil", phil, NR, NPOLY);
+    dumpm("guess_Pr", Pr, NR, NPOLY);
+    dumpm("guess_Pr2", Pr2, NR, NPOLY);
+    const char *dfile = getenv("FJREF_DELTA_FILE");
+    if (dfile) {
+        FILE *df = fopen(dfile, "r");
+        for (int i = 0; i < NGRID; i++) if (fscanf(df, "%lf", &Egrid[i]) != 1) return 3;
+        for (int i = 0; i < NGRID; i++) if (fscanf(df, "%lf", &Dgrid[i]) != 1) return 3;
+        fclose(df);
+    } else tabulateDelta(&p);
+    dumpv("Egrid", Egrid, NGRID);
+    dumpv("Dgrid", Dgrid, NGRID);
+    fflush(out);
+    char nm[64];
+    for (int k = 0; k < fJP.itermax; k++) {
+        printf("\n Iter:%d\n", k);
+        setDF(&fJP, &p, 1);
+        computeNewPhi(&p, rhl, sigRl, sigpl, sigzl, sigRzl, vrotl);
+        setDF(&fJP, &p, 2);
+        computeNewPhi(&p2, rhl2, sigRl2, sigpl2, sigzl2, sigRzl2, vrotl2);
+        updatePhil(&p, &p2);
+        double **m1[9] = {rhl, vrotl, sigRl, sigpl, sigzl, sigRzl, p.philP, p.PrP, p.Pr2P};
+        double **m2[9] = {rhl2, vrotl2, sigRl2, sigpl2, sigzl2, sigRzl2, p2.philP, p2.PrP, p2.Pr2P};
+        const char *names[9] = {"rhl", "vrotl", "sigRl", "sigpl", "sigzl", "sigRzl", "phil", "Pr", "Pr2"};
+        for (int q = 0; q < 9; q++) {
+            snprintf(nm, sizeof nm, "it%d_c1_%s", k, names[q]); dumpm(nm, m1[q], NR, NPOLY);
+            snprintf(nm, sizeof nm, "it%d_c2_%s", k, names[q]); dumpm(nm, m2[q], NR, NPOLY);
+        }
+        double **tot[3] = {phil, Pr, Pr2};
+        for (int q = 0; q < 3; q++) { snprintf(nm, sizeof nm, "it%d_%s", k, names[6 + q]); dumpm(nm, tot[q], NR, NPOLY); }
+        fflush(out);
+    }
+    fclose(out);
+    return 0;
 }
 
 int main(int argc, char **argv)
@@ -83,6 +143,7 @@ int main(int argc, char **argv)
         }
     }
     dumpv("ar", ar, NR);
+    if (components == 2) return two_components(fJP);
 
     SetModel(fJP);
     Potential p;

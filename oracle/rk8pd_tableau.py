@@ -1,0 +1,141 @@
+"""The Runge-Kutta 8(7) pair of Prince & Dormand (1981, "High order embedded
+Runge-Kutta formulae", J. Comput. Appl. Math. 7, 67-75; RK8(7)13M), the
+stepper the reference asks GSL for (delta/Delta.cpp:59-60,
+gsl_odeiv2_step_rk8pd).  Test infrastructure: the published tableau as exact
+rationals, a check of the Butcher order conditions, and the C table
+orc_rk8pd.h generated from it for the oracle and the GSL stand-in.
+
+    python oracle/rk8pd_tableau.py            # verify, then write orc_rk8pd.h
+"""
+import os
+from fractions import Fraction as Fr
+
+S = 13
+C = [Fr(0), Fr(1, 18), Fr(1, 12), Fr(1, 8), Fr(5, 16), Fr(3, 8), Fr(59, 400), Fr(93, 200),
+     Fr(5490023248, 9719169821), Fr(13, 20), Fr(1201146811, 1299019798), Fr(1), Fr(1)]
+A = [[Fr(0)] * S for _ in range(S)]
+_rows = {
+    1: {0: Fr(1, 18)},
+    2: {0: Fr(1, 48), 1: Fr(1, 16)},
+    3: {0: Fr(1, 32), 2: Fr(3, 32)},
+    4: {0: Fr(5, 16), 2: Fr(-75, 64), 3: Fr(75, 64)},
+    5: {0: Fr(3, 80), 3: Fr(3, 16), 4: Fr(3, 20)},
+    6: {0: Fr(29443841, 614563906), 3: Fr(77736538, 692538347), 4: Fr(-28693883, 1125000000),
+        5: Fr(23124283, 1800000000)},
+    7: {0: Fr(16016141, 946692911), 3: Fr(61564180, 158732637), 4: Fr(22789713, 633445777),
+        5: Fr(545815736, 2771057229), 6: Fr(-180193667, 1043307555)},
+    8: {0: Fr(39632708, 573591083), 3: Fr(-433636366, 683701615), 4: Fr(-421739975, 2616292301),
+        5: Fr(100302831, 723423059), 6: Fr(790204164, 839813087), 7: Fr(800635310, 3783071287)},
+    9: {0: Fr(246121993, 1340847787), 3: Fr(-37695042795, 15268766246), 4: Fr(-309121744, 1061227803),
+        5: Fr(-12992083, 490766935), 6: Fr(6005943493, 2108947869), 7: Fr(393006217, 1396673457),
+        8: Fr(123872331, 1001029789)},
+    10: {0: Fr(-1028468189, 846180014), 3: Fr(8478235783, 508512852), 4: Fr(1311729495, 1432422823),
+         5: Fr(-10304129995, 1701304382), 6: Fr(-48777925059, 3047939560), 7: Fr(15336726248, 1032824649),
+         8: Fr(-45442868181, 3398467696), 9: Fr(3065993473, 597172653)},
+    11: {0: Fr(185892177, 718116043), 3: Fr(-3185094517, 667107341), 4: Fr(-477755414, 1098053517),
+         5: Fr(-703635378, 230739211), 6: Fr(5731566787, 1027545527), 7: Fr(5232866602, 850066563),
+         8: Fr(-4093664535, 808688257), 9: Fr(3962137247, 1805957418), 10: Fr(65686358, 487910083)},
+    12: {0: Fr(403863854, 491063109), 3: Fr(-5068492393, 434740067), 4: Fr(-411421997, 543043805),
+         5: Fr(652783627, 914296604), 6: Fr(11173962825, 925320556), 7: Fr(-13158990841, 6184727034),
+         8: Fr(3936647629, 1978049680), 9: Fr(-160528059, 685178525), 10: Fr(248638103, 1413531060)},
+}
+for i, row in _rows.items():
+    for j, v in row.items():
+        A[i][j] = v
+B8 = [Fr(14005451, 335480064), 0, 0, 0, 0, Fr(-59238493, 1068277825), Fr(181606767, 758867731),
+      Fr(561292985, 797845732), Fr(-1041891430, 1371343529), Fr(760417239, 1151165299),
+      Fr(118820643, 751138087), Fr(-528747749, 2220607170), Fr(1, 4)]
+B7 = [Fr(13451932, 455176623), 0, 0, 0, 0, Fr(-808719846, 976000145), Fr(1757004468, 5645159321),
+      Fr(656045339, 265891186), Fr(-3867574721, 1518517206), Fr(465885868, 322736535),
+      Fr(53011238, 667516719), Fr(2, 45), 0]
+B8 = [Fr(x) for x in B8]
+B7 = [Fr(x) for x in B7]
+
+
+def trees(order):
+    """Rooted trees with `order` vertices, each a sorted tuple of child trees."""
+    memo = {1: [()]}
+
+    def gen(n):
+        if n in memo:
+            return memo[n]
+        out = set()
+
+        def parts(rem, maxt, acc):  # multisets of subtrees with total size rem, non-increasing
+            if rem == 0:
+                out.add(tuple(sorted(acc)))
+                return
+            for k in range(rem, 0, -1):
+                for t in gen(k):
+                    key = (k, t)
+                    if maxt is not None and key > maxt:
+                        continue
+                    parts(rem - k, key, acc + [t])
+
+        parts(n - 1, None, [])
+        memo[n] = sorted(out)
+        return memo[n]
+
+    return gen(order)
+
+
+def size(t):
+    return 1 + sum(size(c) for c in t)
+
+
+def gamma(t):
+    g = size(t)
+    for c in t:
+        g *= gamma(c)
+    return g
+
+
+def phi(t):
+    """Elementary weight vector: Phi_i(t) = prod over children of sum_j a_ij Phi_j(child)."""
+    v = [Fr(1)] * S
+    for c in t:
+        pc = phi(c)
+        for i in range(S):
+            v[i] *= sum(A[i][j] * pc[j] for j in range(S))
+    return v
+
+
+def max_defect(b, order):
+    worst = 0.0
+    for p in range(1, order + 1):
+        for t in trees(p):
+            d = abs(float(sum(bi * x for bi, x in zip(b, phi(t))) - Fr(1, gamma(t))))
+            worst = max(worst, d)
+    return worst
+
+
+def check():
+    rows = max(abs(float(sum(A[i]) - C[i])) for i in range(S))
+    assert sum(len(trees(p)) for p in range(1, 9)) == 200
+    d8, d7 = max_defect(B8, 8), max_defect(B7, 7)
+    # the published coefficients are rationals rounded to ~1e-18: conditions hold to that level
+    assert rows < 1e-16 and d8 < 1e-15 and d7 < 1e-15, (rows, d8, d7)
+    # the embedded pair differs at order 8 (else it could not estimate the error)
+    d78 = max_defect(B7, 8)
+    assert d78 > 1e-6, d78
+    return rows, d8, d7, d78
+
+
+def write_header(path):
+    def lit(x):
+        return repr(float(x))
+    lines = ["/* orc_rk8pd.h -- generated by oracle/rk8pd_tableau.py: the RK8(7)13M pair of",
+             "   Prince & Dormand (1981) as doubles (test infrastructure). */",
+             "#ifndef ORC_RK8PD_H", "#define ORC_RK8PD_H", f"#define RK8PD_STAGES {S}",
+             "static const double rk8pd_c[13] = {" + ", ".join(lit(x) for x in C) + "};",
+             "static const double rk8pd_a[13][12] = {"]
+    for i in range(S):
+        lines.append("    {" + ", ".join(lit(A[i][j]) for j in range(S - 1)) + "},")
+    lines += ["};", "static const double rk8pd_b8[13] = {" + ", ".join(lit(x) for x in B8) + "};",
+              "static const double rk8pd_b7[13] = {" + ", ".join(lit(x) for x in B7) + "};", "#endif", ""]
+    open(path, "w").write("\n".join(lines))
+
+
+if __name__ == "__main__":
+    print("row sums, order-8 defect, order-7 defect, embedded order-8 defect:", check())
+    write_header(os.path.join(os.path.dirname(os.path.abspath(__file__)), "orc_rk8pd.h"))

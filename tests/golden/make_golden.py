@@ -4,10 +4,10 @@ Builds oracle/_ref (the reference's unmodified C++ compiled against the GSL
 stand-in in oracle/ref_build) for small grids, runs it on seeded inputs and
 stores every dumped intermediate in tests/golden/<scenario>.npz, plus the
 coefficient file the reference's writeOut produced.  Needs the reference
-checkout (REF_DIR, default /root/reference); the fixtures it writes are
-committed so the tests never need the reference at run time.
+checkout, named by the REF_DIR environment variable; the fixtures it writes
+are committed so the tests never need the reference at run time.
 
-    python tests/golden/make_golden.py
+    REF_DIR=<reference checkout> python tests/golden/make_golden.py [scenario ...]
 """
 import os
 import subprocess
@@ -20,7 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 BUILD = os.path.join(ROOT, "oracle", "ref_build")
 REFBIN = os.path.join(ROOT, "oracle", "_ref")
-REF_DIR = os.environ.get("REF_DIR", "/root/reference")
+REF_DIR = os.environ.get("REF_DIR")
 
 PARAM = """itermax {itermax}
 model {model}
@@ -45,7 +45,29 @@ SCENARIOS = {
     "hern_qiso": dict(nr=12, ng=4, np=3, df="qiso", k=1.0, rmin=0.01, rmax=100.0,
                       p=dict(itermax=1, model="Hernquist", dphi_h=0.55, dz_h=0.55, dphi_g=1.0, dz_g=1.0,
                              chi=0.0, mass=1.0, r0=1.0)),
+    # the full 40 x 20, l <= 8 Hernquist configuration, five iterations from the guess
+    "c1_hern": dict(nr=40, ng=20, np=5, df="dpl", k=0.5, rmin=0.01, rmax=100.0,
+                    p=dict(itermax=5, model="Hernquist", dphi_h=0.55, dz_h=0.55, dphi_g=1.0, dz_g=1.0,
+                           chi=0.0, mass=1.0, r0=1.0)),
+    # the reference's two-component loop (twoComp, its own component order): a Hernquist bulge
+    # and a rotating NFW halo, two iterations
+    "twocomp_ref": dict(nr=12, ng=4, np=3, df="dpl", k=0.5, rmin=0.01, rmax=300.0,
+                        p=dict(itermax=2, model="Hernquist", dphi_h=0.7, dz_h=0.5, dphi_g=0.9, dz_g=0.6,
+                               chi=0.0, mass=0.1, r0=1.0),
+                        p2=dict(model="NFW", dphi_h=0.45, dz_h=0.8, dphi_g=0.55, dz_g=0.95, chi=1.0, mass=1.0,
+                                r0=10.0)),
 }
+
+PARAM2 = """2:model {model}
+2:h(J):dphi {dphi_h}
+2:h(J):dz {dz_h}
+2:g(J):dphi {dphi_g}
+2:g(J):dz {dz_g}
+2:chi {chi}
+2:mass {mass}
+2:r0 {r0}
+2:q 1.
+"""
 
 
 def points(seed):
@@ -110,7 +132,8 @@ def run(name, sc):
     exe = os.path.join(REFBIN, f"fjref_{sc['df']}_{tag}")
     with tempfile.TemporaryDirectory() as td:
         os.makedirs(os.path.join(td, "models"))
-        open(os.path.join(td, "param.txt"), "w").write(PARAM.format(**sc["p"]))
+        param = PARAM.format(**sc["p"]) + (PARAM2.format(**sc["p2"]) if "p2" in sc else "")
+        open(os.path.join(td, "param.txt"), "w").write(param)
         pts = points(abs(hash(name)) % 2**31 if False else sum(map(ord, name)))
         open(os.path.join(td, "points.txt"), "w").write(pts)
         env = dict(os.environ, FJREF_K=str(sc["k"]), OMP_NUM_THREADS=str(os.cpu_count()))
@@ -129,6 +152,8 @@ def run(name, sc):
 
 
 if __name__ == "__main__":
+    if not REF_DIR or not os.path.isdir(REF_DIR):
+        sys.exit("make_golden.py: set REF_DIR to the reference checkout")
     names = sys.argv[1:] or list(SCENARIOS)
     for n in names:
         run(n, SCENARIOS[n])

@@ -1,0 +1,106 @@
+"""Whole runs of the reference itself (golden fixtures from its own sources, built by
+oracle/ref_build) against the plain FP64 GPU form, through the C ABI:
+
+- the full first configuration: a Hernquist model on 40 log radii in [0.01, 100] x 20
+  polar nodes, even multipoles to l = 8, the reference's 22^3-node velocity rule, five
+  iterations from the analytic guess (fJmodels.cpp:86-144).  Each iteration is checked
+  from the reference's own input potential (no accumulation), and the five chained
+  iterations of fj_run_model against the reference's fifth;
+- the reference's two-component loop (twoComp, fJmodels.cpp:38-81) in its own
+  component order, two iterations.
+
+The focal-distance table is an input (the fixture's): the reference's fit of it is not
+continuous in rounding.  Gates: the density and potential multipoles within 1e-9 of the
+monopole of their shell (with the floor of rel_shells for the outermost, nearly empty
+shells), the virial ratio within the 6 printed decimals of the reference's vir2 line.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+import fjmodels_gb300 as F  # noqa: E402
+from fjmodels_gb300 import _abi as A  # noqa: E402
+from tests.conftest import load_golden  # noqa: E402
+from tests.test_gpu_parity import df_of, dev, host, rel_shells  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-9
+FIELDS = ((0, "rhl"), (2, "sigRl"), (3, "sigpl"), (4, "sigzl"), (5, "sigRzl"))
+
+
+def _check_coefs(coef, g, prefix, nr, npl, tol):
+    for q, key in FIELDS:
+        ref = g[prefix + key].reshape(nr, npl)
+        if q == 5:  # sigma_Rz from |m5|: compare on the scale of the dispersions
+            s = np.abs(g[prefix + "sigRl"].reshape(nr, npl)[:, :1]) + 1e-300
+            assert np.max(np.abs(coef[q] - ref) / s) < tol, key
+        else:
+            assert rel_shells(coef[q], ref) < tol, key
+    vr = g[prefix + "vrotl"].reshape(nr, npl)
+    s = np.abs(g[prefix + "sigpl"].reshape(nr, npl)[:, :1]) + 1e-300
+    assert np.max(np.abs(coef[1] - vr) / s) < 1e-7
+
+
+def test_c1_each_iteration_from_reference_potential(ctx):
+    g, meta, _ = load_golden("c1_hern")
+    nr, ng, npl = meta["nr"], meta["ng"], meta["np"]
+    assert (nr, ng, npl, meta["p"]["itermax"]) == (40, 20, 5, 5)
+    df = df_of(meta)
+    ar = dev(g["ar"])
+    delta = ctx.delta(dev(g["Egrid"]), dev(g["Dgrid"]))
+    for k in range(5):
+        src = "guess_" if k == 0 else f"it{k - 1}_"
+        tabs = [dev(g[src + t].reshape(nr, npl)) for t in ("phil", "Pr", "Pr2")]
+        pot = ctx.potential(ar, *tabs)
+        grids = torch.zeros((6, nr, ng), dtype=torch.float64, device="cuda")
+        coef = torch.zeros((6, nr, npl), dtype=torch.float64, device="cuda")
+        outs = [torch.zeros((nr, npl), dtype=torch.float64, device="cuda") for _ in range(3)]
+        st = ctx.computeNewPhi(pot, delta, df, F.Rule(), ng, grids, coef, *outs)
+        assert st.failures == 0 and st.nodes == nr * ng * 22 ** 3
+        _check_coefs(host(coef), g, f"it{k}_", nr, npl, TOL)
+        for o, t in zip(outs, ("phil", "Pr", "Pr2")):
+            assert rel_shells(host(o), g[f"it{k}_{t}"].reshape(nr, npl)) < TOL, (k, t)
+        # the reference prints vir2 (libs/Stats.cpp:12-41) after each iteration with %f
+        v = ctx.vir2(ctx.potential(ar, *outs), ng, coef)
+        wk = v["pot"] / (v["KRR"] + v["Kzz"])
+        assert abs(wk - g["vir2"][k][4]) <= 5.1e-7 + 1e-6 * abs(wk), (k, wk, g["vir2"][k][4])
+
+
+def test_c1_five_chained_iterations(ctx):
+    g, meta, _ = load_golden("c1_hern")
+    nr, ng, npl = meta["nr"], meta["ng"], meta["np"]
+    out = ctx.run_model(nr, ng, npl, meta["rmin"], meta["rmax"], df_of(meta), F.Rule(), itermax=5,
+                        delta_table=(g["Egrid"], g["Dgrid"]))
+    assert out["iterations"] == 5 and out["failures"] == 0
+    # five iterations pass the first's rounding-level differences (CUDA's exp/log/pow
+    # against the host's libm) through four Poisson solves and moment sweeps
+    assert rel_shells(out["coef6"][0], g["it4_rhl"].reshape(nr, npl)) < 5 * TOL
+    assert rel_shells(out["phil"], g["it4_phil"].reshape(nr, npl)) < 5 * TOL
+    K = out["vir7"][0] + out["vir7"][1]
+    assert abs(out["vir7"][4] / K - g["vir2"][4][4]) <= 5.1e-7 + 1e-6 * abs(g["vir2"][4][4])
+
+
+def _twocomp_dfs(meta):
+    p, q = meta["p"], meta["p2"]
+    c1 = F.DFParams(p["model"], p["dphi_h"], p["dz_h"], p["dphi_g"], p["dz_g"], p["chi"], p["mass"], p["r0"],
+                    k=meta["k"])
+    c2 = F.DFParams(q["model"], q["dphi_h"], q["dz_h"], q["dphi_g"], q["dz_g"], q["chi"], q["mass"], q["r0"],
+                    k=meta["k"])
+    return c1, c2
+
+
+@pytest.mark.parametrize("iters", [1, 2])
+def test_two_components_in_reference_order(ctx, iters):
+    g, meta, _ = load_golden("twocomp_ref")
+    nr, ng, npl = meta["nr"], meta["ng"], meta["np"]
+    c1, c2 = _twocomp_dfs(meta)
+    out = ctx.run_model(nr, ng, npl, meta["rmin"], meta["rmax"], c1, F.Rule(), itermax=iters,
+                        delta_table=(g["Egrid"], g["Dgrid"]), df2=c2, twocomp_order=A.FJ_TWOCOMP_REFERENCE)
+    assert out["iterations"] == iters and out["failures"] == 0
+    k = iters - 1
+    tol = TOL * iters  # the halo's step is chained on the bulge's (and iteration 2 on iteration 1)
+    _check_coefs(out["coef6"], g, f"it{k}_c1_", nr, npl, tol)
+    _check_coefs(out["coef6_2"], g, f"it{k}_c2_", nr, npl, 2 * tol)
+    for t in ("phil", "Pr"):
+        assert rel_shells(out[t], g[f"it{k}_{t}"].reshape(nr, npl)) < 2 * tol, t

@@ -123,3 +123,49 @@ def test_tanh_sinh_table_is_the_reference_table():
     x, w = O.tanh_sinh01()
     assert np.all(np.diff(x) > 0) and x[11] == 0.5 and abs(w.sum() - 1) < 4e-5  # the table stops at k = 10 and -11
     assert np.allclose(x[1:] + x[:0:-1], 1, atol=2e-12)
+
+
+def test_two_component_reference_order_matches_reference():
+    """The reference's two-component loop (twoComp, fJmodels.cpp:38-81), first iteration:
+    component 1's moments in the total guess potential; its own potential, which replaces
+    the total (Potential.cpp:182-188); component 2's moments in that; the total potential
+    the sum of the two (updatePhil, potLeg.cpp:21-29).  The oracle composes the same
+    sequence from its one-component pieces."""
+    g, meta, _ = load_golden("twocomp_ref")
+    nr, ng, npl = meta["nr"], meta["ng"], meta["np"]
+    p, p2 = meta["p"], meta["p2"]
+    ar = g["ar"]
+    r1 = O.guess_rhl(ar, ng, npl, p["model"], p["mass"], p["r0"])
+    r2 = O.guess_rhl(ar, ng, npl, p2["model"], p2["mass"], p2["r0"])
+    assert rel_rows(r1, g["c1_guess_rhl"].reshape(nr, npl)) < 1e-14
+    assert rel_rows(r2, g["c2_guess_rhl"].reshape(nr, npl)) < 1e-14
+    total = [a + b for a, b in zip(O.compute_phil(ar, r1), O.compute_phil(ar, r2))]
+    for a, key in zip(total, ("guess_phil", "guess_Pr", "guess_Pr2")):
+        assert rel_rows(a, g[key].reshape(nr, npl)) < 1e-13, key
+    m1 = oracle_model(g, meta, *total)
+    grids, st = m1.moment_grid()
+    assert st["failures"] == 0
+    c1, _ = O.project6(ar, ng, npl, grids)
+    pot1 = O.compute_phil(ar, c1[0].reshape(nr, npl))
+    meta2 = dict(meta, p=p2)
+    for a, key in zip(pot1, ("phil", "Pr", "Pr2")):
+        assert rel_rows(a, g["it0_c1_" + key].reshape(nr, npl)) < 1e-11, key
+    for q, key in ((0, "rhl"), (2, "sigRl"), (3, "sigpl"), (4, "sigzl")):
+        assert rel_rows(c1[q], g["it0_c1_" + key].reshape(nr, npl)) < 1e-12, key
+    # component 2's step on its own: its moments in the reference's component-1 potential
+    ref_pot1 = [g["it0_c1_" + k].reshape(nr, npl) for k in ("phil", "Pr", "Pr2")]
+    grids2, st2 = oracle_model(g, meta2, *ref_pot1).moment_grid()
+    assert st2["failures"] == 0
+    c2, _ = O.project6(ar, ng, npl, grids2)
+    for q, key in ((0, "rhl"), (2, "sigRl"), (3, "sigpl"), (4, "sigzl")):
+        assert rel_rows(c2[q], g["it0_c2_" + key].reshape(nr, npl)) < 1e-12, key
+    pot2 = O.compute_phil(ar, c2[0].reshape(nr, npl))
+    for a, b, key in zip(ref_pot1, pot2, ("phil", "Pr", "Pr2")):
+        assert rel_rows(a + b, g["it0_" + key].reshape(nr, npl)) < 1e-11, key
+    # the whole chain from the oracle's own component-1 potential, which differs from the
+    # reference's at 1e-12 (moment sums in OpenMP order): the halo's adaptive quadrature
+    # passes that on at up to ~1e-10
+    grids2c, _ = oracle_model(g, meta2, *pot1).moment_grid()
+    c2c, _ = O.project6(ar, ng, npl, grids2c)
+    for q, key in ((0, "rhl"), (2, "sigRl"), (3, "sigpl"), (4, "sigzl")):
+        assert rel_rows(c2c[q], g["it0_c2_" + key].reshape(nr, npl)) < 5e-10, key
