@@ -745,12 +745,38 @@ void orc_compute_phil(int nr, int npoly, const double *ar, const double *rhl, do
    intervals span a small ratio of radii), [0, ar[0]] the same way with
    rho = rhl[0] (linterp's clamp), the tail in closed form; running sums
    from the centre (internal) and from the tail (external). */
+/* Gauss-Legendre nodes and weights on (0,1) to full double precision (Newton
+   on the Legendre recurrence until the step stops shrinking; the reference's
+   gauleg stops at 3e-11 with pi = 3.141592654, too coarse for this check) */
+static void gauleg_full(int n, double *x, double *w)
+{
+    for (int i = 0; i < (n + 1) / 2; i++) {
+        double z = cos(M_PI * (i + 0.75) / (n + 0.5)), pp = 0, dz = 1;
+        for (int it = 0; it < 100; it++) {
+            double p1 = 1, p2 = 0;
+            for (int j = 0; j < n; j++) {
+                const double p3 = p2;
+                p2 = p1;
+                p1 = ((2 * j + 1) * z * p2 - j * p3) / (j + 1);
+            }
+            pp = n * (z * p1 - p2) / (z * z - 1);
+            const double step = p1 / pp;
+            z -= step;
+            if (fabs(step) >= fabs(dz) && fabs(step) < 1e-14) break;
+            dz = step;
+        }
+        x[i] = 0.5 * (1 - z);
+        x[n - 1 - i] = 0.5 * (1 + z);
+        w[i] = w[n - 1 - i] = 1 / ((1 - z * z) * pp * pp);
+    }
+}
+
 void orc_compute_phil_cumulative(int nr, int npoly, const double *ar, const double *rhl, double *phil,
                                  double *Pr, double *Pr2)
 {
     enum { NGL = 24 };
     double xg[NGL], wg[NGL];
-    orc_gauleg(0, 1, NGL, xg, wg);
+    gauleg_full(NGL, xg, wg);
     double *Iint = malloc(sizeof(double) * nr), *Iext = malloc(sizeof(double) * nr);
     for (int np = 0; np < npoly; np++) {
         const int l = 2 * np;
