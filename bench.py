@@ -48,9 +48,10 @@ sys.path.insert(0, ROOT)
 CFG = dict(model="NFW", nr=80, ngauss=40, npoly=7, rmin=1e-3, rmax=300.0, dphi_h=0.55, dz_h=0.55, dphi_g=1.0,
            dz_g=1.0, chi=1.0, k=0.5, mass=1.0, r0=1.0, nq=22, tol=1e-5, itermax=100)
 # iterations this workload needs to converge (measured on the GB300: the change falls
-# by ~0.55 per iteration and is 6.2e-6 after the 20th); the reference arm times one
-# iteration of the reference's algorithm and multiplies by it
-ITERS_TO_CONVERGE = 20
+# by ~0.55 per iteration and is 7.8e-6 after the 19th); the reference arm, which cannot
+# iterate to convergence in minutes, times one iteration of the reference's algorithm and
+# multiplies by it
+ITERS_TO_CONVERGE = 19
 METRIC = "wall-s per converged model at rho err<=1e-4, chosen vs plain FP64, same GB300"
 UNIT = "s/model"
 # FP64 operations per phase-space evaluation executed by active threads of the
@@ -77,6 +78,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--form", default="mixed", choices=["mixed", "plain"])
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison step")
+    ap.add_argument("--poisson", default="cumulative", choices=["cumulative", "qags"],
+                    help="radial Poisson integrals: cumulative (exact over the interpolated density, the chosen "
+                         "form) or qags (the reference's adaptive quadrature, which does not let the loop converge)")
     ap.add_argument("--converged-plain", action="store_true",
                     help="also run the plain FP64 form to convergence and compare the converged models (minutes)")
     ap.add_argument("--mixed-config", default=None,
@@ -195,10 +199,13 @@ def df_params(F):
                       CFG["r0"], k=CFG["k"])
 
 
+POISSON = {"mode": "cumulative"}
+
+
 def new_context(F, index):
     from fjmodels_gb300 import _abi as A
     ctx = F.Context(index)
-    ctx.set_poisson(A.FJ_POISSON_CUMULATIVE)
+    ctx.set_poisson(A.FJ_POISSON_CUMULATIVE if POISSON["mode"] == "cumulative" else A.FJ_POISSON_QAGS)
     return ctx
 
 
@@ -290,7 +297,8 @@ def run_ours(args, rank, world):
         "vs_baseline": None, "dtype": "f32+f64" if fp32 else "f64",
         "data": "synthetic (analytic NFW guess density, seeded by construction)",
         "config": {"workload": WORKLOAD, "l2": L2_NOTE},
-        "form": FORM_TEXT[args.form], "parallelism": f"replicas{world}",
+        "form": FORM_TEXT[args.form] + ("" if args.poisson == "cumulative" else " (adaptive QAGS Poisson solve)"),
+        "parallelism": f"replicas{world}",
         "phase_space_evals_per_step": nodes, "bound_evals_per_step": stats[-1].bound,
         "phase_space_evals_per_s": nodes / (ms_per_step * 1e-3) * world,
         "kernel_ms_per_step": k_ms,
@@ -315,7 +323,7 @@ def run_ours(args, rank, world):
     return out, dict(d_ar=d_ar, delta=delta, rule=rule, df=df, x=x, w=w, f64=f64)
 
 
-def plain_at(F, env, tabs_host):
+def plain_at(F, env, tabs_host, iters):
     """One iteration of each form from the same (converged) potential: the plain FP64 form's
     time per iteration and the chosen form's density error against it (max over all grid
     points of |rho - rho64| / rho64; the second moments likewise; the density multipoles
@@ -346,11 +354,11 @@ def plain_at(F, env, tabs_host):
     ca, cb = res["mixed"][1][0], res["plain"][1][0]
     rhl_err = float(np.max(np.abs(ca - cb) / np.abs(cb[:, :1])))
     t64 = res["plain"][2]
-    return {"plain_s_per_iteration": t64, "plain_value": t64 * ITERS_TO_CONVERGE, "unit": UNIT,
+    return {"plain_s_per_iteration": t64, "plain_value": t64 * iters, "unit": UNIT,
             "plain_kernel_ms": res["plain"][3].kernel_ms, "plain_failures": res["plain"][3].failures,
             "rho_max_rel_err": err, "sigma_max_rel_err": sig, "rhl_max_rel_err": rhl_err,
             "note": f"one iteration of each form from the chosen form's converged potential, all grid points; "
-                    f"plain_value = its time x {ITERS_TO_CONVERGE} iterations"}
+                    f"plain_value = its time x the {iters} iterations the model needs"}
 
 
 def run_model_host(F, ctx, form, itermax):
@@ -530,6 +538,7 @@ def workload_c4(args):
 
 def main():
     args = parse()
+    POISSON["mode"] = args.poisson
     if args.profile_points:
         profile_case(args)
         return
@@ -572,7 +581,7 @@ def main():
         if e2e:
             out["e2e"] = e2e
         if args.form == "mixed" and not args.no_plain and r is not None:
-            out["vs_plain_fp64"] = plain_at(F, env, (r["phil"], r["Pr"], r["Pr2"]))
+            out["vs_plain_fp64"] = plain_at(F, env, (r["phil"], r["Pr"], r["Pr2"]), iters or ITERS_TO_CONVERGE)
             if args.converged_plain:
                 out["vs_plain_fp64"]["converged"] = converged_plain(F, r)
         if not args.no_cpu and world == 1:

@@ -34,7 +34,7 @@ struct fj_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t own = nullptr;
     std::string err;
-    DevBuf partial, counters, rule, misc;
+    DevBuf partial, counters, rule, misc, defer;
     std::map<int, DevBuf> gauss_nodes;                 // ngauss -> [2][ngauss] (ci, wi)
     std::map<std::pair<int, int>, DevBuf> poly;        // (ngauss, npoly) -> [npoly][ngauss]
     std::map<int, DevBuf> gl_rules;                    // jquad -> [2][n]
@@ -80,6 +80,33 @@ int ensure(fj_ctx *ctx, DevBuf &b, size_t bytes)
     cudaError_t e = cudaMalloc(&b.p, bytes);
     if (e != cudaSuccess) return fail(ctx, FJ_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     b.bytes = bytes;
+    return FJ_OK;
+}
+
+// Scratch of the mixed form's FP64 pass over capped nodes for a launch of
+// nblocks blocks (nw bitmap words each) and `nodes` phase-space nodes, in one
+// buffer: bitmaps | counts | offsets | scan carries | list (nodes, blocks,
+// moments).  The list holds 1/256 of the nodes (at least 64 Ki, at most 4 Mi
+// entries); a launch that leaves more is still exact (the extra nodes are
+// solved by their block's adding thread), only slower.
+int defer_setup(fj_ctx *ctx, long long nblocks, int nw, long long nodes, DeferWork &dw, unsigned *&bitmaps)
+{
+    const long long nchunks = (nblocks + kScanChunk - 1) / kScanChunk;
+    long long cap = nodes / 256;
+    cap = cap < 65536 ? 65536 : (cap > (4ll << 20) ? (4ll << 20) : cap);
+    const size_t ints = (size_t)nblocks * nw + 2 * (size_t)nblocks + nchunks + 2 + 2 * (size_t)cap;
+    const size_t off_mom = (ints * sizeof(int) + 15) / 16 * 16;
+    int rc = ensure(ctx, ctx->defer, off_mom + (size_t)cap * 6 * sizeof(double));
+    if (rc) return rc;
+    int *base = (int *)ctx->defer.p;
+    bitmaps = (unsigned *)base;
+    dw.count = base + (size_t)nblocks * nw;
+    dw.offset = dw.count + nblocks;
+    dw.chunk_sum = dw.offset + nblocks;
+    dw.node = dw.chunk_sum + nchunks + 2;
+    dw.block = dw.node + cap;
+    dw.mom = (double *)((char *)ctx->defer.p + off_mom);
+    dw.cap = (int)cap;
     return FJ_OK;
 }
 
@@ -283,17 +310,23 @@ int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delt
     int rc = build_args(ctx, pot, delta, df, rule, ngauss, Rz, npts, out6, a, mixed);
     if (rc) return rc;
     if ((rc = ensure(ctx, ctx->partial, (size_t)npts * a.blocks_per_point * 6 * sizeof(double)))) return rc;
+    const long long nq3 = (long long)rule->nq * rule->nq * rule->nq;
+    DeferWork dw{};
+    if (mixed) {
+        const long long nb = (long long)npts * a.blocks_per_point;
+        if ((rc = defer_setup(ctx, nb, defer_words(a.mixed_chunk), (long long)npts * nq3, dw, a.defer))) return rc;
+        a.defer_count = dw.count;
+    }
     if ((rc = ensure(ctx, ctx->counters, kNumCounters * sizeof(unsigned long long)))) return rc;
     a.partial = (double *)ctx->partial.p;
     a.counters = (unsigned long long *)ctx->counters.p;
-    const long long nq3 = (long long)rule->nq * rule->nq * rule->nq;
     if (mixed && ctx->jout) {  // unbound nodes keep the all-ones (NaN) pattern
         a.jout = ctx->jout;
         FJ_CUDA(cudaMemsetAsync(a.jout, 0xFF, (size_t)npts * nq3 * 2 * sizeof(float), ctx->stream));
     }
     FJ_CUDA(cudaMemsetAsync(a.counters, 0, kNumCounters * sizeof(unsigned long long), ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    FJ_CUDA(mixed ? launch_moments_mixed(a, ctx->mixed_variant, ctx->stream) : launch_moments(a, ctx->stream));
+    FJ_CUDA(mixed ? launch_moments_mixed(a, ctx->mixed_variant, dw, ctx->stream) : launch_moments(a, ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     return stats ? read_stats(ctx, nq3 * npts, stats) : FJ_OK;
 }
@@ -362,7 +395,7 @@ int fj_ctx_destroy(fj_ctx *ctx)
     if (!ctx) return FJ_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (DevBuf *b : {&ctx->partial, &ctx->counters, &ctx->rule, &ctx->misc})
+    for (DevBuf *b : {&ctx->partial, &ctx->counters, &ctx->rule, &ctx->misc, &ctx->defer})
         if (b->p) cudaFree(b->p);
     for (auto &kv : ctx->gauss_nodes) cudaFree(kv.second.p);
     for (auto &kv : ctx->poly) cudaFree(kv.second.p);
@@ -412,7 +445,7 @@ int fj_moments_batch(fj_ctx *ctx, int n, const fj_batch_item *items, const fj_qu
     if (!ctx || n < 1 || !items || !rule) return fail(ctx, FJ_ERR_ARG, "moments_batch: bad arguments");
     std::vector<MomentArgs> args(n);
     std::vector<int> bs(n + 1, 0), ps(n + 1, 0);
-    size_t smem = 0, partial = 0;
+    size_t smem = 0, partial = 0, defer_words_total = 0;
     bool mixed = false;
     long long nodes = 0;
     const long long nq3 = (long long)rule->nq * rule->nq * rule->nq;
@@ -430,15 +463,27 @@ int fj_moments_batch(fj_ctx *ctx, int n, const fj_batch_item *items, const fj_qu
         ps[m + 1] = ps[m] + npts;
         args[m].partial = reinterpret_cast<double *>(partial);  // offset, made a pointer below
         partial += (size_t)nb * 6;
+        if (mixed) {  // offsets, made pointers below
+            args[m].defer = reinterpret_cast<unsigned *>(defer_words_total);
+            args[m].defer_count = reinterpret_cast<int *>((size_t)bs[m]);
+            defer_words_total += (size_t)nb * defer_words(args[m].mixed_chunk);
+        }
         const size_t sm = mixed ? moment_mixed_smem_bytes(args[m]) : moment_smem_bytes(args[m]);
         smem = sm > smem ? sm : smem;
         nodes += nq3 * npts;
     }
     int rc;
     if ((rc = ensure(ctx, ctx->partial, partial * sizeof(double)))) return rc;
+    DeferWork dw{};
+    unsigned *bitmaps = nullptr;
+    if (mixed && (rc = defer_setup(ctx, bs[n], defer_words(ctx->mixed_chunk), nodes, dw, bitmaps))) return rc;
     if ((rc = ensure(ctx, ctx->counters, kNumCounters * sizeof(unsigned long long)))) return rc;
     for (int m = 0; m < n; m++) {
         args[m].partial = (double *)ctx->partial.p + reinterpret_cast<size_t>(args[m].partial);
+        if (mixed) {
+            args[m].defer = bitmaps + reinterpret_cast<size_t>(args[m].defer);
+            args[m].defer_count = dw.count + reinterpret_cast<size_t>(args[m].defer_count);
+        }
         args[m].counters = (unsigned long long *)ctx->counters.p;
     }
     // descriptor block: MomentArgs[n] | block_start[n+1] | point_start[n+1]
@@ -458,7 +503,7 @@ int fj_moments_batch(fj_ctx *ctx, int n, const fj_batch_item *items, const fj_qu
                         (const int *)(db + n * sizeof(MomentArgs) + (n + 1) * sizeof(int)), n};
     FJ_CUDA(cudaMemsetAsync(ctx->counters.p, 0, kNumCounters * sizeof(unsigned long long), ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    FJ_CUDA(launch_moments_batch(args[0], b, bs[n], smem, mixed, ctx->mixed_variant, ctx->stream));
+    FJ_CUDA(launch_moments_batch(args[0], b, bs[n], smem, mixed, ctx->mixed_variant, dw, ctx->stream));
     FJ_CUDA(launch_moments_finalize_batch(b, ps[n], ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     return stats ? read_stats(ctx, nodes, stats) : FJ_OK;

@@ -11,6 +11,7 @@ struct fj_quad_rule;
 
 namespace fj {
 
+struct DeferWork;  // scratch of the mixed form's FP64 pass (below)
 constexpr int kMomentBlock = 128;  // threads per block of the phase-space kernel
 // Device counters of one call (fj_moment_stats): nodes with H < 0, nodes whose
 // action solve still hit a cap (any kind), Poisson integrals that hit theirs,
@@ -45,6 +46,9 @@ struct MomentArgs {
     int mixed_chunk;         // mixed form: nodes per block (<= kMixedMaxNodes)
     float *jout;             // mixed form, optional: (Jr, Jz) of every bound node [npts][nq^3][2]
     double *partial;         // [npts][blocks_per_point][6]
+    unsigned *defer;         // mixed form: [npts * blocks_per_point][mixed_chunk / 32] bitmaps of the nodes
+                             // left to the FP64 pass
+    int *defer_count;        // mixed form: [npts * blocks_per_point] how many nodes each block left
     unsigned long long *counters;  // [kNumCounters], the slots below
     double *out6;            // [6][npts]
 };
@@ -130,7 +134,7 @@ size_t moment_smem_bytes(const MomentArgs &a);
 cudaError_t launch_moments(const MomentArgs &a, cudaStream_t s);
 // batched forms: grid = total blocks, smem = the largest model's
 cudaError_t launch_moments_batch(const MomentArgs &a0, const MomentBatch &b, int nblocks, size_t smem, bool mixed,
-                                 int variant, cudaStream_t s);
+                                 int variant, const DeferWork &dw, cudaStream_t s);
 cudaError_t launch_moments_finalize_batch(const MomentBatch &b, int npoints, cudaStream_t s);
 // dst6[q][idx[t]] = src6[q][t] (moments of n points into a grid of npts)
 cudaError_t launch_scatter6(int n, const int *idx, const double *src6, int npts, double *dst6, cudaStream_t s);
@@ -139,11 +143,30 @@ cudaError_t launch_moments_finalize(const MomentArgs &a, cudaStream_t s);
 // mixed-precision form (FJ_PREC_MIXED, double-power-law DF, QAGS momentum
 // integrals); counters[3] gets the nodes whose turning points ran in FP64
 constexpr int kMixedBlock = 128;     // threads per block of the mixed kernel
+// A mixed-form node whose FP32 solve hits a cap is not re-solved in the block
+// (one FP64 solve would hold its warp and block for as long as hundreds of FP32
+// ones): its block marks it in a bitmap of its node range, leaves it out of its
+// sums and records how many it left.  The FP64 pass (launch_deferred) then lists
+// every launch's left nodes compactly, block by block in node order (an
+// exclusive scan of the counts gives each block its offset), solves them all in
+// parallel, one thread per node, and adds each block's nodes to its partial
+// sums in list order: the same sums whatever order the threads ran in.
+struct DeferWork {
+    int *count;      // [nblocks] the blocks' counts (the launch's defer_count arrays, in block order)
+    int *offset;     // [nblocks] exclusive prefix of the blocks' counts
+    int *chunk_sum;  // [nblocks / kScanChunk + 2] scan carries; [nchunks] = the launch's total
+    int *node;       // [cap] listed nodes (index within the point's nq^3 rule)
+    int *block;      // [cap] global block index of each listed node
+    double *mom;     // [cap][6] moment contributions of the listed nodes
+    int cap;         // list capacity; nodes beyond it are solved by their block's adding thread
+};
+constexpr int kScanChunk = 1024;  // blocks per chunk of the count scan
 constexpr int kMixedMaxNodes = 8192; // largest node range of one block (shared-memory list)
+FJ_HD int defer_words(int chunk) { return (chunk + 31) / 32; }  // bitmap words of one block
 constexpr int kMixedVariants = 8;    // builds of the mixed kernel (2 forms x 4 register budgets)
 size_t moment_mixed_smem_bytes(const MomentArgs &a);
 int mixed_blocks_per_point(long long nq3, int chunk);
-cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, cudaStream_t s);
+cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, const DeferWork &dw, cudaStream_t s);
 
 cudaError_t launch_actions(PotView P, const double *Eg, const double *Dg, int ngrid, GLRule gl,
                            const double *pts, size_t n, double *out, cudaStream_t s);

@@ -535,7 +535,10 @@ FJ_HD void qelg_f(float *tab, int &n_io, float *res3, int &nres, float &result, 
     abserr = fmaxf(abserr, 5 * FLT_EPSILON * fabsf(result));
 }
 
-constexpr int kQagsCapF = 64;
+#ifndef FJ_MIXED_QAGS_CAP
+#define FJ_MIXED_QAGS_CAP 64
+#endif
+constexpr int kQagsCapF = FJ_MIXED_QAGS_CAP;  // intervals of the FP32 QAGS list (a full list: the node is re-solved in FP64)
 static_assert(kQagsCapF <= 256, "qags_f keeps interval indices as bytes");
 
 // QAGS (DQAGSE) in FP32 on [a,b] with the reference's tolerances; interval

@@ -64,8 +64,12 @@ template <int MINB, bool DYN>
 __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs a0, MomentBatch batch)
 {
     extern __shared__ double sm[];
+    __shared__ unsigned s_bits[kMixedMaxNodes / 32];  // nodes left to the FP64 pass
+    __shared__ int s_nleft;
     MomentArgs a = a0;
     int bid = blockIdx.x;
+    for (int i = threadIdx.x; i < kMixedMaxNodes / 32; i += blockDim.x) s_bits[i] = 0u;
+    if (threadIdx.x == 0) s_nleft = 0;
     if (batch.n > 0) {
         const int m = batch_model(batch.block_start, batch.n, bid);
         a = batch.args[m];
@@ -148,14 +152,15 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
     const double jacob = Ve * Ve * Ve;
 
     double m[6] = {0, 0, 0, 0, 0, 0};
-    unsigned esc = 0, resolved = 0;
+    unsigned esc = 0;
     FailTally tally;
     // one node's solve; returns the DF that enters the moments.  A node whose
     // FP32 solve hits a cap (a full QAGS list, a bracket walk or Brent at its
-    // step limit) is solved again by the plain form's FP64 solve (QAGS lists of
-    // kQagsCap intervals); only what that solve still caps is counted as a
-    // failure, with the plain form's policy (a capped bracket or root: DF 0; a
-    // full QAGS list: the estimate so far, as QUADPACK returns it).
+    // step limit) is marked in the block's bitmap and counts 0 here: k_moments_deferred
+    // solves it again with the plain form's FP64 solve (QAGS lists of kQagsCap
+    // intervals) and adds it to this block's sums.  Only what that solve still
+    // caps is a failure, with the plain form's policy (a capped bracket or root:
+    // DF 0; a full QAGS list: the estimate so far, as QUADPACK returns it).
     auto solve = [&](int q) {
         const int node = n0 + s_list[q];
         const int i = node / nq2, j = (node / nq) % nq, k = node % nq;
@@ -165,19 +170,17 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
         const double Delta = deltafn(s_Eg, s_Dg, a.ngrid, H);
         double J[2];
         double f = mixed_node_df(P, PF, *sK, a.df, Delta, R, z, Phi_h, V0, V1, V2, fail, e, J);
-        if (fail) {
-            fail = 0;
-            const GLRule qags{0, nullptr, nullptr};
-            fudge_actions(P, Delta, R, z, Phi_h, V0, V1, V2, qags, J[0], J[1], fail);
-            f = df_value(a.df, P, R, J[0], J[1], R * V1, fail);
-            resolved++;
+        esc += e;
+        if (fail && a.defer) {
+            atomicOr(&s_bits[(node - n0) >> 5], 1u << ((node - n0) & 31));
+            atomicAdd(&s_nleft, 1);
+            return 0.;
         }
         if (a.jout) {
             float *jo = a.jout + ((size_t)p * nq3 + node) * 2;
             jo[0] = (float)J[0];
             jo[1] = (float)J[1];
         }
-        esc += e;
         tally.add(fail);
         return (fail & (kFailBracket | kFailRoot)) ? 0. : f;
     };
@@ -214,14 +217,241 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
     }
     warp_count_fails(a.counters, tally);
     warp_count(&a.counters[kCntEscalated], esc);
-    warp_count(&a.counters[kCntResolved64], resolved);
     __syncthreads();
     if (threadIdx.x < 6) {
         double s = 0;
         for (int w = 0; w < kMixedBlock / 32; w++) s += s_red[w * 6 + threadIdx.x];
         a.partial[((size_t)p * B + chunk) * 6 + threadIdx.x] = s;
     }
+    if (a.defer) {  // the block's bitmap of deferred nodes and their number
+        const int nw = defer_words(a.mixed_chunk);
+        for (int i = threadIdx.x; i < nw; i += blockDim.x) a.defer[((size_t)p * B + chunk) * nw + i] = s_bits[i];
+        if (threadIdx.x == 0) a.defer_count[(size_t)p * B + chunk] = s_nleft;
+    }
     if (threadIdx.x == 0 && nbound) atomicAdd(&a.counters[kCntBound], (unsigned long long)nbound);
+}
+
+// ------------------------------------------------------ the FP64 pass
+// Over the nodes the mixed kernel left (launch_deferred): a scan of the
+// blocks' counts, the compact list, one thread per listed node, one thread per
+// block adding its nodes in list order.
+
+// the arguments and the model-local index of global block g of a launch
+__device__ __forceinline__ const MomentArgs &block_args(const MomentArgs &a0, const MomentBatch &b, int g, int &bid)
+{
+    bid = g;
+    if (b.n == 0) return a0;
+    const int m = batch_model(b.block_start, b.n, g);
+    bid -= b.block_start[m];
+    return b.args[m];
+}
+
+// the block's point, its potential and escape speed (as the mixed kernel's setup)
+__device__ void defer_point(const MomentArgs &a, int bid, double &R, double &z, double &Phi_h, double &Ve)
+{
+    const int nr = a.P.nr, p = bid / a.blocks_per_point;
+    if (a.Rz) { R = a.Rz[2 * p]; z = a.Rz[2 * p + 1]; }
+    else {
+        const int n = p / a.ngauss, gg = p % a.ngauss;
+        const double c = a.ci[gg], si = sqrt(1 - c * c);
+        R = a.P.ar[n] * si; z = a.P.ar[n] * c;
+    }
+    const PotView P{nr, a.P.npoly, a.P.ar, a.P.phil, a.P.Pr, a.P.Pr2};
+    const double rmax = a.P.ar[nr - 1];
+    Phi_h = pot_phi(P, R, z);
+    Ve = sqrt(-2 * (Phi_h - pot_phi(P, 10 * rmax, 10 * rmax)));
+}
+
+// one left node with the plain form's FP64 solve (fudge_actions with QAGS lists
+// of kQagsCap intervals, df_value): its six moment contributions
+__device__ void defer_solve(const MomentArgs &a, int bid, int node, double *c6, FailTally &tally)
+{
+    double R, z, Phi_h, Ve;
+    defer_point(a, bid, R, z, Phi_h, Ve);
+    const PotView P{a.P.nr, a.P.npoly, a.P.ar, a.P.phil, a.P.Pr, a.P.Pr2};
+    const int nq = a.nq, nq2 = nq * nq;
+    const int i = node / nq2, j = (node / nq) % nq, l = node % nq;
+    const double V0 = 1e-6 + Ve * a.xq[i], V1 = 1e-6 + Ve * a.xq[j], V2 = 1e-6 + Ve * a.xq[l];
+    const double H = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h;
+    unsigned fail = 0;
+    double Jr, Jz;
+    const GLRule qags{0, nullptr, nullptr};
+    fudge_actions(P, deltafn(a.Eg, a.Dg, a.ngrid, H), R, z, Phi_h, V0, V1, V2, qags, Jr, Jz, fail);
+    double DF = df_value(a.df, P, R, Jr, Jz, R * V1, fail);
+    if (fail & (kFailBracket | kFailRoot)) DF = 0.;
+    tally.add(fail);
+    if (a.jout) {
+        float *jo = a.jout + ((size_t)(bid / a.blocks_per_point) * nq2 * nq + node) * 2;
+        jo[0] = (float)Jr;
+        jo[1] = (float)Jz;
+    }
+    const double jd = (a.wq[i] * a.wq[j] * a.wq[l]) * (Ve * Ve * Ve * DF);
+    c6[0] = jd; c6[1] = jd * V1; c6[2] = jd * V0 * V0;
+    c6[3] = jd * V1 * V1; c6[4] = jd * V2 * V2; c6[5] = jd * V0 * V2;
+}
+
+__device__ void add_tally(unsigned long long *counters, const FailTally &t, unsigned solved)
+{
+    if (solved) atomicAdd(&counters[kCntResolved64], (unsigned long long)solved);
+    if (!t.any) return;
+    atomicAdd(&counters[kCntFailed], (unsigned long long)t.any);
+    if (t.quad) atomicAdd(&counters[kCntFailQuad], (unsigned long long)t.quad);
+    if (t.bracket) atomicAdd(&counters[kCntFailBracket], (unsigned long long)t.bracket);
+    if (t.root) atomicAdd(&counters[kCntFailRoot], (unsigned long long)t.root);
+}
+
+// exclusive scan of the counts: per chunk of kScanChunk blocks, then the chunk
+// carries (one CTA; chunk_sum[nchunks] = the total), then the carries added
+__device__ __forceinline__ int block_exclusive_scan(int v, int *s_warp, int &total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < nwarp ? s_warp[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nwarp) s_warp[lane] = w;
+    }
+    __syncthreads();
+    total = s_warp[nwarp - 1];
+    const int res = x - v + (warp ? s_warp[warp - 1] : 0);
+    __syncthreads();
+    return res;
+}
+
+__global__ void __launch_bounds__(kScanChunk) k_defer_scan_chunks(DeferWork dw, int nblocks)
+{
+    __shared__ int s_warp[32];
+    const int i = blockIdx.x * kScanChunk + threadIdx.x;
+    int total;
+    const int ex = block_exclusive_scan(i < nblocks ? dw.count[i] : 0, s_warp, total);
+    if (i < nblocks) dw.offset[i] = ex;
+    if (threadIdx.x == 0) dw.chunk_sum[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanChunk) k_defer_scan_carries(DeferWork dw, int nchunks)
+{
+    __shared__ int s_warp[32];
+    int carry = 0;
+    for (int base = 0; base < nchunks; base += kScanChunk) {
+        const int i = base + threadIdx.x;
+        const int v = i < nchunks ? dw.chunk_sum[i] : 0;
+        int total;
+        const int ex = block_exclusive_scan(v, s_warp, total);
+        if (i < nchunks) dw.chunk_sum[i] = carry + ex;
+        carry += total;
+    }
+    if (threadIdx.x == 0) dw.chunk_sum[nchunks] = carry;
+}
+
+// adds the carries and lists each block's left nodes in node order (a warp per block)
+constexpr int kListWarps = 4;
+__global__ void __launch_bounds__(32 * kListWarps) k_defer_list(MomentArgs a0, MomentBatch batch, DeferWork dw,
+                                                                 int nblocks)
+{
+    const int lane = threadIdx.x & 31;
+    const int g = blockIdx.x * kListWarps + (threadIdx.x >> 5);
+    if (g >= nblocks) return;  // the whole warp
+    const int off = dw.offset[g] + dw.chunk_sum[g / kScanChunk];
+    __syncwarp();
+    if (lane == 0) dw.offset[g] = off;
+    const int cnt = dw.count[g];
+    if (cnt == 0) return;
+    int bid;
+    const MomentArgs &a = block_args(a0, batch, g, bid);
+    const int nw = defer_words(a.mixed_chunk), B = a.blocks_per_point, chunk = bid % B;
+    const long long nq3 = (long long)a.nq * a.nq * a.nq;
+    const int n0 = (int)(chunk * nq3 / B);
+    const unsigned *bits = a.defer + (size_t)bid * nw;
+    int rank = 0;
+    for (int w = 0; w < nw && rank < cnt; w++) {
+        const unsigned word = bits[w];  // the same word on every lane
+        if ((word >> lane) & 1u) {
+            const int e = off + rank + __popc(word & ((1u << lane) - 1u));
+            if (e < dw.cap) { dw.node[e] = n0 + w * 32 + lane; dw.block[e] = g; }
+        }
+        rank += __popc(word);
+    }
+}
+
+// one thread per listed node (grid-stride over the launch's total)
+__global__ void __launch_bounds__(64) k_defer_solve(MomentArgs a0, MomentBatch batch, DeferWork dw, int nchunks)
+{
+    const int total = min(dw.chunk_sum[nchunks], dw.cap);
+    FailTally tally;
+    unsigned solved = 0;
+    unsigned long long *counters = a0.counters;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        int bid;
+        const MomentArgs &a = block_args(a0, batch, dw.block[e], bid);
+        counters = a.counters;
+        defer_solve(a, bid, dw.node[e], dw.mom + (size_t)e * 6, tally);
+        solved++;
+    }
+    add_tally(counters, tally, solved);
+}
+
+// one thread per block: its listed nodes added in list order (nodes beyond the
+// list's capacity solved here, in node order)
+__global__ void __launch_bounds__(128) k_defer_add(MomentArgs a0, MomentBatch batch, DeferWork dw, int nblocks)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nblocks) return;
+    const int cnt = dw.count[g];
+    if (cnt == 0) return;
+    int bid;
+    const MomentArgs &a = block_args(a0, batch, g, bid);
+    const int off = dw.offset[g];
+    double msum[6] = {0, 0, 0, 0, 0, 0};
+    FailTally tally;
+    unsigned solved = 0;
+    for (int k = 0; k < cnt; k++) {
+        const int e = off + k;
+        if (e < dw.cap) {
+            for (int q = 0; q < 6; q++) msum[q] += dw.mom[(size_t)e * 6 + q];
+            continue;
+        }
+        // past the list: the block's k-th left node, from its bitmap
+        const int nw = defer_words(a.mixed_chunk), B = a.blocks_per_point;
+        const long long nq3 = (long long)a.nq * a.nq * a.nq;
+        const int n0 = (int)((bid % B) * nq3 / B);
+        const unsigned *bits = a.defer + (size_t)bid * nw;
+        int r = k, w = 0;
+        while (r >= __popc(bits[w])) r -= __popc(bits[w++]);
+        unsigned word = bits[w];
+        for (int t = 0; t < r; t++) word &= word - 1;
+        double c6[6];
+        defer_solve(a, bid, n0 + w * 32 + (__ffs((int)word) - 1), c6, tally);
+        solved++;
+        for (int q = 0; q < 6; q++) msum[q] += c6[q];
+    }
+    double *pt = a.partial + (size_t)bid * 6;
+    for (int q = 0; q < 6; q++) pt[q] += msum[q];
+    add_tally(a.counters, tally, solved);
+}
+
+static cudaError_t launch_deferred(const MomentArgs &a, const MomentBatch &b, long long nblocks, const DeferWork &dw,
+                                   cudaStream_t s)
+{
+    if (!dw.count) return cudaSuccess;
+    const int nb = (int)nblocks, nchunks = (nb + kScanChunk - 1) / kScanChunk;
+    k_defer_scan_chunks<<<nchunks, kScanChunk, 0, s>>>(dw, nb);
+    k_defer_scan_carries<<<1, kScanChunk, 0, s>>>(dw, nchunks);
+    k_defer_list<<<(nb + kListWarps - 1) / kListWarps, 32 * kListWarps, 0, s>>>(a, b, dw, nb);
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    k_defer_solve<<<8 * (nsm > 0 ? nsm : 1), 64, 0, s>>>(a, b, dw, nchunks);
+    k_defer_add<<<(nb + 127) / 128, 128, 0, s>>>(a, b, dw, nb);
+    return cudaGetLastError();
 }
 
 namespace {
@@ -262,12 +492,14 @@ size_t local_bytes()
 }
 }  // namespace
 
-cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, cudaStream_t s)
+cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, const DeferWork &dw, cudaStream_t s)
 {
     if (a.mixed_chunk < kMixedBlock || a.mixed_chunk > kMixedMaxNodes) return cudaErrorInvalidValue;
     const size_t smem = moment_mixed_smem_bytes(a);
-    const cudaError_t e = launch_mixed_any(a, MomentBatch{nullptr, nullptr, nullptr, 0},
-                                           (long long)a.npts * a.blocks_per_point, smem, variant, s);
+    const MomentBatch none{nullptr, nullptr, nullptr, 0};
+    const long long nblocks = (long long)a.npts * a.blocks_per_point;
+    cudaError_t e = launch_mixed_any(a, none, nblocks, smem, variant, s);
+    if (e == cudaSuccess) e = launch_deferred(a, none, nblocks, dw, s);
     if (e != cudaSuccess) return e;
     return launch_moments_finalize(a, s);
 }
@@ -276,10 +508,11 @@ cudaError_t launch_moments_plain_batch(const MomentArgs &a0, const MomentBatch &
                                       cudaStream_t s);
 
 cudaError_t launch_moments_batch(const MomentArgs &a0, const MomentBatch &b, int nblocks, size_t smem, bool mixed,
-                                 int variant, cudaStream_t s)
+                                 int variant, const DeferWork &dw, cudaStream_t s)
 {
     if (!mixed) return launch_moments_plain_batch(a0, b, nblocks, smem, s);
-    return launch_mixed_any(a0, b, nblocks, smem, variant, s);
+    const cudaError_t e = launch_mixed_any(a0, b, nblocks, smem, variant, s);
+    return e == cudaSuccess ? launch_deferred(a0, b, nblocks, dw, s) : e;
 }
 
 size_t moments_mixed_local_bytes()
@@ -289,6 +522,9 @@ size_t moments_mixed_local_bytes()
                                       local_bytes<6, true>(), local_bytes<8, true>()};
     size_t m = 0;
     for (size_t x : v) m = x > m ? x : m;
+    cudaFuncAttributes at;
+    for (const void *k : {(const void *)k_defer_solve, (const void *)k_defer_add})
+        if (cudaFuncGetAttributes(&at, k) == cudaSuccess && at.localSizeBytes > m) m = at.localSizeBytes;
     return m;
 }
 

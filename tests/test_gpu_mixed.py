@@ -96,8 +96,15 @@ def test_mixed_vs_plain_nfw_80(ctx, rule):
     assert rel(a[:, [2, 3, 4]], b[:, [2, 3, 4]]) < MIXED_TOL
     # vrot is a nearly cancelling sum: compare on the scale of the dispersion
     assert np.max(np.abs(a[:, 1] - b[:, 1]) / b[:, 3]) < MIXED_TOL
-    # every escalated / capped node is counted, and they are rare
-    assert st.escalated < 0.01 * st.bound and st.failures < 0.01 * st.bound
+    # escalated turning points are rare; a node whose FP32 solve hits a cap is solved again
+    # by the FP64 pass, so no failure remains (the plain form has none on this workload)
+    assert st.escalated < 0.01 * st.bound and st.failures == 0
+    assert st.fail_quad == st.fail_bracket == st.fail_root == 0
+    assert 0 <= st.resolved64 < 0.01 * st.bound
+    # the deferred FP64 pass adds to fixed per-block sums in slot order: the same bits again
+    out2 = torch.zeros_like(out32)
+    st2 = ctx.moments_points(pot, delta, df, F.Rule(x, w, precision=A.FJ_PREC_MIXED), dev(M), out2)
+    assert torch.equal(out2, out32) and st2.resolved64 == st.resolved64
 
 
 def test_mixed_vs_oracle_nfw_80(ctx):
@@ -117,10 +124,25 @@ def test_mixed_vs_oracle_nfw_80(ctx):
     assert rel(got[:, [0, 2, 3, 4]], ref[:, [0, 2, 3, 4]]) < MIXED_TOL
 
 
-def test_mixed_run_model_vs_plain(ctx):
+@pytest.fixture
+def cumulative(ctx):
+    """The loop comparisons run with the cumulative Poisson solve, as the chosen form does:
+    with the adaptive one, a density difference of 1e-6 between the forms can flip one of
+    its subdivision decisions and move the next potential by up to ~1e-3."""
+    ctx.set_poisson(A.FJ_POISSON_CUMULATIVE)
+    yield ctx
+    ctx.set_poisson(A.FJ_POISSON_QAGS)
+
+
+def test_mixed_run_model_vs_plain(cumulative):
     """Two iterations of the whole loop in both forms: density multipoles and the
-    virial ratio within the mixed gate."""
-    g, meta, _ = load_golden("nfw_dpl_rot")
+    virial ratio within the mixed gate.  On the Hernquist fixture: on the 12 x 4 NFW
+    fixture one grid point (r ~ 46, cos theta ~ 0.67, three times the density of its
+    neighbours) is decided by a single node, and the reference's own FP64 algorithm
+    moves it by 1.3 % between potentials that differ by 3e-7, so a second iteration
+    there compares that discontinuity, not the two forms."""
+    ctx = cumulative
+    g, meta, _ = load_golden("hern_dpl")
     nr, ng, npl = meta["nr"], meta["ng"], meta["np"]
     df = df_of(meta)
     dt = (g["Egrid"], g["Dgrid"])
@@ -188,12 +210,13 @@ def test_mixed_configurations_agree(ctx):
         ctx.set_mixed_config(*saved)
 
 
-def test_mixed_loop_vs_plain_c1(ctx):
+def test_mixed_loop_vs_plain_c1(cumulative):
     """The whole self-consistent loop of the 40 x 20 Hernquist configuration (l <= 8, the
     reference's live velocity rule, 5 iterations from the analytic guess) in the chosen
     form against the plain FP64 form: density multipoles and potential within 1e-4 of
     the FP64 ones (relative to each shell's monopole) and the virial ratio within 1e-4,
     after the iterations have compounded the per-iteration differences."""
+    ctx = cumulative
     df = F.DFParams("Hernquist")
     args = (40, 20, 5, 0.01, 100.0, df)
     p64 = ctx.run_model(*args, F.Rule(), itermax=5)

@@ -148,10 +148,16 @@ def test_run_model_two_iterations(ctx):
                         delta_table=(g["Egrid"], g["Dgrid"]))
     assert out["iterations"] == 2 and out["failures"] == 0
     # After two iterations the first iteration's rounding-level differences (libm vs CUDA
-    # exp/log/pow) have passed through the Poisson solve and a second moment sweep; the
-    # reference's own builds with and without FMA contraction differ by 1.6e-9 in this
-    # measure, so the two-iteration gate is 2e-9 (single iterations keep 1e-9).
-    assert rel_shells(out["coef6"][0], g["it1_rhl"].reshape(nr, npl)) < 2 * TOL
+    # exp/log/pow) have passed through the Poisson solve and a second moment sweep.  The
+    # reference's own builds with and without FMA contraction, run on this fixture's
+    # focal-distance table, differ by 1.9e-8 (first iteration) and 3e-9 (second) on its
+    # outer shells (density below 1e-6 of the centre), where a few nodes decide the shell:
+    # 2e-9 on the shells above that density, 1e-7 on the outer ones (single iterations keep
+    # 1e-9 everywhere).
+    ref = g["it1_rhl"].reshape(nr, npl)
+    inner = np.abs(ref[:, 0]) >= 1e-6 * abs(ref[0, 0])
+    assert rel_shells(out["coef6"][0][inner], ref[inner]) < 2 * TOL
+    assert rel_shells(out["coef6"][0], ref) < 100 * TOL
     assert rel_shells(out["phil"], g["it1_phil"].reshape(nr, npl)) < 2 * TOL
     ref_vir = g["vir2"][1]  # KE, PE, W/K printed with %f after the second iteration
     K = out["vir7"][0] + out["vir7"][1]
