@@ -243,6 +243,35 @@ class Model:
         return E.copy(), D.copy(), fail
 
 
+_FLIB = None
+
+
+def flop_counts(model, points):
+    """The reference's algorithm with its floating-point operations tallied (liboracle_flops.so,
+    orc_flops.cpp): the moments of the grid points `points` (indices p = n*ngauss + g) of
+    `model`, one host thread.  Returns (moments [6][npts] for those points, counts dict add, mul,
+    div, sqrt, trans); the moments are the oracle's bit for bit."""
+    global _FLIB
+    if _FLIB is None:
+        so = os.path.join(_HERE, "liboracle_flops.so")
+        subprocess.run(["make", "-s", "-C", _HERE, "liboracle_flops.so"], check=True)
+        L = C.CDLL(so)
+        L.orc_moment_grid.argtypes = [C.POINTER(_Model), C.c_int, C.c_int, DP, C.c_int, C.POINTER(Stats)]
+        L.orc_flops_reset.argtypes = []
+        L.orc_flops_get.argtypes = [C.POINTER(C.c_ulonglong)]
+        _FLIB = L
+    L = _FLIB
+    npts = model.nr * model.ngauss
+    out = np.zeros((6, npts))
+    mc = model.c()
+    L.orc_flops_reset()
+    for p in points:
+        L.orc_moment_grid(mc, int(p), int(p) + 1, out.ctypes.data_as(DP), 1, C.byref(Stats()))
+    cnt = (C.c_ulonglong * 5)()
+    L.orc_flops_get(cnt)
+    return out[:, list(points)], dict(zip(("add", "mul", "div", "sqrt", "trans"), [int(v) for v in cnt]))
+
+
 def project6(ar, ngauss, npoly, grids6):
     nr = len(ar)
     g = _f64(grids6).copy()
