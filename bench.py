@@ -54,19 +54,19 @@ CFG = dict(model="NFW", nr=80, ngauss=40, npoly=7, rmin=1e-3, rmax=300.0, dphi_h
 ITERS_TO_CONVERGE = 19
 METRIC = "wall-s per converged model at rho err<=1e-4, chosen vs plain FP64, same GB300"
 UNIT = "s/model"
-# FP64 operations per phase-space evaluation executed by active threads of the
-# plain phase-space kernel (dadd + dmul + 2*dfma, from an ncu capture of the same
-# workload); the work unit of the roofline.
-FP64_FLOPS_PER_EVAL = {"plain": 1.21e5}
-# FP32 operations (fadd + fmul + 2*ffma) executed by active lanes per phase-space
-# evaluation of the mixed form, from an ncu capture of a 240-point spread of the
-# same workload
-FP32_FLOPS_PER_EVAL = {"mixed": 4.68e4}
-# DRAM bytes (read + write) per phase-space evaluation from the same captures:
-# 1678.2 MB over 2,555,520 evaluations (mixed, the 64-register build with 8 blocks
-# per SM; local-memory and partial-sum traffic, the inputs are < 16 KB), 7.58 MB over
-# 255,552 (plain FP64); a launch's traffic scales with its evaluations
-DRAM_BYTES_PER_EVAL = {"mixed": 1678.2e6 / 2555520, "plain": 7.58e6 / 255552}
+# Algorithmic work per phase-space evaluation of this workload: the reference's algorithm
+# with every floating-point operation tallied (oracle/count_flops.py on 24 grid points of the
+# guess potential): 24,583 add + 29,604 mul + 9,158 div + 897 sqrt + 20 x 3,437 transcendental
+# calls = 1.33e5 FLOPs per (grid point, velocity node), bound or not.  The same for both forms
+# (the mixed form runs the same algorithm in FP32 with FP64 where FP32 would change decisions).
+ALG_FLOPS_PER_EVAL = 1.33e5
+# FLOPs executed by active lanes (ncu: fadd + fmul + 2*ffma, resp. the FP64 ones) per
+# evaluation in each form's kernel, from captures of the same workload
+EXEC_FLOPS_PER_EVAL = {"mixed": 4.68e4, "plain": 1.21e5}
+# DRAM bytes (read + write) per phase-space evaluation from ncu captures of the same workload
+# (mixed: a 240-point spread, 2,555,520 evaluations; plain: 24 points): local-memory and
+# partial-sum traffic, the inputs are < 16 KB; a launch's traffic scales with its evaluations
+DRAM_BYTES_PER_EVAL = {"mixed": 1416.7e6 / 2555520, "plain": 7.58e6 / 255552}
 L2_NOTE = "256 MiB buffer written between steps"
 
 
@@ -288,8 +288,8 @@ def run_ours(args, rank, world):
     fp32 = args.form == "mixed"
     peak = np.zeros(1)
     F.load_library().fj_measure_fma_peak(1 if fp32 else 0, peak.ctypes.data_as(F._abi.DP))
-    flops = FP32_FLOPS_PER_EVAL.get(args.form) if fp32 else FP64_FLOPS_PER_EVAL.get(args.form)
-    achieved = flops * nodes / (k_ms * 1e-3) / 1e12 if flops else None
+    achieved = ALG_FLOPS_PER_EVAL * nodes / (k_ms * 1e-3) / 1e12
+    executed = EXEC_FLOPS_PER_EVAL[args.form] * nodes / (k_ms * 1e-3) / 1e12
     tot = lambda f: int(sum(getattr(st, f) for st in stats))  # noqa: E731
     out = {
         "metric": METRIC, "value": None, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -312,9 +312,14 @@ def run_ours(args, rank, world):
         "mixed_kernel_config": tuned,
         "roofline": {"bound": "fp32" if fp32 else "fp64", "kernel": "k_moments_mixed" if fp32 else "k_moments",
                      "achieved": achieved, "peak": float(peak[0]),
-                     "unit": "TFLOP/s", "frac": (achieved / peak[0]) if achieved else None,
-                     "peak_source": f"fj_measure_fma_peak ({'FP32' if fp32 else 'FP64'} FMA chains, this GPU)",
-                     "flops_per_eval": flops,
+                     "unit": "TFLOP/s", "frac": achieved / peak[0],
+                     "peak_source": f"fj_measure_fma_peak ({'FP32' if fp32 else 'FP64'} FMA chains, this GPU; "
+                                    "the measured peaks file covers HBM and BF16 only)",
+                     "flops_per_eval": ALG_FLOPS_PER_EVAL,
+                     "flops_source": "algorithmic: the reference's algorithm with its operations tallied "
+                                     "(oracle/count_flops.py), transcendental calls weighted 20",
+                     "executed_achieved": executed, "executed_frac": executed / peak[0],
+                     "executed_flops_per_eval": EXEC_FLOPS_PER_EVAL[args.form],
                      "traffic": (DRAM_BYTES_PER_EVAL[args.form] * nodes) if args.form in DRAM_BYTES_PER_EVAL else None,
                      "traffic_unit": "bytes per launch (ncu capture of a 240-point case, scaled by evaluations)"},
         "clocks": clk.summary(),
