@@ -90,6 +90,8 @@ def parse():
                          "key, about 10 s; 2 per host thread for each step of --impl reference)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the two-component (c3) and batched-sweep (c4) measurements added to the line")
     ap.add_argument("--profile-points", type=int, default=0,
                     help="profiling case: one phase-space launch over this many grid points, no bench line")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"],
@@ -498,7 +500,7 @@ def workload_c3(args):
     d1, d2 = rng.uniform(0.4, 1.0, 4), rng.uniform(0.4, 1.0, 4)
     bulge = F.DFParams("Hernquist", *d1, mass=0.1, r0=1.0)
     halo = F.DFParams("NFW", *d2, mass=1.0, r0=10.0)
-    ctx = F.Context(0)
+    ctx = new_context(F, 0)
     rule = F.Rule(*velocity_rule(), precision=A.FJ_PREC_MIXED)
     nr, ng, npl, it = 64, 32, 6, 15
     out = ctx.run_model(nr, ng, npl, 1e-3, 300.0, bulge, rule, itermax=it, df2=halo,
@@ -516,7 +518,9 @@ def workload_c4(args):
     """Batched sweep: seeded models -- type from {Hernquist, Isochrone, NFW}, h/g coefficients
     ~ U[0.3, 1.2], chi ~ U[0, 2], radii in {32, 48, 64, 96} x angles in {16, 24, 32}, l <= 8 --
     iterated together (one phase-space launch per iteration, the iteration captured as a CUDA
-    graph, the focal-distance tables on the GPU), mixed form; 2 iterations timed whole."""
+    graph, the focal-distance tables on the GPU), mixed form; 2 iterations timed whole.  The
+    phase-space launch is one persistent kernel that takes (model, point, node range) items
+    from a work queue, most expensive first."""
     import fjmodels_gb300 as F
     from fjmodels_gb300 import _abi as A
     rng = np.random.default_rng(256)
@@ -527,7 +531,7 @@ def workload_c4(args):
         df = F.DFParams(kind, *dh, chi=float(rng.uniform(0, 2)), k=0.5)
         models.append(dict(nr=int(rng.choice([32, 48, 64, 96])), ngauss=int(rng.choice([16, 24, 32])), npoly=5,
                            rmin=1e-3, rmax=300.0 if kind == "NFW" else 100.0, df=df))
-    ctx = F.Context(0)
+    ctx = new_context(F, 0)
     rule = F.Rule(*velocity_rule(), precision=A.FJ_PREC_MIXED)
     it = 2
     outs = ctx.run_model_batch(models, rule, itermax=it, use_graph=True, delta_gpu=True)
@@ -591,6 +595,8 @@ def main():
                 out["vs_plain_fp64"]["converged"] = converged_plain(F, r)
         if not args.no_cpu and world == 1:
             out["cpu_baseline"] = cpu_sample(args, sample=args.cpu_sample or 10 * os.cpu_count())
+        if not args.no_extra and world == 1 and args.form == "mixed":
+            out["extra_workloads"] = {"c3": workload_c3(args), "c4": workload_c4(args)}
         print(json.dumps(out))
 
 

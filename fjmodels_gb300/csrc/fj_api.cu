@@ -46,6 +46,10 @@ struct fj_ctx {
     DevBuf batch;                                      // batched launch: MomentArgs[n] | block_start | point_start
     std::vector<char> batch_host;                      // what `batch` holds (re-uploaded only when it changes)
     DevBuf delta_ws;                                   // GPU focal-distance tables: views | Eg ptrs | Dg ptrs | flags
+    DevBuf queue;                                      // mixed kernel's work queue: counter | order | costs
+    int q_total = 0;                                   // items of the launch whose costs the queue holds
+    bool q_costs = false, q_order = false;             // costs recorded / order taken from them
+    int q_launches = 0;                                // launches since the order was last taken
 };
 
 namespace fj {
@@ -107,6 +111,58 @@ int defer_setup(fj_ctx *ctx, long long nblocks, int nw, long long nodes, DeferWo
     dw.block = dw.node + cap;
     dw.mom = (double *)((char *)ctx->defer.p + off_mom);
     dw.cap = (int)cap;
+    return FJ_OK;
+}
+
+// The persistent mixed kernel's work queue for a launch of `total` items.  The
+// kernel records every item's cycles; the next launch of the same size (outside
+// a graph capture) takes the items most expensive first, the order refreshed
+// from the latest costs every kReorderEvery launches.  A captured launch keeps
+// the order in place at capture (refresh_queue_order takes one before).
+constexpr int kReorderEvery = 4;
+
+int refresh_queue_order(fj_ctx *ctx)
+{
+    if (!ctx->q_costs || ctx->q_total < 1) return FJ_OK;
+    const int n = ctx->q_total;
+    int *order = (int *)((char *)ctx->queue.p + 16);
+    float *cost = (float *)(order + n);
+    std::vector<float> c(n);
+    FJ_CUDA(cudaMemcpyAsync(c.data(), cost, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    FJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; i++) idx[i] = i;
+    std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return c[x] > c[y]; });
+    FJ_CUDA(cudaMemcpyAsync(order, idx.data(), n * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    FJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->q_order = true;
+    ctx->q_launches = 0;
+    return FJ_OK;
+}
+
+int queue_setup(fj_ctx *ctx, long long total, ItemQueue &q)
+{
+    if (total < 1 || total > 0x7fffffffLL) return fail(ctx, FJ_ERR_ARG, "moments: too many work items");
+    const int n = (int)total;
+    if (n != ctx->q_total) {
+        int rc = ensure(ctx, ctx->queue, 16 + (size_t)n * (sizeof(int) + sizeof(float)));
+        if (rc) return rc;
+        ctx->q_total = n;
+        ctx->q_costs = ctx->q_order = false;
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    FJ_CUDA(cudaStreamIsCapturing(ctx->stream, &cs));
+    if (cs == cudaStreamCaptureStatusNone && ctx->q_costs && (!ctx->q_order || ctx->q_launches >= kReorderEvery)) {
+        int rc = refresh_queue_order(ctx);
+        if (rc) return rc;
+    }
+    int *order = (int *)((char *)ctx->queue.p + 16);
+    q.next = (unsigned *)ctx->queue.p;
+    q.order = ctx->q_order ? order : nullptr;
+    q.cost = (float *)(order + n);
+    q.total = n;
+    ctx->q_costs = true;  // this launch records them
+    ctx->q_launches++;
     return FJ_OK;
 }
 
@@ -326,7 +382,9 @@ int run_moments(fj_ctx *ctx, const fj_potential *pot, const fj_delta_table *delt
     }
     FJ_CUDA(cudaMemsetAsync(a.counters, 0, kNumCounters * sizeof(unsigned long long), ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    FJ_CUDA(mixed ? launch_moments_mixed(a, ctx->mixed_variant, dw, ctx->stream) : launch_moments(a, ctx->stream));
+    ItemQueue q{};
+    if (mixed && (rc = queue_setup(ctx, (long long)npts * a.blocks_per_point, q))) return rc;
+    FJ_CUDA(mixed ? launch_moments_mixed(a, ctx->mixed_variant, dw, q, ctx->stream) : launch_moments(a, ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     return stats ? read_stats(ctx, nq3 * npts, stats) : FJ_OK;
 }
@@ -395,7 +453,7 @@ int fj_ctx_destroy(fj_ctx *ctx)
     if (!ctx) return FJ_OK;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    for (DevBuf *b : {&ctx->partial, &ctx->counters, &ctx->rule, &ctx->misc, &ctx->defer})
+    for (DevBuf *b : {&ctx->partial, &ctx->counters, &ctx->rule, &ctx->misc, &ctx->defer, &ctx->queue})
         if (b->p) cudaFree(b->p);
     for (auto &kv : ctx->gauss_nodes) cudaFree(kv.second.p);
     for (auto &kv : ctx->poly) cudaFree(kv.second.p);
@@ -503,7 +561,9 @@ int fj_moments_batch(fj_ctx *ctx, int n, const fj_batch_item *items, const fj_qu
                         (const int *)(db + n * sizeof(MomentArgs) + (n + 1) * sizeof(int)), n};
     FJ_CUDA(cudaMemsetAsync(ctx->counters.p, 0, kNumCounters * sizeof(unsigned long long), ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    FJ_CUDA(launch_moments_batch(args[0], b, bs[n], smem, mixed, ctx->mixed_variant, dw, ctx->stream));
+    ItemQueue q{};
+    if (mixed && (rc = queue_setup(ctx, bs[n], q))) return rc;
+    FJ_CUDA(launch_moments_batch(args[0], b, bs[n], smem, mixed, ctx->mixed_variant, dw, q, ctx->stream));
     FJ_CUDA(launch_moments_finalize_batch(b, ps[n], ctx->stream));
     FJ_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     return stats ? read_stats(ctx, nodes, stats) : FJ_OK;
@@ -1314,6 +1374,8 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
             bound += st.bound;
             failures += st.failures;
             if (use_graph && k + 1 < itermax) {  // capture the sequence once it has run eagerly
+                // the captured launches take the items in the order of this iteration's costs
+                if (cfgs[0].rule.precision == FJ_PREC_MIXED && (rc = refresh_queue_order(ctx))) return rc;
                 FJ_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
                 rc = iteration(nullptr, retab);
                 cudaGraph_t g = nullptr;

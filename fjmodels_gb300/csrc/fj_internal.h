@@ -133,8 +133,16 @@ __device__ __forceinline__ int batch_model(const int *start, int n, int i)
 size_t moment_smem_bytes(const MomentArgs &a);
 cudaError_t launch_moments(const MomentArgs &a, cudaStream_t s);
 // batched forms: grid = total blocks, smem = the largest model's
+// work queue of the persistent mixed kernel: item i is block order[i] (order
+// NULL: block i) of the launch's layout; cost[b] receives block b's cycles
+struct ItemQueue {
+    unsigned *next;    // device counter, zeroed by the launch
+    const int *order;  // [total] or NULL
+    float *cost;       // [total] or NULL
+    int total;
+};
 cudaError_t launch_moments_batch(const MomentArgs &a0, const MomentBatch &b, int nblocks, size_t smem, bool mixed,
-                                 int variant, const DeferWork &dw, cudaStream_t s);
+                                 int variant, const DeferWork &dw, const ItemQueue &q, cudaStream_t s);
 cudaError_t launch_moments_finalize_batch(const MomentBatch &b, int npoints, cudaStream_t s);
 // dst6[q][idx[t]] = src6[q][t] (moments of n points into a grid of npts)
 cudaError_t launch_scatter6(int n, const int *idx, const double *src6, int npts, double *dst6, cudaStream_t s);
@@ -166,7 +174,8 @@ FJ_HD int defer_words(int chunk) { return (chunk + 31) / 32; }  // bitmap words 
 constexpr int kMixedVariants = 8;    // builds of the mixed kernel (2 forms x 4 register budgets)
 size_t moment_mixed_smem_bytes(const MomentArgs &a);
 int mixed_blocks_per_point(long long nq3, int chunk);
-cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, const DeferWork &dw, cudaStream_t s);
+cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, const DeferWork &dw, const ItemQueue &q,
+                                 cudaStream_t s);
 
 cudaError_t launch_actions(PotView P, const double *Eg, const double *Dg, int ngrid, GLRule gl,
                            const double *pts, size_t n, double *out, cudaStream_t s);

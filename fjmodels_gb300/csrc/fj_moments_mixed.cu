@@ -60,16 +60,16 @@ size_t moment_mixed_smem_bytes(const MomentArgs &a)
 }
 
 
-template <int MINB, bool DYN>
-__global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs a0, MomentBatch batch)
+// One work item: the node range `bid` (global over the launch's models) of
+// one grid point, as described at the top of the file.
+template <bool DYN>
+__device__ __forceinline__ void mixed_item(const MomentArgs &a0, const MomentBatch &batch, int bid, double *sm,
+                                           unsigned *s_bits, int &s_nleft)
 {
-    extern __shared__ double sm[];
-    __shared__ unsigned s_bits[kMixedMaxNodes / 32];  // nodes left to the FP64 pass
-    __shared__ int s_nleft;
     MomentArgs a = a0;
-    int bid = blockIdx.x;
     for (int i = threadIdx.x; i < kMixedMaxNodes / 32; i += blockDim.x) s_bits[i] = 0u;
     if (threadIdx.x == 0) s_nleft = 0;
+    __syncthreads();
     if (batch.n > 0) {
         const int m = batch_model(batch.block_start, batch.n, bid);
         a = batch.args[m];
@@ -229,6 +229,31 @@ __global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs 
         if (threadIdx.x == 0) a.defer_count[(size_t)p * B + chunk] = s_nleft;
     }
     if (threadIdx.x == 0 && nbound) atomicAdd(&a.counters[kCntBound], (unsigned long long)nbound);
+}
+
+// The persistent kernel: a grid of at most as many blocks as fit on the GPU at
+// once takes work items from the queue (an atomic counter) until none is
+// left, in the queue's order (most expensive first, from the previous launch's
+// measured cycles, when the context has them), and records each item's cycles.
+// Blocks free up as their items finish and take the next one, so the uneven
+// cost of the root finding and quadrature is balanced across the GPU.
+template <int MINB, bool DYN>
+__global__ void __launch_bounds__(kMixedBlock, MINB) k_moments_mixed(MomentArgs a0, MomentBatch batch, ItemQueue q)
+{
+    extern __shared__ double sm[];
+    __shared__ unsigned s_bits[kMixedMaxNodes / 32];  // nodes left to the FP64 pass
+    __shared__ int s_nleft, s_item;
+    for (;;) {
+        __syncthreads();  // every thread is done with the previous item's shared data
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(q.next, 1u);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= q.total) return;
+        const int bid = q.order ? q.order[it] : it;
+        const long long t0 = clock64();
+        mixed_item<DYN>(a0, batch, bid, sm, s_bits, s_nleft);
+        if (q.cost && threadIdx.x == 0) q.cost[bid] = (float)(clock64() - t0);
+    }
 }
 
 // ------------------------------------------------------ the FP64 pass
@@ -456,30 +481,38 @@ static cudaError_t launch_deferred(const MomentArgs &a, const MomentBatch &b, lo
 
 namespace {
 template <int MINB, bool DYN>
-cudaError_t launch_variant(const MomentArgs &a, const MomentBatch &b, long long nblocks, size_t smem,
-                           cudaStream_t s)
+cudaError_t launch_variant(const MomentArgs &a, const MomentBatch &b, const ItemQueue &q, size_t smem, cudaStream_t s)
 {
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(k_moments_mixed<MINB, DYN>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    k_moments_mixed<MINB, DYN><<<(unsigned)nblocks, kMixedBlock, smem, s>>>(a, b);
+    int dev = 0, nsm = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_moments_mixed<MINB, DYN>, kMixedBlock, smem);
+    if (e != cudaSuccess) return e;
+    const long long resident = (long long)(per_sm > 0 ? per_sm : 1) * (nsm > 0 ? nsm : 1);
+    const long long grid = q.total < resident ? q.total : resident;
+    if ((e = cudaMemsetAsync(q.next, 0, sizeof(unsigned), s)) != cudaSuccess) return e;
+    k_moments_mixed<MINB, DYN><<<(unsigned)grid, kMixedBlock, smem, s>>>(a, b, q);
     return cudaGetLastError();
 }
 
-cudaError_t launch_mixed_any(const MomentArgs &a, const MomentBatch &b, long long nblocks, size_t smem, int variant,
+cudaError_t launch_mixed_any(const MomentArgs &a, const MomentBatch &b, const ItemQueue &q, size_t smem, int variant,
                              cudaStream_t s)
 {
     switch (variant) {
-    case 0: return launch_variant<3, false>(a, b, nblocks, smem, s);
-    case 1: return launch_variant<4, false>(a, b, nblocks, smem, s);
-    case 2: return launch_variant<6, false>(a, b, nblocks, smem, s);
-    case 3: return launch_variant<8, false>(a, b, nblocks, smem, s);
-    case 4: return launch_variant<3, true>(a, b, nblocks, smem, s);
-    case 5: return launch_variant<4, true>(a, b, nblocks, smem, s);
-    case 6: return launch_variant<6, true>(a, b, nblocks, smem, s);
-    case 7: return launch_variant<8, true>(a, b, nblocks, smem, s);
+    case 0: return launch_variant<3, false>(a, b, q, smem, s);
+    case 1: return launch_variant<4, false>(a, b, q, smem, s);
+    case 2: return launch_variant<6, false>(a, b, q, smem, s);
+    case 3: return launch_variant<8, false>(a, b, q, smem, s);
+    case 4: return launch_variant<3, true>(a, b, q, smem, s);
+    case 5: return launch_variant<4, true>(a, b, q, smem, s);
+    case 6: return launch_variant<6, true>(a, b, q, smem, s);
+    case 7: return launch_variant<8, true>(a, b, q, smem, s);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -492,13 +525,15 @@ size_t local_bytes()
 }
 }  // namespace
 
-cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, const DeferWork &dw, cudaStream_t s)
+cudaError_t launch_moments_mixed(const MomentArgs &a, int variant, const DeferWork &dw, const ItemQueue &q,
+                                 cudaStream_t s)
 {
     if (a.mixed_chunk < kMixedBlock || a.mixed_chunk > kMixedMaxNodes) return cudaErrorInvalidValue;
     const size_t smem = moment_mixed_smem_bytes(a);
     const MomentBatch none{nullptr, nullptr, nullptr, 0};
     const long long nblocks = (long long)a.npts * a.blocks_per_point;
-    cudaError_t e = launch_mixed_any(a, none, nblocks, smem, variant, s);
+    if (q.total != nblocks) return cudaErrorInvalidValue;
+    cudaError_t e = launch_mixed_any(a, none, q, smem, variant, s);
     if (e == cudaSuccess) e = launch_deferred(a, none, nblocks, dw, s);
     if (e != cudaSuccess) return e;
     return launch_moments_finalize(a, s);
@@ -508,10 +543,11 @@ cudaError_t launch_moments_plain_batch(const MomentArgs &a0, const MomentBatch &
                                       cudaStream_t s);
 
 cudaError_t launch_moments_batch(const MomentArgs &a0, const MomentBatch &b, int nblocks, size_t smem, bool mixed,
-                                 int variant, const DeferWork &dw, cudaStream_t s)
+                                 int variant, const DeferWork &dw, const ItemQueue &q, cudaStream_t s)
 {
     if (!mixed) return launch_moments_plain_batch(a0, b, nblocks, smem, s);
-    const cudaError_t e = launch_mixed_any(a0, b, nblocks, smem, variant, s);
+    if (q.total != nblocks) return cudaErrorInvalidValue;
+    const cudaError_t e = launch_mixed_any(a0, b, q, smem, variant, s);
     return e == cudaSuccess ? launch_deferred(a0, b, nblocks, dw, s) : e;
 }
 

@@ -3,7 +3,8 @@ tabulateDelta code, delta/tabulate.cpp:13-38 and delta/Delta.cpp, one thread per
 (model, energy), 8 per block).  The focal-distance fit is not continuous in rounding (one unit in
 the last place of the orbit equations moves entries by tens of per cent; the host code
 does the same), so the GPU table is checked for what is stable: the energies against
-the host's and the reference's to 1e-12, run-to-run identity, and the density moments a
+the host's and the reference's to 1e-12, every focal distance within the spread the fit
+itself shows under one-ulp perturbations, run-to-run identity, and the density moments a
 table gives -- within a few per cent of the host table's (the Staeckel fudge depends on
 the focal distance only through the quality of its fit; 2.6e-2 measured on the GB300,
 bound 5e-2).  In the model loops: a GPU table gives
@@ -77,14 +78,32 @@ def test_gpu_table_against_host_table(ctx):
     assert drho < 5e-2
 
 
-@pytest.mark.parametrize("name", ["hern_dpl", "nfw_dpl_rot"])
-def test_gpu_table_energies_match_reference(ctx, name):
+@pytest.mark.parametrize("name", ["hern_dpl", "nfw_dpl_rot", "c1_hern", "twocomp_ref"])
+def test_gpu_table_entrywise_against_reference(ctx, name):
+    """The GPU table against the reference's own (the fixture's, which the host code
+    reproduces bit for bit), entry by entry.  The fit is chaotic in rounding, so the bound
+    is the fit's own spread: the host tables of the same potential with its multipoles
+    scaled by 1 + j 2^-52, j = -16..16, give each entry an envelope [lo, hi]; each GPU
+    entry must lie within it widened by half its width on each side, and at least 90 % of
+    them inside it (measured: 115 of 120 inside, the rest within 0.34 widths).  The
+    energies agree to 1e-12."""
     g, meta, _ = load_golden(name)
     nr, npl = meta["nr"], meta["np"]
-    pot = ctx.potential(dev(g["ar"]), dev(g["guess_phil"].reshape(nr, npl)), dev(g["guess_Pr"].reshape(nr, npl)),
-                        dev(g["guess_Pr2"].reshape(nr, npl)))
+    tabs = [g[k].reshape(nr, npl) for k in ("guess_phil", "guess_Pr", "guess_Pr2")]
+    pot = ctx.potential(dev(g["ar"]), *[dev(t) for t in tabs])
     E, D, _ = ctx.tabulate_delta_batch([pot], 30)
-    assert rel(E.cpu().numpy()[0], g["Egrid"]) < 1e-12 and np.all(np.isfinite(D.cpu().numpy()))
+    E, D = E.cpu().numpy()[0], D.cpu().numpy()[0]
+    assert rel(E, g["Egrid"]) < 1e-12
+    host = np.array([F.tabulate_delta(g["ar"], tabs[0] * (1 + j * 2.0 ** -52), tabs[1], tabs[2])[1]
+                     for j in range(-16, 17)])
+    assert np.array_equal(host[16], g["Dgrid"])  # the unperturbed host table is the reference's
+    lo, hi = host.min(0), host.max(0)
+    w = hi - lo
+    inside = (D >= lo) & (D <= hi)
+    print(f"{name}: {inside.sum()}/30 GPU entries inside the host envelope; median |dD2/D2| against the "
+          f"reference {np.median(np.abs(D - g['Dgrid']) / np.abs(g['Dgrid'])):.3f}")
+    assert np.all((D >= lo - w / 2) & (D <= hi + w / 2))
+    assert inside.sum() >= 27
 
 
 MODELS = [dict(nr=32, ngauss=12, npoly=4, rmin=1e-2, rmax=100.0, df=F.DFParams("Hernquist")),
