@@ -112,11 +112,11 @@ def _nfw_80_tanh():
 
 def test_surrogate_moments_gain(ctx):
     """Fit to one exact iteration of the 80 x 40 rotating NFW workload (22^3 tanh-sinh
-    nodes), then the surrogate's grid of moments.  The fused tensor-core kernel equals
-    the separate passes and is > 20x faster than the exact mixed kernel; the
-    densities are only within tens of per cent (median 15 % measured), so the
-    schedule's audit keeps the iterations exact -- the accuracy bound here guards
-    against regressions of the fit, not a target."""
+    nodes), then the surrogate's grid of moments.  What the trained network gains over the
+    same network untrained: its densities' median error falls from 100 % to 8 %; over the
+    exact kernel: the fused tensor-core kernel (equal to the separate passes) is > 20x
+    faster.  The accuracy (median 8 %, 90th percentile 63 % measured) is what keeps it out
+    of the chosen form: as a warm start it saves no exact iterations."""
     from fjmodels_gb300 import _abi as A
     (nr, ng, npl), tabs, (E, D) = _nfw_80_tanh()
     pot, delta = ctx.potential(*tabs), ctx.delta(E, D)
@@ -128,6 +128,13 @@ def test_surrogate_moments_gain(ctx):
     ctx.set_action_output(jout)
     st = ctx.moments(pot, delta, df, rule, ng, g_exact)
     ctx.set_action_output(None)
+    b = g_exact[0].cpu().numpy().ravel()
+    untrained = F.Surrogate(ctx, batch=8192, seed=3)
+    g_un = torch.zeros_like(g_exact)
+    untrained.moments(pot, df, rule, ng, g_un)
+    torch.cuda.synchronize()
+    rel_un = np.abs(g_un[0].cpu().numpy().ravel() - b) / b
+    untrained.close()
     s = F.Surrogate(ctx, batch=8192, seed=3)
     loss = s.fit(pot, df, ng, rule, jout, 1 << 20, seed=5, epochs=24, lr=2e-3, rho=g_exact[0].reshape(-1))
     g_sg = torch.zeros_like(g_exact)
@@ -142,29 +149,38 @@ def test_surrogate_moments_gain(ctx):
           f"{np.max(np.abs(g_sg[0].cpu().numpy().ravel() - ru) / ru):.2e}")
     assert np.max(np.abs(g_sg[0].cpu().numpy().ravel() - ru) / ru) < 1e-3
     assert ms < st.kernel_ms / 20
-    a, b = g_sg[0].cpu().numpy().ravel(), g_exact[0].cpu().numpy().ravel()
-    rel = np.abs(a - b) / b
-    print(f"surrogate: fit loss {loss:.3e}, moments {ms:.1f} ms vs exact {st.kernel_ms:.1f} ms, "
-          f"rho rel err median {np.median(rel):.2e} p90 {np.percentile(rel, 90):.2e} max {rel.max():.2e}")
-    assert np.median(rel) < 0.3
+    rel = np.abs(g_sg[0].cpu().numpy().ravel() - b) / b
+    print(f"surrogate: fit loss {loss:.3e}, moments {ms:.1f} ms vs exact {st.kernel_ms:.1f} ms, rho rel err median "
+          f"{np.median(rel):.2e} p90 {np.percentile(rel, 90):.2e} (untrained: median {np.median(rel_un):.2e})")
+    assert np.median(rel) < 0.12 and np.percentile(rel, 90) < 0.8
+    assert np.median(rel) < 0.5 * np.median(rel_un)
     s.close()
 
 
 def test_surrogate_schedule(ctx):
-    """The surrogate-accelerated loop (exact first and last iterations) lands within
-    1e-3 of the exact mixed loop after the same number of iterations, on a smaller NFW
-    model, and reports its iteration kinds."""
+    """The surrogate as a warm start of the loop, on a smaller NFW model: an exact first
+    iteration (the fit), three surrogate iterations (no audit fallback), then exact
+    iterations until converged.  The converged model is the exact loop's (density
+    multipoles within 1e-4); the exact iterations it takes are printed next to the exact
+    loop's: the surrogate saves none on this workload (it is not part of the chosen form)."""
     from fjmodels_gb300 import _abi as A
+    from tests.helpers import rel_rows
     rule = F.Rule(*F.tanh_sinh_rule(16), precision=A.FJ_PREC_MIXED)
     df = F.DFParams("NFW", chi=1.0, k=0.5)
     args = (40, 16, 5, 1e-3, 300.0, df, rule)
-    ref = ctx.run_model(*args, itermax=8)
-    s = F.Surrogate(ctx, batch=4096, seed=9)
-    out, rep = ctx.run_model_surrogate(*args, itermax=8, surrogate=s, samples=1 << 18, epochs_first=8, epochs=2,
-                                       lr=2e-3, exact_first=1, exact_last=3, audit_stride=50, audit_tol=0.05)
-    print("schedule report", rep)
-    assert out["iterations"] == 8
-    assert rep["surrogate_iterations"] + rep["fallback_iterations"] == 4 and rep["fits"] >= 1
-    from tests.helpers import rel_rows
-    assert rel_rows(out["phil"], ref["phil"]) < 1e-3
-    s.close()
+    ctx.set_poisson(A.FJ_POISSON_CUMULATIVE)
+    try:
+        ref = ctx.run_model(*args, itermax=100, tol=1e-5)
+        s = F.Surrogate(ctx, batch=4096, seed=9)
+        S, T = 3, 60
+        out, rep = ctx.run_model_surrogate(*args, itermax=1 + S + T, surrogate=s, tol=1e-5, samples=1 << 18,
+                                           epochs_first=8, epochs=8, lr=2e-3, exact_first=1, exact_last=T,
+                                           audit_stride=50, audit_tol=10.0)
+        s.close()
+    finally:
+        ctx.set_poisson(A.FJ_POISSON_QAGS)
+    print(f"exact loop: {ref['iterations']} iterations; warm start: {rep['surrogate_iterations']} surrogate + "
+          f"{out['iterations'] - rep['surrogate_iterations']} exact; report {rep}")
+    assert rep["surrogate_iterations"] == S and rep["fallback_iterations"] == 0 and rep["fits"] == 1
+    assert out["last_change"] < 1e-5 and out["iterations"] < 1 + S + T
+    assert rel_rows(out["coef6"][0], ref["coef6"][0]) < 1e-4
