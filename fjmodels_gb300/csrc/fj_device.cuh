@@ -964,10 +964,19 @@ FJ_HDNI double mom_integral(F &f, double b, const GLRule &gl, unsigned &fail)
     return s;
 }
 
-// Actions of one phase-space point: uvOrb ctor (uvOrb.cpp:15-36), Ju, Jv.
+// The momentum integrals of one thread: QAGS or fixed Gauss-Legendre (mom_integral)
+struct SerialMomInt {
+    const GLRule *gl;
+    template <class F>
+    FJ_HD double operator()(F &f, double b, unsigned &fail) const { return mom_integral(f, b, *gl, fail); }
+};
+
+// Actions of one phase-space point: uvOrb ctor (uvOrb.cpp:15-36), Ju, Jv, the
+// momentum integrals by mi(integrand, upper limit, fail).
 // Returns false for an unbound orbit (Jr = Jz = 1e31).
-FJ_HDNI bool fudge_actions(const PotView &P, double Delta, double R, double z, double Phi, double pR,
-                         double vphi, double pz, const GLRule &gl, double &Jr, double &Jz, unsigned &fail)
+template <class MI>
+FJ_HDNI bool fudge_actions_with(const PotView &P, double Delta, double R, double z, double Phi, double pR,
+                                double vphi, double pz, const MI &mi, double &Jr, double &Jz, unsigned &fail)
 {
     Fudge o;
     o.P = P;
@@ -1025,17 +1034,23 @@ FJ_HDNI bool fudge_actions(const PotView &P, double Delta, double R, double z, d
         o.ubar = .5 * (o.uinner + o.uouter);
         o.Deltau = .5 * (o.uouter - o.uinner);
         JuIntF fju{&o};
-        Jr = rtwo * Delta * o.Deltau * mom_integral(fju, kPI, gl, o.fail) / kPI;
+        Jr = rtwo * Delta * o.Deltau * mi(fju, kPI, o.fail) / kPI;
     }
     // Jv (uvOrb.cpp:247-257)
     o.vturn = get_turn_v(o, .5 * kPIH);
     if (fabs(o.vturn - kPIH) < kTINY) Jz = 0;
     else {
         JvIntF fjv{&o};
-        Jz = 2 * rtwo * Delta * (kPIH - o.vturn) * mom_integral(fjv, kPIH, gl, o.fail) / kPI;
+        Jz = 2 * rtwo * Delta * (kPIH - o.vturn) * mi(fjv, kPIH, o.fail) / kPI;
     }
     fail |= o.fail;
     return true;
+}
+
+FJ_HDNI bool fudge_actions(const PotView &P, double Delta, double R, double z, double Phi, double pR,
+                         double vphi, double pz, const GLRule &gl, double &Jr, double &Jz, unsigned &fail)
+{
+    return fudge_actions_with(P, Delta, R, z, Phi, pR, vphi, pz, SerialMomInt{&gl}, Jr, Jz, fail);
 }
 
 // ----------------------------------------------------------------------------

@@ -11,6 +11,7 @@
 #include "fj_internal.h"
 #include "fj_mixed.cuh"
 #include "fj_order.cuh"
+#include "fj_qags_warp.cuh"
 
 namespace fj {
 
@@ -287,9 +288,30 @@ __device__ void defer_point(const MomentArgs &a, int bid, double &R, double &z, 
     Ve = sqrt(-2 * (Phi_h - pot_phi(P, 10 * rmax, 10 * rmax)));
 }
 
-// one left node with the plain form's FP64 solve (fudge_actions with QAGS lists
-// of kQagsCap intervals, df_value): its six moment contributions
-__device__ void defer_solve(const MomentArgs &a, int bid, int node, double *c6, FailTally &tally)
+// The momentum integrals of a warp: QAGS with the panels spread over the lanes
+struct WarpMomInt {
+    WarpQagsWs w;
+    int lane;
+    template <class F>
+    FJ_HD double operator()(F &f, double b, unsigned &fail) const
+    {
+#ifdef __CUDA_ARCH__
+        double r, e;
+        qags_warp<21>(f, 0.0, b, 1e-5, 1e-3, 1000, r, e, fail, w.ws(), w.buf, lane);
+        return r;
+#else
+        (void)f; (void)b; (void)fail;
+        return 0.;
+#endif
+    }
+};
+
+// one left node with the plain form's FP64 solve (the actions with QAGS lists
+// of kQagsCap intervals, df_value) by a whole warp (every lane calls it with the
+// same node; the turning points run on every lane, the momentum integrals
+// spread their panels over the lanes): its six moment contributions
+__device__ void defer_solve(const MomentArgs &a, int bid, int node, double *c6, FailTally &tally,
+                            const WarpQagsWs &w, int lane)
 {
     double R, z, Phi_h, Ve;
     defer_point(a, bid, R, z, Phi_h, Ve);
@@ -300,15 +322,17 @@ __device__ void defer_solve(const MomentArgs &a, int bid, int node, double *c6, 
     const double H = .5 * (V0 * V0 + V1 * V1 + V2 * V2) + Phi_h;
     unsigned fail = 0;
     double Jr, Jz;
-    const GLRule qags{0, nullptr, nullptr};
-    fudge_actions(P, deltafn(a.Eg, a.Dg, a.ngrid, H), R, z, Phi_h, V0, V1, V2, qags, Jr, Jz, fail);
+    fudge_actions_with(P, deltafn(a.Eg, a.Dg, a.ngrid, H), R, z, Phi_h, V0, V1, V2, WarpMomInt{w, lane}, Jr, Jz,
+                       fail);
     double DF = df_value(a.df, P, R, Jr, Jz, R * V1, fail);
     if (fail & (kFailBracket | kFailRoot)) DF = 0.;
-    tally.add(fail);
-    if (a.jout) {
-        float *jo = a.jout + ((size_t)(bid / a.blocks_per_point) * nq2 * nq + node) * 2;
-        jo[0] = (float)Jr;
-        jo[1] = (float)Jz;
+    if (lane == 0) {
+        tally.add(fail);
+        if (a.jout) {
+            float *jo = a.jout + ((size_t)(bid / a.blocks_per_point) * nq2 * nq + node) * 2;
+            jo[0] = (float)Jr;
+            jo[1] = (float)Jz;
+        }
     }
     const double jd = (a.wq[i] * a.wq[j] * a.wq[l]) * (Ve * Ve * Ve * DF);
     c6[0] = jd; c6[1] = jd * V1; c6[2] = jd * V0 * V0;
@@ -407,34 +431,52 @@ __global__ void __launch_bounds__(32 * kListWarps) k_defer_list(MomentArgs a0, M
     }
 }
 
-// one thread per listed node (grid-stride over the launch's total)
-__global__ void __launch_bounds__(64) k_defer_solve(MomentArgs a0, MomentBatch batch, DeferWork dw, int nchunks)
+// one warp per listed node (grid-stride over the launch's total)
+constexpr int kSolveWarps = 4;
+__global__ void __launch_bounds__(32 * kSolveWarps) k_defer_solve(MomentArgs a0, MomentBatch batch, DeferWork dw,
+                                                                   int nchunks)
 {
+    __shared__ double s_list[kSolveWarps][4 * kQagsCap];
+    __shared__ int s_iord[kSolveWarps][kQagsCap];
+    __shared__ double s_buf[kSolveWarps][42];
+    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+    const WarpQagsWs w{s_list[wq], s_iord[wq], s_buf[wq], kQagsCap};
     const int total = min(dw.chunk_sum[nchunks], dw.cap);
     FailTally tally;
     unsigned solved = 0;
     unsigned long long *counters = a0.counters;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+    for (int e = blockIdx.x * kSolveWarps + wq; e < total; e += gridDim.x * kSolveWarps) {
         int bid;
         const MomentArgs &a = block_args(a0, batch, dw.block[e], bid);
         counters = a.counters;
-        defer_solve(a, bid, dw.node[e], dw.mom + (size_t)e * 6, tally);
-        solved++;
+        double c6[6];
+        defer_solve(a, bid, dw.node[e], c6, tally, w, lane);
+        if (lane == 0) {
+            for (int q = 0; q < 6; q++) dw.mom[(size_t)e * 6 + q] = c6[q];
+            solved++;
+        }
     }
-    add_tally(counters, tally, solved);
+    if (lane == 0) add_tally(counters, tally, solved);
 }
 
-// one thread per block: its listed nodes added in list order (nodes beyond the
-// list's capacity solved here, in node order)
-__global__ void __launch_bounds__(128) k_defer_add(MomentArgs a0, MomentBatch batch, DeferWork dw, int nblocks)
+// one warp per block: its listed nodes added in list order by lane 0 (nodes
+// beyond the list's capacity solved here by the warp, in node order)
+constexpr int kAddWarps = 4;
+__global__ void __launch_bounds__(32 * kAddWarps) k_defer_add(MomentArgs a0, MomentBatch batch, DeferWork dw,
+                                                               int nblocks)
 {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= nblocks) return;
+    __shared__ double s_list[kAddWarps][4 * kQagsCap];
+    __shared__ int s_iord[kAddWarps][kQagsCap];
+    __shared__ double s_buf[kAddWarps][42];
+    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5;
+    const int g = blockIdx.x * kAddWarps + wq;
+    if (g >= nblocks) return;  // the whole warp
     const int cnt = dw.count[g];
     if (cnt == 0) return;
     int bid;
     const MomentArgs &a = block_args(a0, batch, g, bid);
     const int off = dw.offset[g];
+    const WarpQagsWs w{s_list[wq], s_iord[wq], s_buf[wq], kQagsCap};
     double msum[6] = {0, 0, 0, 0, 0, 0};
     FailTally tally;
     unsigned solved = 0;
@@ -449,18 +491,20 @@ __global__ void __launch_bounds__(128) k_defer_add(MomentArgs a0, MomentBatch ba
         const long long nq3 = (long long)a.nq * a.nq * a.nq;
         const int n0 = (int)((bid % B) * nq3 / B);
         const unsigned *bits = a.defer + (size_t)bid * nw;
-        int r = k, w = 0;
-        while (r >= __popc(bits[w])) r -= __popc(bits[w++]);
-        unsigned word = bits[w];
+        int r = k, wd = 0;
+        while (r >= __popc(bits[wd])) r -= __popc(bits[wd++]);
+        unsigned word = bits[wd];
         for (int t = 0; t < r; t++) word &= word - 1;
         double c6[6];
-        defer_solve(a, bid, n0 + w * 32 + (__ffs((int)word) - 1), c6, tally);
+        defer_solve(a, bid, n0 + wd * 32 + (__ffs((int)word) - 1), c6, tally, w, lane);
         solved++;
         for (int q = 0; q < 6; q++) msum[q] += c6[q];
     }
-    double *pt = a.partial + (size_t)bid * 6;
-    for (int q = 0; q < 6; q++) pt[q] += msum[q];
-    add_tally(a.counters, tally, solved);
+    if (lane == 0) {
+        double *pt = a.partial + (size_t)bid * 6;
+        for (int q = 0; q < 6; q++) pt[q] += msum[q];
+        add_tally(a.counters, tally, solved);
+    }
 }
 
 static cudaError_t launch_deferred(const MomentArgs &a, const MomentBatch &b, long long nblocks, const DeferWork &dw,
@@ -474,8 +518,8 @@ static cudaError_t launch_deferred(const MomentArgs &a, const MomentBatch &b, lo
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    k_defer_solve<<<8 * (nsm > 0 ? nsm : 1), 64, 0, s>>>(a, b, dw, nchunks);
-    k_defer_add<<<(nb + 127) / 128, 128, 0, s>>>(a, b, dw, nb);
+    k_defer_solve<<<4 * (nsm > 0 ? nsm : 1), 32 * kSolveWarps, 0, s>>>(a, b, dw, nchunks);
+    k_defer_add<<<(nb + kAddWarps - 1) / kAddWarps, 32 * kAddWarps, 0, s>>>(a, b, dw, nb);
     return cudaGetLastError();
 }
 

@@ -3,6 +3,7 @@
 // component potentials and the tensor-virial sums.  All FP64; each is small
 // next to the phase-space kernel.
 #include "fj_internal.h"
+#include "fj_qags_warp.cuh"
 
 namespace fj {
 
@@ -78,46 +79,6 @@ struct IExternalT {  // I_external (pot/Potential.cpp:90-101) on x = a + (1-t)/t
 // per pair the 2 nr npoly integrals (560 on 80 x 7) sat on a few SMs, each
 // thread evaluating its thousands of integrand values one after another.
 constexpr int kPoissonWarps = 4;
-
-template <int RULE, class F>
-struct WarpPanels64 {
-    F &f;
-    double *buf;
-    int lane;
-    __device__ void one(double a, double b, double &r, double &e, double &ra, double &rc)
-    {
-        constexpr int n = GKRule<RULE>::npts;
-        for (int i = lane; i < n; i += 32) buf[i] = f(gk_abscissa<RULE>(a, b, i));
-        __syncwarp();
-        gk_sum<RULE>(a, b, buf, r, e, ra, rc);
-        __syncwarp();
-    }
-    __device__ void two(double a1, double b1, double a2, double b2, double &r1, double &e1, double &ra1,
-                        double &rc1, double &r2, double &e2, double &ra2, double &rc2)
-    {
-        constexpr int n = GKRule<RULE>::npts;
-        for (int i = lane; i < 2 * n; i += 32) {
-            const bool second = i >= n;
-            buf[i] = f(gk_abscissa<RULE>(second ? a2 : a1, second ? b2 : b1, second ? i - n : i));
-        }
-        __syncwarp();
-        gk_sum<RULE>(a1, b1, buf, r1, e1, ra1, rc1);
-        gk_sum<RULE>(a2, b2, buf + n, r2, e2, ra2, rc2);
-        __syncwarp();
-    }
-};
-
-template <int RULE, class F>
-__device__ int qags_warp(F &f, double a, double b, double epsabs, double epsrel, int limit, double &result,
-                         double &abserr, unsigned &fail, const QagsWs &ws, double *buf, int lane)
-{
-    WarpPanels64<RULE, F> pn{f, buf, lane};
-    double res0, err0, resabs0, resasc0;
-    pn.one(a, b, res0, err0, resabs0, resasc0);
-    const int h = qags_head(res0, err0, resabs0, resasc0, epsabs, epsrel, limit, result, abserr);
-    if (h >= 0) return h;
-    return qags_rest<RULE>(pn, a, b, res0, err0, resabs0, epsabs, epsrel, limit, result, abserr, fail, ws);
-}
 
 // computeInts + computePhil (pot/Potential.cpp:110-200)
 __global__ void __launch_bounds__(32 * kPoissonWarps) k_poisson(int nr, int npoly, const double *ar,
