@@ -86,8 +86,9 @@ def parse():
     ap.add_argument("--mixed-config", default=None,
                     help="variant,nodes_per_block of the mixed kernel (default: autotuned before warm-up)")
     ap.add_argument("--cpu-sample", type=int, default=0,
-                    help="grid points timed for the CPU baseline (default: 10 per host thread for the cpu_baseline "
-                         "key, about 10 s; 2 per host thread for each step of --impl reference)")
+                    help="grid points timed for the CPU baseline, spread over the grid (default: 10 per host thread, "
+                         "about 6 s on the 16-core box; the same sample for the cpu_baseline key and each step of "
+                         "--impl reference)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
@@ -565,7 +566,7 @@ def main():
             flush.fill(0.0)
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            res.append(cpu_sample(args, sample=args.cpu_sample or 2 * os.cpu_count()))
+            res.append(cpu_sample(args, sample=args.cpu_sample or 10 * os.cpu_count()))
             flush.fill(0.0)
         wall = time.perf_counter() - t0
         v = float(np.mean([r["value"] for r in res]))
