@@ -144,3 +144,21 @@ def test_rk8pd_tableau_order_conditions_and_tables():
     b = _header_numbers(os.path.join(root, "fjmodels_gb300", "csrc", "fj_rk8pd.h"))
     assert a.shape == b.shape == (13 + 13 * 12 + 13 + 13,) and np.array_equal(a, b)
 
+
+
+def test_counting_oracle_is_the_oracle_bit_for_bit():
+    """oracle/orc_flops.cpp (the oracle with every floating-point operation tallied, the
+    source of the bench's algorithmic FLOPs) gives the oracle's moments bit for bit, and
+    counts every kind of operation."""
+    ar = O.log_grid(1e-2, 100.0, 12)
+    rhl = O.guess_rhl(ar, 4, 3, "Hernquist")
+    phil, Pr, Pr2 = O.compute_phil(ar, rhl)
+    m = O.Model(ar, phil, Pr, Pr2, np.zeros(30), np.zeros(30), 4)
+    E, D, _ = m.tabulate_delta(30)
+    m.Egrid, m.Dgrid = E, D
+    pts = [21]
+    mom, counts = O.flop_counts(m, pts)
+    grids, _ = m.moment_grid(pts[0], pts[0] + 1, nthreads=1)
+    assert np.array_equal(mom, grids[:, pts])
+    assert all(counts[k] > 0 for k in ("add", "mul", "div", "sqrt", "trans"))
+    assert counts["mul"] > counts["div"] > counts["sqrt"]
