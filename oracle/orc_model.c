@@ -869,6 +869,7 @@ void orc_vir2(const orc_model *m, const double *coef6, double *out7)
             /* ev_dens, 5-field (UtilsLeg.h:337-354) with the float weight of int_dens (:312) */
             double c = z / sqrt(R * R + z * z), rr = sqrt(R * R + z * z);
             double densp[MAXP], Vrotp[MAXP], sigup[MAXP], sigpp[MAXP], sigvp[MAXP];
+            densp[0] = Vrotp[0] = sigup[0] = sigpp[0] = sigvp[0] = 0; /* npoly >= 1 overwrites */
             orc_evenlegend(npoly, c, pol);
             if (rr > ar[nr - 1]) {
                 for (int k = 0; k < npoly; k++) densp[k] = Vrotp[k] = sigup[k] = sigpp[k] = sigvp[k] = 0;
