@@ -65,7 +65,8 @@ class fj_model_config(C.Structure):
                 ("Egrid_in", DP), ("Dgrid_in", DP), ("ncomp", C.c_int), ("guess2", C.c_int),
                 ("mass2", C.c_double), ("r0_2", C.c_double), ("q2", C.c_double), ("df2", fj_df_params),
                 ("twocomp_order", C.c_int), ("ar_in", DP), ("phil_in", DP), ("Pr_in", DP), ("Pr2_in", DP),
-                ("delta_gpu", C.c_int), ("delta_every", C.c_int), ("ext_phil", DP), ("ext_Pr", DP), ("ext_Pr2", DP)]
+                ("delta_gpu", C.c_int), ("delta_every", C.c_int), ("ext_phil", DP), ("ext_Pr", DP), ("ext_Pr2", DP),
+                ("accel", C.c_int)]
 
 
 class fj_model_result(C.Structure):
@@ -76,11 +77,14 @@ class fj_model_result(C.Structure):
 
 
 P = C.POINTER
+FJ_ANDERSON_MAX_DEPTH = 8
 FJ_LOS_SIGMA, FJ_LOS_LINE, FJ_LOS_PVPHI, FJ_LOS_PVZ, FJ_LOS_PVR = range(5)
 CTX = C.c_void_p
 SIGNATURES = {
     "fj_version": ([], C.c_char_p),
     "fj_ctx_create": ([C.c_int, P(C.c_void_p)], C.c_int),
+    "fj_anderson_reset": ([CTX, C.c_int], C.c_int),
+    "fj_anderson_step": ([CTX, C.c_int, C.c_int, C.c_void_p, C.c_void_p, DP], C.c_int),
     "fj_ctx_destroy": ([CTX], C.c_int),
     "fj_ctx_set_stream": ([CTX, C.c_void_p], C.c_int),
     "fj_ctx_own_stream": ([CTX], C.c_void_p),

@@ -396,9 +396,25 @@ class Context:
         return dict(zip(("KRR", "Kzz", "WRR", "Wzz", "pot", "mass_pr", "mass_sum"), out))
 
     # ---------------------------------------------------------------- whole model
+    def anderson_reset(self, depth):
+        """Start a new mixed iteration with history depth m (fj_anderson_reset; 0 = plain steps)."""
+        self._check(self.lib.fj_anderson_reset(self.h, int(depth)), "fj_anderson_reset")
+
+    def anderson_step(self, x, g):
+        """One Anderson step (fj_anderson_step): x, g are contiguous device tensors [3][nr][npoly]
+        (phil, Pr, Pr2) of the last input and its computeNewPhi output; x is overwritten with the
+        next input.  Returns the plain step's change max|dphil|/|phil(r, 0)|."""
+        if x.shape != g.shape or x.dim() != 3 or x.shape[0] != 3 or not (x.is_contiguous() and g.is_contiguous()):
+            raise FJError("anderson_step: x and g must be contiguous [3][nr][npoly] tensors")
+        self._on_torch_stream()
+        ch = np.zeros(1)
+        self._check(self.lib.fj_anderson_step(self.h, x.shape[1], x.shape[2], _ptr(x), _ptr(g), _dp(ch)),
+                    "fj_anderson_step")
+        return float(ch[0])
+
     def run_model(self, nr, ngauss, npoly, rmin, rmax, df, rule, itermax, tol=0.0, ngrid=30, q=1.0,
                   keep_grids=False, delta_table=None, df2=None, q2=1.0, twocomp_order=A.FJ_TWOCOMP_SUMMED,
-                  restart=None, delta_gpu=False, delta_every=0, ext=None):
+                  restart=None, delta_gpu=False, delta_every=0, ext=None, accel=0):
         """Self-consistent model (oneComp, fJmodels.cpp:86-144; with df2, the two-component
         loop of fJmodels.cpp:38-84 in `twocomp_order`) with host buffers.
         delta_table = (Egrid, Dgrid) uses a given focal-distance table instead of tabulating one;
@@ -407,12 +423,15 @@ class Context:
         delta_gpu tabulates the focal-distance table on the GPU; delta_every = k > 0 tabulates it
         again from the new potential after every k-th iteration (the reference: once).
         ext = (phil, Pr, Pr2) of a fixed external potential added after the guess and after every
-        iteration (the reference's external mode, fJmodels.cpp:120-125, 134)."""
+        iteration (the reference's external mode, fJmodels.cpp:120-125, 134).
+        accel = m > 0 mixes each next input potential from the last m + 1 outputs (Anderson;
+        the reference iterates the plain map); with tol the loop then ends with a confirming
+        plain step."""
         self.use_own_stream()
         din = [None, None] if delta_table is None else [_f64(delta_table[0]), _f64(delta_table[1])]
         cfg = A.fj_model_config(nr, ngauss, npoly, ngrid, rmin, rmax, A.FJ_GUESS.get(df.model, 0), df.mass, df.r0,
                                 q, df.c, rule.c, itermax, tol, *[_dp(d) if d is not None else None for d in din])
-        cfg.delta_gpu, cfg.delta_every = int(delta_gpu), int(delta_every)
+        cfg.delta_gpu, cfg.delta_every, cfg.accel = int(delta_gpu), int(delta_every), int(accel)
         if ext is not None:
             ex = [_f64(t) for t in ext]
             if any(t.size != nr * npoly for t in ex):

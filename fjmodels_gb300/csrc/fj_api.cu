@@ -50,6 +50,11 @@ struct fj_ctx {
     int q_total = 0;                                   // items of the launch whose costs the queue holds
     bool q_costs = false, q_order = false;             // costs recorded / order taken from them
     int q_launches = 0;                                // launches since the order was last taken
+    struct {                                           // Anderson mixing history (fj_anderson_step)
+        int depth = 0;
+        double last = -1;                              // the previous step's change
+        std::vector<std::vector<double>> f, g;         // weighted phil residuals [nt], outputs [3 nt]
+    } anderson;
 };
 
 namespace fj {
@@ -984,6 +989,96 @@ extern "C" int fj_read_out(const char *path, int *nr, int *npoly, int *ngauss, d
 }
 
 // ------------------------------------------------------------ whole model
+extern "C" int fj_anderson_reset(fj_ctx *ctx, int depth)
+{
+    if (!ctx || depth < 0 || depth > FJ_ANDERSON_MAX_DEPTH)
+        return fail(ctx, FJ_ERR_ARG, "anderson_reset: depth must be in [0, FJ_ANDERSON_MAX_DEPTH]");
+    ctx->anderson.depth = depth;
+    ctx->anderson.last = -1;
+    ctx->anderson.f.clear();
+    ctx->anderson.g.clear();
+    return FJ_OK;
+}
+
+// Least squares min |r - sum_j c_j A_j| over the columns A_j (modified Gram-Schmidt;
+// a column whose remaining norm is below 1e-12 of its own is left out, c_j = 0).
+static std::vector<double> lsq_columns(const std::vector<std::vector<double>> &A, const std::vector<double> &r)
+{
+    const int m = (int)A.size(), n = (int)r.size();
+    std::vector<std::vector<double>> Q(A);
+    std::vector<double> R((size_t)m * m, 0.0), c(m, 0.0);
+    std::vector<bool> keep(m, true);
+    for (int j = 0; j < m; j++) {
+        double n0 = 0;
+        for (int i = 0; i < n; i++) n0 += A[j][i] * A[j][i];
+        for (int k = 0; k < j; k++) {
+            if (!keep[k]) continue;
+            double d = 0;
+            for (int i = 0; i < n; i++) d += Q[k][i] * Q[j][i];
+            R[k * m + j] = d;
+            for (int i = 0; i < n; i++) Q[j][i] -= d * Q[k][i];
+        }
+        double nn = 0;
+        for (int i = 0; i < n; i++) nn += Q[j][i] * Q[j][i];
+        if (!(nn > 1e-24 * n0) || nn == 0) { keep[j] = false; continue; }
+        nn = std::sqrt(nn);
+        R[j * m + j] = nn;
+        for (int i = 0; i < n; i++) Q[j][i] /= nn;
+    }
+    std::vector<double> qr(m, 0.0);
+    for (int j = 0; j < m; j++)
+        if (keep[j])
+            for (int i = 0; i < n; i++) qr[j] += Q[j][i] * r[i];
+    for (int j = m - 1; j >= 0; j--) {
+        if (!keep[j]) continue;
+        double v = qr[j];
+        for (int k = j + 1; k < m; k++)
+            if (keep[k]) v -= R[j * m + k] * c[k];
+        c[j] = v / R[j * m + j];
+    }
+    return c;
+}
+
+extern "C" int fj_anderson_step(fj_ctx *ctx, int nr, int npoly, double *x, const double *g, double *change)
+{
+    if (!ctx || nr < 1 || npoly < 1 || !x || !g) return fail(ctx, FJ_ERR_ARG, "anderson_step: bad arguments");
+    const int nt = nr * npoly, n = 3 * nt;
+    std::vector<double> hx(n), hg(n);
+    FJ_CUDA(cudaMemcpyAsync(hx.data(), x, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    FJ_CUDA(cudaMemcpyAsync(hg.data(), g, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    FJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    // the residual as the stopping test weighs it: phil, per radius over |phil(r, 0)|
+    std::vector<double> res(nt);
+    double maxd = 0;
+    for (int i = 0; i < nr; i++)
+        for (int j = 0; j < npoly; j++) {
+            res[i * npoly + j] = (hg[i * npoly + j] - hx[i * npoly + j]) / std::fabs(hg[i * npoly]);
+            maxd = std::fmax(maxd, std::fabs(res[i * npoly + j]));
+        }
+    if (change) *change = maxd;
+    auto &H = ctx->anderson;
+    if (H.last >= 0 && maxd > 2 * H.last) { H.f.clear(); H.g.clear(); }  // diverging: restart from a plain step
+    H.last = maxd;
+    std::vector<double> xn(hg);
+    if (H.depth > 0) {
+        H.f.push_back(res);
+        H.g.push_back(hg);
+        if ((int)H.f.size() > H.depth + 1) { H.f.erase(H.f.begin()); H.g.erase(H.g.begin()); }
+        const int m = (int)H.f.size() - 1;
+        if (m > 0) {
+            std::vector<std::vector<double>> dF(m, std::vector<double>(nt));
+            for (int j = 0; j < m; j++)
+                for (int i = 0; i < nt; i++) dF[j][i] = H.f[j + 1][i] - H.f[j][i];
+            const std::vector<double> c = lsq_columns(dF, res);
+            for (int j = 0; j < m; j++)
+                for (int i = 0; i < n; i++) xn[i] -= c[j] * (H.g[j + 1][i] - H.g[j][i]);
+        }
+    }
+    FJ_CUDA(cudaMemcpyAsync(x, xn.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    FJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    return FJ_OK;
+}
+
 extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_result *res)
 {
     if (!ctx || !cfg || !res || !res->ar || !res->coef6 || !res->phil || !res->Pr || !res->Pr2 || !res->Egrid ||
@@ -998,8 +1093,12 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
     const bool two = cfg->ncomp == 2;
     const bool ref_order = two && cfg->twocomp_order == FJ_TWOCOMP_REFERENCE;
     auto t0 = std::chrono::steady_clock::now();
-    int rc;
+    int rc = FJ_OK;
     if (cfg->delta_every < 0) return fail(ctx, FJ_ERR_ARG, "run_model: delta_every must be >= 0");
+    if (cfg->accel < 0 || cfg->accel > FJ_ANDERSON_MAX_DEPTH)
+        return fail(ctx, FJ_ERR_ARG, "run_model: accel must be in [0, FJ_ANDERSON_MAX_DEPTH]");
+    const int accel = cfg->accel;
+    if (accel && (rc = fj_anderson_reset(ctx, accel))) return rc;
     const bool ext = cfg->ext_phil || cfg->ext_Pr || cfg->ext_Pr2;
     if (ext && !(cfg->ext_phil && cfg->ext_Pr && cfg->ext_Pr2))
         return fail(ctx, FJ_ERR_ARG, "run_model: an external potential needs ext_phil, ext_Pr and ext_Pr2");
@@ -1100,6 +1199,7 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
         res->kernel_ms += st.kernel_ms;
     };
     int k = 0;
+    bool confirmed = false;
     for (k = 0; k < cfg->itermax; k++) {
         fj_moment_stats st;
         const fj_potential pot{nr, npl, d_ar, cur, cur + nt, cur + 2 * nt};
@@ -1141,12 +1241,22 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
             for (int j = 0; j < npl; j++)
                 maxd = fmax(maxd, fabs((neu[i * npl + j] - old[i * npl + j]) / neu[i * npl]));
         res->last_change = maxd;
-        old.swap(neu);
-        std::swap(cur, nxt);
-        if (cfg->tol > 0 && maxd < cfg->tol) { k++; break; }
-        if (cfg->delta_every > 0 && (k + 1) % cfg->delta_every == 0 && k + 1 < cfg->itermax &&
-            (rc = tabulate(cur)))
-            return rc;
+        const bool below = cfg->tol > 0 && maxd < cfg->tol;
+        if (!accel || below || k + 1 >= cfg->itermax) {  // a plain step: the next input is this output
+            old.swap(neu);
+            std::swap(cur, nxt);
+            if (below && (!accel || confirmed)) { k++; break; }
+            confirmed = below;  // mixed: a change below tol is confirmed by one plain step
+        } else {                // mixed: the next input from the last outputs
+            if ((rc = fj_anderson_step(ctx, nr, npl, cur, nxt, nullptr))) return rc;
+            FJ_CUDA(cudaMemcpyAsync(old.data(), cur, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+            FJ_CUDA(cudaStreamSynchronize(s));
+            confirmed = false;
+        }
+        if (cfg->delta_every > 0 && (k + 1) % cfg->delta_every == 0 && k + 1 < cfg->itermax) {
+            if ((rc = tabulate(cur))) return rc;
+            if (accel && (rc = fj_anderson_reset(ctx, accel))) return rc;  // a new map: a new history
+        }
     }
     res->iterations = k;
     const fj_potential pot{nr, npl, d_ar, cur, cur + nt, cur + 2 * nt};
@@ -1183,9 +1293,9 @@ extern "C" int fj_run_model_batch(fj_ctx *ctx, int n, const fj_model_config *cfg
         if (c.ncomp == 2 && c.twocomp_order != FJ_TWOCOMP_SUMMED)
             return fail(ctx, FJ_ERR_ARG, "run_model_batch: two components in the summed order (the reference's "
                                          "order is a fj_run_model option)");
-        if (c.ar_in || c.phil_in || c.Pr_in || c.Pr2_in || c.ext_phil || c.ext_Pr || c.ext_Pr2)
-            return fail(ctx, FJ_ERR_ARG, "run_model_batch: restart tables and external potentials are fj_run_model "
-                                         "options");
+        if (c.ar_in || c.phil_in || c.Pr_in || c.Pr2_in || c.ext_phil || c.ext_Pr || c.ext_Pr2 || c.accel)
+            return fail(ctx, FJ_ERR_ARG, "run_model_batch: restart tables, external potentials and Anderson mixing "
+                                         "are fj_run_model options");
         if (c.delta_every != cfgs[0].delta_every || c.delta_every < 0 || c.delta_every > 1 ||
             (c.delta_every && !c.delta_gpu))
             return fail(ctx, FJ_ERR_ARG, "run_model_batch: delta_every is 0 or 1 (with delta_gpu) for all models");
@@ -1435,9 +1545,9 @@ extern "C" int fj_run_model_surrogate(fj_ctx *ctx, const fj_model_config *cfg, c
         sch->exact_last < 0 || sch->audit_stride < 1 || sch->samples < 1 || sch->epochs_first < 1 || sch->epochs < 1)
         return fail(ctx, FJ_ERR_ARG, "run_model_surrogate: needs one DPL component, the mixed rule and a valid schedule");
     if (cfg->ar_in || cfg->phil_in || cfg->Pr_in || cfg->Pr2_in || cfg->delta_gpu || cfg->delta_every ||
-        cfg->ext_phil || cfg->ext_Pr || cfg->ext_Pr2)
-        return fail(ctx, FJ_ERR_ARG, "run_model_surrogate: restart tables and GPU or repeated Delta tables are "
-                                     "fj_run_model options");
+        cfg->ext_phil || cfg->ext_Pr || cfg->ext_Pr2 || cfg->accel)
+        return fail(ctx, FJ_ERR_ARG, "run_model_surrogate: restart tables, GPU or repeated Delta tables and "
+                                     "Anderson mixing are fj_run_model options");
     fj_surrogate_report rp{};
     auto now = [] { return std::chrono::steady_clock::now(); };
     auto ms_since = [](std::chrono::steady_clock::time_point t) {

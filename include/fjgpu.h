@@ -418,6 +418,14 @@ typedef struct fj_model_config {
        the guess and after every iteration); host [nr*npoly] tables, NULL = none.
        A restart's tables are taken as the total.  fj_run_model only. */
     const double *ext_phil, *ext_Pr, *ext_Pr2;
+    /* Anderson mixing of the iteration (no reference counterpart: the reference
+       iterates the plain map, fJmodels.cpp:131-143): 0 = the plain iteration;
+       m in [1, FJ_ANDERSON_MAX_DEPTH] = each next input potential mixed from
+       the last m + 1 outputs (fj_anderson_step).  With tol > 0 the loop ends
+       with a plain step: a change below tol after a mixed step is confirmed by
+       one plain step from that output, whose change must be below tol too.
+       fj_run_model only. */
+    int accel;
 } fj_model_config;
 
 /* Two-component iteration order.  SUMMED: both components' moments in the
@@ -445,6 +453,22 @@ typedef struct fj_model_result {
 } fj_model_result;
 
 int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_result *res);
+
+/* Anderson mixing of the self-consistent iteration x <- G(x) over the
+   potential tables (no reference counterpart).  The context keeps the history
+   of one iteration: fj_anderson_reset starts it with depth m (0 = plain steps).
+   fj_anderson_step takes the device tables x (the input of the last
+   computeNewPhi, [3][nr*npoly]: phil, Pr, Pr2) and g (its output), sets
+   *change (may be NULL) to the plain step's change max|g_phil - x_phil| /
+   |g_phil(r, 0)| (fj_run_model's stopping test) and overwrites x with the next
+   input: g - sum_j gamma_j (g_{j+1} - g_j) over the last m + 1 outputs, gamma
+   the least-squares fit of the residual by the residual differences (the
+   residual weighted as the stopping test).  The history restarts (a plain
+   step, x = g) when the change grew by more than a factor 2.  Host work and
+   two small copies on the context's stream; synchronous. */
+#define FJ_ANDERSON_MAX_DEPTH 8
+int fj_anderson_reset(fj_ctx *ctx, int depth);
+int fj_anderson_step(fj_ctx *ctx, int nr, int npoly, double *x, const double *g, double *change);
 
 /* n models iterated together (no reference counterpart): one- and
    two-component models (the latter in the summed order, FJ_TWOCOMP_SUMMED:
