@@ -109,6 +109,9 @@ def parse():
                     help="c2: the bench line (NFW 80x40); c3: a two-component model (64x32, 15 iterations); "
                          "c4: a batched sweep of seeded models (extra measurements, not the bench line)")
     ap.add_argument("--models", type=int, default=256, help="c4: number of models")
+    ap.add_argument("--loop-study", action="store_true",
+                    help="the workload's loop to convergence in the mixed form: the plain loop and the Anderson-mixed "
+                         "loops of depth 1, 2, 3, 5 against the fixed point (the plain loop run 42 times); no bench line")
     return ap.parse_args()
 
 
@@ -412,10 +415,31 @@ def plain_at(F, env, tabs_host, iters):
                     f"(plain_value_chosen_loop: x the chosen loop's {iters})"}
 
 
-def run_model_host(F, ctx, form, itermax, accel=0):
+def run_model_host(F, ctx, form, itermax, accel=0, tol=None):
     x, w = velocity_rule()
     return ctx.run_model(CFG["nr"], CFG["ngauss"], CFG["npoly"], CFG["rmin"], CFG["rmax"], df_params(F),
-                         make_rule(F, form, x, w), itermax=itermax, tol=CFG["tol"], accel=accel)
+                         make_rule(F, form, x, w), itermax=itermax, tol=CFG["tol"] if tol is None else tol, accel=accel)
+
+
+def loop_study(args):
+    """Iterations and distance to the fixed point of each loop (mixed form): the potential
+    (max |dphil| / |phil(r, 0)|) and the density multipoles (relative to each shell's
+    monopole, with the shell of the largest difference)."""
+    import fjmodels_gb300 as F
+    ctx = new_context(F, 0)
+    ctx.set_mixed_config(*[int(v) for v in (args.mixed_config or "7,1024").split(",")])
+    fixed = run_model_host(F, ctx, "mixed", 42, tol=0.0)
+    rows = {"fixed_point": {"iterations": fixed["iterations"], "last_change": fixed["last_change"]}}
+    s0, rho0 = np.abs(fixed["phil"][:, :1]), fixed["coef6"][0]
+    for m in (0, 1, 2, 3, 5):
+        r = run_model_host(F, ctx, "mixed", CFG["itermax"], accel=m)
+        e = np.abs(r["coef6"][0] - rho0) / np.abs(rho0[:, :1])
+        rows["plain" if m == 0 else f"anderson{m}"] = {
+            "iterations": r["iterations"], "last_change": r["last_change"],
+            "potential": float(np.max(np.abs(r["phil"] - fixed["phil"]) / s0)),
+            "density_multipoles": float(np.max(e)), "worst_shell": int(np.unravel_index(np.argmax(e), e.shape)[0])}
+    ctx.close()
+    print(json.dumps({"loop_study": rows, "workload": WORKLOAD, "tol": CFG["tol"]}))
 
 
 def e2e_ours(args, mixed_cfg=None):
@@ -592,6 +616,8 @@ def workload_c4(args):
 def main():
     args = parse()
     POISSON["mode"] = args.poisson
+    if args.loop_study:
+        return loop_study(args)
     if args.profile_points:
         profile_case(args)
         return
