@@ -66,7 +66,7 @@ class fj_model_config(C.Structure):
                 ("mass2", C.c_double), ("r0_2", C.c_double), ("q2", C.c_double), ("df2", fj_df_params),
                 ("twocomp_order", C.c_int), ("ar_in", DP), ("phil_in", DP), ("Pr_in", DP), ("Pr2_in", DP),
                 ("delta_gpu", C.c_int), ("delta_every", C.c_int), ("ext_phil", DP), ("ext_Pr", DP), ("ext_Pr2", DP),
-                ("accel", C.c_int)]
+                ("accel", C.c_int), ("accel_beta", C.c_double)]
 
 
 class fj_model_result(C.Structure):
@@ -83,7 +83,7 @@ CTX = C.c_void_p
 SIGNATURES = {
     "fj_version": ([], C.c_char_p),
     "fj_ctx_create": ([C.c_int, P(C.c_void_p)], C.c_int),
-    "fj_anderson_reset": ([CTX, C.c_int], C.c_int),
+    "fj_anderson_reset": ([CTX, C.c_int, C.c_double], C.c_int),
     "fj_anderson_step": ([CTX, C.c_int, C.c_int, C.c_void_p, C.c_void_p, DP], C.c_int),
     "fj_ctx_destroy": ([CTX], C.c_int),
     "fj_ctx_set_stream": ([CTX, C.c_void_p], C.c_int),

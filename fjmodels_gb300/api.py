@@ -396,9 +396,10 @@ class Context:
         return dict(zip(("KRR", "Kzz", "WRR", "Wzz", "pot", "mass_pr", "mass_sum"), out))
 
     # ---------------------------------------------------------------- whole model
-    def anderson_reset(self, depth):
-        """Start a new mixed iteration with history depth m (fj_anderson_reset; 0 = plain steps)."""
-        self._check(self.lib.fj_anderson_reset(self.h, int(depth)), "fj_anderson_reset")
+    def anderson_reset(self, depth, beta=1.0):
+        """Start a new mixed iteration with history depth m and mixing factor beta
+        (fj_anderson_reset; depth 0 = plain steps)."""
+        self._check(self.lib.fj_anderson_reset(self.h, int(depth), float(beta)), "fj_anderson_reset")
 
     def anderson_step(self, x, g):
         """One Anderson step (fj_anderson_step): x, g are contiguous device tensors [3][nr][npoly]
@@ -414,7 +415,7 @@ class Context:
 
     def run_model(self, nr, ngauss, npoly, rmin, rmax, df, rule, itermax, tol=0.0, ngrid=30, q=1.0,
                   keep_grids=False, delta_table=None, df2=None, q2=1.0, twocomp_order=A.FJ_TWOCOMP_SUMMED,
-                  restart=None, delta_gpu=False, delta_every=0, ext=None, accel=0):
+                  restart=None, delta_gpu=False, delta_every=0, ext=None, accel=0, accel_beta=1.0):
         """Self-consistent model (oneComp, fJmodels.cpp:86-144; with df2, the two-component
         loop of fJmodels.cpp:38-84 in `twocomp_order`) with host buffers.
         delta_table = (Egrid, Dgrid) uses a given focal-distance table instead of tabulating one;
@@ -424,14 +425,15 @@ class Context:
         again from the new potential after every k-th iteration (the reference: once).
         ext = (phil, Pr, Pr2) of a fixed external potential added after the guess and after every
         iteration (the reference's external mode, fJmodels.cpp:120-125, 134).
-        accel = m > 0 mixes each next input potential from the last m + 1 outputs (Anderson;
-        the reference iterates the plain map); with tol the loop then ends with a confirming
-        plain step."""
+        accel = m > 0 mixes each next input potential from the last m + 1 outputs (Anderson,
+        mixing factor accel_beta; the reference iterates the plain map); with tol the loop then
+        ends with a confirming plain step."""
         self.use_own_stream()
         din = [None, None] if delta_table is None else [_f64(delta_table[0]), _f64(delta_table[1])]
         cfg = A.fj_model_config(nr, ngauss, npoly, ngrid, rmin, rmax, A.FJ_GUESS.get(df.model, 0), df.mass, df.r0,
                                 q, df.c, rule.c, itermax, tol, *[_dp(d) if d is not None else None for d in din])
         cfg.delta_gpu, cfg.delta_every, cfg.accel = int(delta_gpu), int(delta_every), int(accel)
+        cfg.accel_beta = float(accel_beta)
         if ext is not None:
             ex = [_f64(t) for t in ext]
             if any(t.size != nr * npoly for t in ex):

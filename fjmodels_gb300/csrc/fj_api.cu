@@ -52,8 +52,9 @@ struct fj_ctx {
     int q_launches = 0;                                // launches since the order was last taken
     struct {                                           // Anderson mixing history (fj_anderson_step)
         int depth = 0;
+        double beta = 1;                               // mixing factor (1: the next input is the mixed output)
         double last = -1;                              // the previous step's change
-        std::vector<std::vector<double>> f, g;         // weighted phil residuals [nt], outputs [3 nt]
+        std::vector<std::vector<double>> f, g, x;      // weighted phil residuals [nt], outputs, inputs [3 nt]
     } anderson;
 };
 
@@ -989,14 +990,16 @@ extern "C" int fj_read_out(const char *path, int *nr, int *npoly, int *ngauss, d
 }
 
 // ------------------------------------------------------------ whole model
-extern "C" int fj_anderson_reset(fj_ctx *ctx, int depth)
+extern "C" int fj_anderson_reset(fj_ctx *ctx, int depth, double beta)
 {
-    if (!ctx || depth < 0 || depth > FJ_ANDERSON_MAX_DEPTH)
-        return fail(ctx, FJ_ERR_ARG, "anderson_reset: depth must be in [0, FJ_ANDERSON_MAX_DEPTH]");
+    if (!ctx || depth < 0 || depth > FJ_ANDERSON_MAX_DEPTH || !(beta > 0 && beta <= 4))
+        return fail(ctx, FJ_ERR_ARG, "anderson_reset: depth in [0, FJ_ANDERSON_MAX_DEPTH] and beta in (0, 4]");
     ctx->anderson.depth = depth;
+    ctx->anderson.beta = beta;
     ctx->anderson.last = -1;
     ctx->anderson.f.clear();
     ctx->anderson.g.clear();
+    ctx->anderson.x.clear();
     return FJ_OK;
 }
 
@@ -1057,22 +1060,35 @@ extern "C" int fj_anderson_step(fj_ctx *ctx, int nr, int npoly, double *x, const
         }
     if (change) *change = maxd;
     auto &H = ctx->anderson;
-    if (H.last >= 0 && maxd > 2 * H.last) { H.f.clear(); H.g.clear(); }  // diverging: restart from a plain step
+    if (H.last >= 0 && maxd > 2 * H.last) { H.f.clear(); H.g.clear(); H.x.clear(); }  // diverging: restart
     H.last = maxd;
     std::vector<double> xn(hg);
     if (H.depth > 0) {
+        const bool relax = H.beta != 1;
         H.f.push_back(res);
         H.g.push_back(hg);
-        if ((int)H.f.size() > H.depth + 1) { H.f.erase(H.f.begin()); H.g.erase(H.g.begin()); }
+        if (relax) H.x.push_back(hx);
+        if ((int)H.f.size() > H.depth + 1) {
+            H.f.erase(H.f.begin());
+            H.g.erase(H.g.begin());
+            if (relax) H.x.erase(H.x.begin());
+        }
         const int m = (int)H.f.size() - 1;
+        std::vector<double> xbar(hx);
         if (m > 0) {
             std::vector<std::vector<double>> dF(m, std::vector<double>(nt));
             for (int j = 0; j < m; j++)
                 for (int i = 0; i < nt; i++) dF[j][i] = H.f[j + 1][i] - H.f[j][i];
             const std::vector<double> c = lsq_columns(dF, res);
             for (int j = 0; j < m; j++)
-                for (int i = 0; i < n; i++) xn[i] -= c[j] * (H.g[j + 1][i] - H.g[j][i]);
+                for (int i = 0; i < n; i++) {
+                    xn[i] -= c[j] * (H.g[j + 1][i] - H.g[j][i]);
+                    if (relax) xbar[i] -= c[j] * (H.x[j + 1][i] - H.x[j][i]);
+                }
         }
+        // beta != 1: the mixed input plus beta times the mixed residual
+        if (relax)
+            for (int i = 0; i < n; i++) xn[i] = xbar[i] + H.beta * (xn[i] - xbar[i]);
     }
     FJ_CUDA(cudaMemcpyAsync(x, xn.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     FJ_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1098,7 +1114,10 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
     if (cfg->accel < 0 || cfg->accel > FJ_ANDERSON_MAX_DEPTH)
         return fail(ctx, FJ_ERR_ARG, "run_model: accel must be in [0, FJ_ANDERSON_MAX_DEPTH]");
     const int accel = cfg->accel;
-    if (accel && (rc = fj_anderson_reset(ctx, accel))) return rc;
+    if (!(cfg->accel_beta >= 0 && cfg->accel_beta <= 4))
+        return fail(ctx, FJ_ERR_ARG, "run_model: accel_beta must be in [0, 4] (0: 1)");
+    const double beta = cfg->accel_beta > 0 ? cfg->accel_beta : 1.0;
+    if (accel && (rc = fj_anderson_reset(ctx, accel, beta))) return rc;
     const bool ext = cfg->ext_phil || cfg->ext_Pr || cfg->ext_Pr2;
     if (ext && !(cfg->ext_phil && cfg->ext_Pr && cfg->ext_Pr2))
         return fail(ctx, FJ_ERR_ARG, "run_model: an external potential needs ext_phil, ext_Pr and ext_Pr2");
@@ -1255,7 +1274,7 @@ extern "C" int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_re
         }
         if (cfg->delta_every > 0 && (k + 1) % cfg->delta_every == 0 && k + 1 < cfg->itermax) {
             if ((rc = tabulate(cur))) return rc;
-            if (accel && (rc = fj_anderson_reset(ctx, accel))) return rc;  // a new map: a new history
+            if (accel && (rc = fj_anderson_reset(ctx, accel, beta))) return rc;  // a new map: a new history
         }
     }
     res->iterations = k;

@@ -426,6 +426,7 @@ typedef struct fj_model_config {
        one plain step from that output, whose change must be below tol too.
        fj_run_model only. */
     int accel;
+    double accel_beta;           /* the mixing factor of fj_anderson_reset, (0, 4]; 0 = 1 */
 } fj_model_config;
 
 /* Two-component iteration order.  SUMMED: both components' moments in the
@@ -456,18 +457,21 @@ int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_result *res);
 
 /* Anderson mixing of the self-consistent iteration x <- G(x) over the
    potential tables (no reference counterpart).  The context keeps the history
-   of one iteration: fj_anderson_reset starts it with depth m (0 = plain steps).
+   of one iteration: fj_anderson_reset starts it with depth m (0 = plain steps)
+   and mixing factor beta in (0, 4].
    fj_anderson_step takes the device tables x (the input of the last
    computeNewPhi, [3][nr*npoly]: phil, Pr, Pr2) and g (its output), sets
    *change (may be NULL) to the plain step's change max|g_phil - x_phil| /
    |g_phil(r, 0)| (fj_run_model's stopping test) and overwrites x with the next
-   input: g - sum_j gamma_j (g_{j+1} - g_j) over the last m + 1 outputs, gamma
-   the least-squares fit of the residual by the residual differences (the
-   residual weighted as the stopping test).  The history restarts (a plain
-   step, x = g) when the change grew by more than a factor 2.  Host work and
-   two small copies on the context's stream; synchronous. */
+   input: with gbar = g - sum_j gamma_j (g_{j+1} - g_j) over the last m + 1
+   outputs and xbar the same combination of the inputs, gamma the
+   least-squares fit of the residual by the residual differences (the
+   residual weighted as the stopping test), x = xbar + beta (gbar - xbar)
+   (beta = 1: x = gbar).  The history restarts when the change grew by more
+   than a factor 2 (that step then has no history: x + beta (g - x)).  Host
+   work and two small copies on the context's stream; synchronous. */
 #define FJ_ANDERSON_MAX_DEPTH 8
-int fj_anderson_reset(fj_ctx *ctx, int depth);
+int fj_anderson_reset(fj_ctx *ctx, int depth, double beta);
 int fj_anderson_step(fj_ctx *ctx, int nr, int npoly, double *x, const double *g, double *change);
 
 /* n models iterated together (no reference counterpart): one- and

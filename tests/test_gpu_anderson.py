@@ -46,6 +46,18 @@ def test_anderson_linear_map(ctx):
     g = (xs + rate * (x - xs)).contiguous()
     ctx.anderson_step(x, g)
     assert torch.equal(x, g)
+    # mixing factor 1.6: the same fixed point (host reference of the same step: 1e-15 by the 8th)
+    x = torch.zeros_like(xs)
+    x[0, :, 0] = -1.0
+    ctx.anderson_reset(2, 1.6)
+    x0 = x.clone()
+    g = (xs + rate * (x - xs)).contiguous()
+    ctx.anderson_step(x, g)
+    assert torch.allclose(x, x0 + 1.6 * (g - x0), rtol=0, atol=1e-15)  # no history: x + beta (g - x)
+    for _ in range(9):
+        g = (xs + rate * (x - xs)).contiguous()
+        ch = ctx.anderson_step(x, g)
+    assert ch < 1e-12 and float((x - xs).abs().max()) < 1e-12
 
 
 def test_anderson_restarts_when_diverging(ctx):
@@ -69,6 +81,9 @@ def test_anderson_arguments(ctx):
         ctx.anderson_reset(A.FJ_ANDERSON_MAX_DEPTH + 1)
     with pytest.raises(F.FJError):
         ctx.anderson_reset(-1)
+    for beta in (0.0, -1.0, 4.5):
+        with pytest.raises(F.FJError):
+            ctx.anderson_reset(2, beta)
     x = torch.zeros((3, 4, 2), dtype=torch.float64, device="cuda")
     with pytest.raises(F.FJError):
         ctx.anderson_step(x, torch.zeros((3, 4, 3), dtype=torch.float64, device="cuda"))
@@ -109,6 +124,12 @@ def test_run_model_accel_reaches_the_fixed_point(cumulative):
           f"plain phil {pp:.2e} rho {pr:.2e}, mixed phil {mp:.2e} rho {mr:.2e}")
     assert mp < 1e-4 and mr < 1e-4
     assert mp <= 1.2 * pp + 1e-9 and mr <= 1.2 * pr + 1e-9
+    # the bench's setting: mixing factor 1.6
+    relaxed = ctx.run_model(*args, itermax=60, tol=1e-5, accel=2, accel_beta=1.6)
+    rp, rr = dist(relaxed)
+    print(f"mixed, beta 1.6: {relaxed['iterations']} iterations, phil {rp:.2e} rho {rr:.2e}")
+    assert relaxed["last_change"] < 1e-5 and relaxed["iterations"] < plain["iterations"]
+    assert rp <= 1.2 * pp + 1e-9 and rr <= 1.2 * pr + 1e-9
 
 
 def test_run_model_accel_range(ctx):
@@ -117,3 +138,5 @@ def test_run_model_accel_range(ctx):
     rule = F.Rule(F.XPT11, F.XW11, precision=A.FJ_PREC_MIXED)
     with pytest.raises(F.FJError, match="accel"):
         ctx.run_model(24, 8, 4, 0.01, 100.0, df, rule, itermax=2, accel=A.FJ_ANDERSON_MAX_DEPTH + 1)
+    with pytest.raises(F.FJError, match="accel_beta"):
+        ctx.run_model(24, 8, 4, 0.01, 100.0, df, rule, itermax=2, accel=2, accel_beta=5.0)
