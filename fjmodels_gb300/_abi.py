@@ -85,6 +85,9 @@ SIGNATURES = {
     "fj_ctx_create": ([C.c_int, P(C.c_void_p)], C.c_int),
     "fj_anderson_reset": ([CTX, C.c_int, C.c_double], C.c_int),
     "fj_anderson_step": ([CTX, C.c_int, C.c_int, C.c_void_p, C.c_void_p, DP], C.c_int),
+    "fj_anderson_create": ([C.c_int, C.c_double, P(C.c_void_p)], C.c_int),
+    "fj_anderson_destroy": ([C.c_void_p], C.c_int),
+    "fj_anderson_host_step": ([C.c_void_p, C.c_int, C.c_int, DP, DP, DP], C.c_int),
     "fj_ctx_destroy": ([CTX], C.c_int),
     "fj_ctx_set_stream": ([CTX, C.c_void_p], C.c_int),
     "fj_ctx_own_stream": ([CTX], C.c_void_p),

@@ -607,6 +607,45 @@ def readParam(path="param.txt"):
     return p, comps
 
 
+class Anderson:
+    """Anderson mixing of a self-consistent loop on host tables (fj_anderson_create /
+    fj_anderson_host_step; no device work): depth m, mixing factor beta.  step(x, g) takes
+    float64 arrays [3][nr][npoly] (phil, Pr, Pr2) of the last input and its output, overwrites
+    x with the next input and returns the plain step's change max|dphil| / |phil(r, 0)|."""
+
+    def __init__(self, depth, beta=1.0):
+        self.lib = A.load()
+        h = C.c_void_p()
+        rc = self.lib.fj_anderson_create(int(depth), float(beta), C.byref(h))
+        if rc != A.FJ_OK:
+            raise FJError(f"fj_anderson_create: depth in [0, {A.FJ_ANDERSON_MAX_DEPTH}] and beta in (0, 4]")
+        self.h = h
+
+    def step(self, x, g):
+        if not (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous and x.ndim == 3
+                and x.shape[0] == 3):
+            raise FJError("Anderson.step: x must be a contiguous float64 array [3][nr][npoly]")
+        g = _f64(g)
+        if g.shape != x.shape:
+            raise FJError("Anderson.step: x and g differ in shape")
+        ch = np.zeros(1)
+        rc = self.lib.fj_anderson_host_step(self.h, x.shape[1], x.shape[2], _dp(x), _dp(g), _dp(ch))
+        if rc != A.FJ_OK:
+            raise FJError(f"fj_anderson_host_step failed ({rc})")
+        return float(ch[0])
+
+    def close(self):
+        if self.h:
+            self.lib.fj_anderson_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Surrogate:
     """The action surrogate (fj_surrogate_*): MLP 16 -> 128 x 4 (GELU) -> 16 on the tensor
     cores, outputs 0 and 1 = (log Jr, log Jz) of normalised features."""

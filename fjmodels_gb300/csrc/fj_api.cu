@@ -11,6 +11,7 @@
 #include <cstring>
 #include <fstream>
 #include <map>
+#include <new>
 #include <string>
 #include <thread>
 #include <vector>
@@ -27,6 +28,14 @@ using namespace fj;
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
+};
+
+// The history of one Anderson-mixed iteration (fj_anderson_step, fj_anderson_host_step)
+struct fj_anderson {
+    int depth = 0;
+    double beta = 1;                               // mixing factor (1: the next input is the mixed output)
+    double last = -1;                              // the previous step's change
+    std::vector<std::vector<double>> f, g, x;      // weighted phil residuals [nt], outputs, inputs [3 nt]
 };
 
 struct fj_ctx {
@@ -50,12 +59,7 @@ struct fj_ctx {
     int q_total = 0;                                   // items of the launch whose costs the queue holds
     bool q_costs = false, q_order = false;             // costs recorded / order taken from them
     int q_launches = 0;                                // launches since the order was last taken
-    struct {                                           // Anderson mixing history (fj_anderson_step)
-        int depth = 0;
-        double beta = 1;                               // mixing factor (1: the next input is the mixed output)
-        double last = -1;                              // the previous step's change
-        std::vector<std::vector<double>> f, g, x;      // weighted phil residuals [nt], outputs, inputs [3 nt]
-    } anderson;
+    fj_anderson anderson;                              // the mixing history of fj_anderson_step
 };
 
 namespace fj {
@@ -990,16 +994,34 @@ extern "C" int fj_read_out(const char *path, int *nr, int *npoly, int *ngauss, d
 }
 
 // ------------------------------------------------------------ whole model
+static bool anderson_args_ok(int depth, double beta)
+{
+    return depth >= 0 && depth <= FJ_ANDERSON_MAX_DEPTH && beta > 0 && beta <= 4;
+}
+
 extern "C" int fj_anderson_reset(fj_ctx *ctx, int depth, double beta)
 {
-    if (!ctx || depth < 0 || depth > FJ_ANDERSON_MAX_DEPTH || !(beta > 0 && beta <= 4))
+    if (!ctx || !anderson_args_ok(depth, beta))
         return fail(ctx, FJ_ERR_ARG, "anderson_reset: depth in [0, FJ_ANDERSON_MAX_DEPTH] and beta in (0, 4]");
+    ctx->anderson = fj_anderson{};
     ctx->anderson.depth = depth;
     ctx->anderson.beta = beta;
-    ctx->anderson.last = -1;
-    ctx->anderson.f.clear();
-    ctx->anderson.g.clear();
-    ctx->anderson.x.clear();
+    return FJ_OK;
+}
+
+extern "C" int fj_anderson_create(int depth, double beta, fj_anderson **out)
+{
+    if (!out || !anderson_args_ok(depth, beta)) return FJ_ERR_ARG;
+    *out = new (std::nothrow) fj_anderson;
+    if (!*out) return FJ_ERR_NOMEM;
+    (*out)->depth = depth;
+    (*out)->beta = beta;
+    return FJ_OK;
+}
+
+extern "C" int fj_anderson_destroy(fj_anderson *a)
+{
+    delete a;
     return FJ_OK;
 }
 
@@ -1042,14 +1064,12 @@ static std::vector<double> lsq_columns(const std::vector<std::vector<double>> &A
     return c;
 }
 
-extern "C" int fj_anderson_step(fj_ctx *ctx, int nr, int npoly, double *x, const double *g, double *change)
+// One mixing step on host tables: hx the last input, hg its output ([3][nr*npoly]
+// each), xn the next input; *change (may be NULL) the plain step's change.
+static void anderson_update(fj_anderson &H, int nr, int npoly, const std::vector<double> &hx,
+                            const std::vector<double> &hg, std::vector<double> &xn, double *change)
 {
-    if (!ctx || nr < 1 || npoly < 1 || !x || !g) return fail(ctx, FJ_ERR_ARG, "anderson_step: bad arguments");
     const int nt = nr * npoly, n = 3 * nt;
-    std::vector<double> hx(n), hg(n);
-    FJ_CUDA(cudaMemcpyAsync(hx.data(), x, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    FJ_CUDA(cudaMemcpyAsync(hg.data(), g, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    FJ_CUDA(cudaStreamSynchronize(ctx->stream));
     // the residual as the stopping test weighs it: phil, per radius over |phil(r, 0)|
     std::vector<double> res(nt);
     double maxd = 0;
@@ -1059,10 +1079,9 @@ extern "C" int fj_anderson_step(fj_ctx *ctx, int nr, int npoly, double *x, const
             maxd = std::fmax(maxd, std::fabs(res[i * npoly + j]));
         }
     if (change) *change = maxd;
-    auto &H = ctx->anderson;
     if (H.last >= 0 && maxd > 2 * H.last) { H.f.clear(); H.g.clear(); H.x.clear(); }  // diverging: restart
     H.last = maxd;
-    std::vector<double> xn(hg);
+    xn = hg;
     if (H.depth > 0) {
         const bool relax = H.beta != 1;
         H.f.push_back(res);
@@ -1090,8 +1109,29 @@ extern "C" int fj_anderson_step(fj_ctx *ctx, int nr, int npoly, double *x, const
         if (relax)
             for (int i = 0; i < n; i++) xn[i] = xbar[i] + H.beta * (xn[i] - xbar[i]);
     }
+}
+
+extern "C" int fj_anderson_step(fj_ctx *ctx, int nr, int npoly, double *x, const double *g, double *change)
+{
+    if (!ctx || nr < 1 || npoly < 1 || !x || !g) return fail(ctx, FJ_ERR_ARG, "anderson_step: bad arguments");
+    const int n = 3 * nr * npoly;
+    std::vector<double> hx(n), hg(n), xn;
+    FJ_CUDA(cudaMemcpyAsync(hx.data(), x, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    FJ_CUDA(cudaMemcpyAsync(hg.data(), g, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    FJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    anderson_update(ctx->anderson, nr, npoly, hx, hg, xn, change);
     FJ_CUDA(cudaMemcpyAsync(x, xn.data(), n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     FJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    return FJ_OK;
+}
+
+extern "C" int fj_anderson_host_step(fj_anderson *a, int nr, int npoly, double *x, const double *g, double *change)
+{
+    if (!a || nr < 1 || npoly < 1 || !x || !g) return FJ_ERR_ARG;
+    const int n = 3 * nr * npoly;
+    std::vector<double> hx(x, x + n), hg(g, g + n), xn;
+    anderson_update(*a, nr, npoly, hx, hg, xn, change);
+    std::copy(xn.begin(), xn.end(), x);
     return FJ_OK;
 }
 

@@ -474,6 +474,16 @@ int fj_run_model(fj_ctx *ctx, const fj_model_config *cfg, fj_model_result *res);
 int fj_anderson_reset(fj_ctx *ctx, int depth, double beta);
 int fj_anderson_step(fj_ctx *ctx, int nr, int npoly, double *x, const double *g, double *change);
 
+/* The same mixing without a context, on host tables (a loop that keeps the
+   potential on the host, as the reference's does): fj_anderson_create(m,
+   beta, &a) holds one iteration's history; fj_anderson_host_step(a, nr,
+   npoly, x, g, &change) as fj_anderson_step with host x and g.  No device
+   work; FJ_ERR_ARG for bad arguments. */
+typedef struct fj_anderson fj_anderson;
+int fj_anderson_create(int depth, double beta, fj_anderson **out);
+int fj_anderson_destroy(fj_anderson *a);
+int fj_anderson_host_step(fj_anderson *a, int nr, int npoly, double *x, const double *g, double *change);
+
 /* n models iterated together (no reference counterpart): one- and
    two-component models (the latter in the summed order, FJ_TWOCOMP_SUMMED:
    both components' grids in the one launch), per iteration one
