@@ -1,0 +1,67 @@
+"""The mixed-precision node solve compiled for the host (tests/host_mixed.cpp over
+fjmodels_gb300/csrc/fj_mixed.cuh, the source the GPU kernel compiles) against the oracle
+(the reference's algorithm in FP64) on the golden Hernquist fixture: the mixed form's gate,
+1e-4 relative on the density and the dispersions, vrot on the dispersion's scale.  Runs on
+the CPU, so the FP32 restatement is checked without a GPU.  The GPU solves the nodes whose
+FP32 solve hits a cap again in FP64; the host build keeps their FP32 estimate (about one
+bound node in 4 000 on this fixture) and is held to the same gate."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import fjmodels_gb300 as F
+from tests.conftest import load_golden
+from tests.helpers import oracle_model, rel
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+MIXED_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def host_mixed(tmp_path_factory):
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    exe = tmp_path_factory.mktemp("host_mixed") / "host_mixed"
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I", os.path.join(ROOT, "fjmodels_gb300", "csrc"),
+                    os.path.join(ROOT, "tests", "host_mixed.cpp"), "-o", str(exe)], check=True)
+    return exe
+
+
+def _run(exe, tmp_path, ar, tabs, E, D, xq, wq, pts, df):
+    nr, npl = tabs[0].shape
+    path = tmp_path / "in.bin"
+    with open(path, "wb") as f:
+        np.array([nr, npl, len(E), len(xq), len(pts)], dtype=np.int32).tofile(f)
+        for a in (ar, *tabs, E, D, xq, wq, np.asarray(pts).ravel()):
+            np.ascontiguousarray(a, dtype=np.float64).tofile(f)
+        c = df.c
+        np.array([c.kind, c.alpha, c.beta, c.J0, c.mass, c.dphi_h, c.dz_h, c.dphi_g, c.dz_g, c.chi, c.k],
+                 dtype=np.float64).tofile(f)
+    out = subprocess.run([str(exe), str(path)], check=True, capture_output=True, text=True).stdout.split("\n")
+    mom = np.array([[float(v) for v in l.split()] for l in out if l and not l.startswith("capped")])
+    capped = int(next(l for l in out if l.startswith("capped")).split()[1])
+    return mom, capped
+
+
+def test_host_mixed_vs_oracle(host_mixed, tmp_path):
+    g, meta, _ = load_golden("hern_dpl")
+    nr, ng, npl = meta["nr"], meta["ng"], meta["np"]
+    tabs = [g[k].reshape(nr, npl) for k in ("guess_phil", "guess_Pr", "guess_Pr2")]
+    p = meta["p"]
+    df = F.DFParams(p["model"], p["dphi_h"], p["dz_h"], p["dphi_g"], p["dz_g"], p["chi"], p["mass"], p["r0"],
+                    k=meta["k"])
+    ci, _ = F.gauleg(0, 1, ng)
+    pts = [(g["ar"][n] * np.sqrt(1 - c * c), g["ar"][n] * c) for n in range(0, nr, 3) for c in ci]
+    mom, capped = _run(host_mixed, tmp_path, g["ar"], tabs, g["Egrid"], g["Dgrid"], F.XPT11, F.XW11, pts, df)
+    m = oracle_model(g, meta, *tabs)
+    ref = np.array([m.rhofDF(R, z)[0] for R, z in pts])
+    print(f"{len(pts)} points, {capped} capped nodes; rho {rel(mom[:, 0], ref[:, 0]):.2e}, "
+          f"sigmas {rel(mom[:, [2, 3, 4]], ref[:, [2, 3, 4]]):.2e}")
+    assert capped < 1e-3 * len(pts) * len(F.XPT11) ** 3
+    assert rel(mom[:, 0], ref[:, 0]) < MIXED_TOL
+    assert rel(mom[:, [2, 3, 4]], ref[:, [2, 3, 4]]) < MIXED_TOL
+    assert np.max(np.abs(mom[:, 1] - ref[:, 1]) / ref[:, 3]) < MIXED_TOL
