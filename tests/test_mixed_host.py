@@ -1,6 +1,6 @@
 """The mixed-precision node solve compiled for the host (tests/host_mixed.cpp over
 fjmodels_gb300/csrc/fj_mixed.cuh, the source the GPU kernel compiles) against the oracle
-(the reference's algorithm in FP64) on the golden Hernquist fixture: the mixed form's gate,
+(the reference's algorithm in FP64) on the golden Hernquist and rotating NFW fixtures: the mixed form's gate,
 1e-4 relative on the density and the dispersions, vrot on the dispersion's scale.  Runs on
 the CPU, so the FP32 restatement is checked without a GPU.  The GPU solves the nodes whose
 FP32 solve hits a cap again in FP64; the host build keeps their FP32 estimate (about one
@@ -47,15 +47,18 @@ def _run(exe, tmp_path, ar, tabs, E, D, xq, wq, pts, df):
     return mom, capped
 
 
-def test_host_mixed_vs_oracle(host_mixed, tmp_path):
-    g, meta, _ = load_golden("hern_dpl")
+@pytest.mark.parametrize("name,stride", [("hern_dpl", 3), ("nfw_dpl_rot", 4)])
+def test_host_mixed_vs_oracle(host_mixed, tmp_path, name, stride):
+    """Every stride-th radius x the 4 polar nodes of the fixture's guess potential; the NFW
+    fixture has the rotating DF (chi = 1, k = 0.5) of the bench workload."""
+    g, meta, _ = load_golden(name)
     nr, ng, npl = meta["nr"], meta["ng"], meta["np"]
     tabs = [g[k].reshape(nr, npl) for k in ("guess_phil", "guess_Pr", "guess_Pr2")]
     p = meta["p"]
     df = F.DFParams(p["model"], p["dphi_h"], p["dz_h"], p["dphi_g"], p["dz_g"], p["chi"], p["mass"], p["r0"],
                     k=meta["k"])
     ci, _ = F.gauleg(0, 1, ng)
-    pts = [(g["ar"][n] * np.sqrt(1 - c * c), g["ar"][n] * c) for n in range(0, nr, 3) for c in ci]
+    pts = [(g["ar"][n] * np.sqrt(1 - c * c), g["ar"][n] * c) for n in range(0, nr, stride) for c in ci]
     mom, capped = _run(host_mixed, tmp_path, g["ar"], tabs, g["Egrid"], g["Dgrid"], F.XPT11, F.XW11, pts, df)
     m = oracle_model(g, meta, *tabs)
     ref = np.array([m.rhofDF(R, z)[0] for R, z in pts])
